@@ -1,0 +1,340 @@
+"""Benchmark of the GB300 Henon step: star-updates/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--N stars]
+
+Workload (N = 1 GPU): King W0 = 6 cluster, N = 1e6 stars, Kroupa (2001) IMF
+masses, single stars, FP64 plain step (sort -> potential -> relaxation -> new
+orbits, with the time step, Stodolkiewicz energy conservation and tidal
+stripping between them), seeded synthetic input.  One "step" is one whole
+Henon step of every star; one star-update is one star carried through it.
+The state (about 250 bytes/star, 250 MB) is larger than the 129 MB L2, so
+every step streams from HBM; no explicit L2 flush is needed.
+
+--impl reference times the reference's algorithm on the host cores instead:
+the CPU restatement in oracle/ (the reference itself needs MPI, GSL and HDF5,
+which this image lacks), with the reference's own taus113 generator, one
+process per core on bounded samples of the same model.
+
+Under torchrun each rank steps its own replica (replicas only: the path has
+no data exchange between independent clusters) and value is the sum over
+ranks of star-updates divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "cmc-cosmic_gb300"))
+
+METRIC = "star-updates/s per Henon step"
+UNIT = "star-updates/s"
+# algorithmic HBM bytes per star for each kernel family (compulsory FP64 SoA
+# traffic: reads + writes of the fields the phase consumes and produces)
+ALG_BYTES = {"sort": 116, "potential": 24, "relax": 72, "orbit": 80, "ec3": 72, "energy": 56,
+             "timestep": 24, "tidal": 16, "begin": 0, "end": 0}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend=backend)
+    return rank, ws, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def make_model(N: int, seed: int):
+    import cmcgpu
+
+    return cmcgpu.generate(cmcgpu.KING, N, seed=seed, w0=6.0, imf=1)
+
+
+# ------------------------------------------------------------- CPU legs ---
+def _ref_worker(args):
+    """One host core: the oracle (reference algorithm, taus113 draws) stepping a
+    bounded sample of the workload's model; returns (stars*steps, seconds)."""
+    n, steps, warmup, seed = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "cmc-cosmic_gb300"))
+    import oracle
+
+    ic = make_model(n, seed)
+    o = oracle.Oracle(ic, oracle.default_params(orbit_r=ic["rtid"], seed=seed, draw_mode=oracle.DRAW_TAUS113))
+    o.initialize()
+    for _ in range(warmup):
+        o.step()
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(steps):
+        done += o.nstars()
+        o.step()
+    return done, time.perf_counter() - t0
+
+
+def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int):
+    import multiprocessing as mp
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_ref_worker, [(n_sample, steps, warmup, 1000 + i) for i in range(procs)])
+    updates = sum(r[0] for r in res)
+    secs = max(r[1] for r in res)
+    return updates / secs, secs
+
+
+# ------------------------------------------------------------ GPU leg ----
+def run_ours(a, rank, ws, dist):
+    import numpy as np
+
+    import cmcgpu
+
+    cmcgpu.build()
+    N = a.N
+    ic = make_model(N, seed=20240607 + rank)
+    p = cmcgpu.default_params(orbit_r=ic["rtid"], seed=cmcgpu.derive_seed(777, rank))
+    ctx = cmcgpu.Context([N], p)
+    ctx.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    ctx.initialize()
+    ctx.step(a.warmup)
+    ctx.check_device("warmup")
+    n_start = ctx.nstars()
+
+    # ---- device-resident timed region
+    import torch
+
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    time.sleep(0.6)
+    ctx.profile(True)
+    ctx.kernel_time("reset")
+    barrier(dist)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    launches = 0
+    for _ in range(a.steps):
+        ctx.step(1)
+        launches += ctx.launch_count()
+    ctx.synchronize()
+    dt = time.perf_counter() - t0
+    barrier(dist)
+    clk = clocks.stop()
+    ctx.check_device("timed steps")
+    fam = {}
+    for name in ALG_BYTES:
+        ms, n = ctx.kernel_time(name)
+        fam[name] = (ms, n)
+    ctx.profile(False)
+    step_ms = sum(v[0] for v in fam.values()) / a.steps
+    dt_max = allreduce_max(dist, dt)
+    updates = allreduce_sum(dist, float(n_start * a.steps))
+    value = updates / dt_max
+    top = max((k for k in fam if ALG_BYTES[k] > 0), key=lambda k: fam[k][0])
+    ms_top, n_top = fam[top]
+    peak, peak_kind = measured_peak()
+    achieved = ALG_BYTES[top] * n_start / (ms_top / n_top * 1e-3) / 1e9
+    per_family = {k: {"ms_per_step": round(v[0] / a.steps, 4), "launches": v[1]} for k, v in fam.items() if v[1]}
+
+    # ---- end to end: host buffers in pinned memory, copies inside the timed region
+    cap = N + 16
+    bufs = {k: torch.empty(cap, dtype=torch.float64, pin_memory=True).numpy() for k in ("r", "m", "vr", "vt", "E", "J")}
+    bufs["id"] = torch.empty(cap, dtype=torch.int64, pin_memory=True).numpy()
+    n_host = ctx.get_stars(0, bufs)
+    h2d = d2h = 0
+    barrier(dist)
+    t1 = time.perf_counter()
+    e2e_updates = 0
+    for _ in range(a.steps):
+        ctx.put_stars(0, n_host, bufs)
+        h2d += n_host * 7 * 8
+        e2e_updates += n_host
+        ctx.step(1)
+        n_host = ctx.get_stars(0, bufs)
+        d2h += n_host * 7 * 8
+    e2e_dt = time.perf_counter() - t1
+    barrier(dist)
+    ctx.check_device("e2e steps")
+    e2e_value = allreduce_sum(dist, float(e2e_updates)) / allreduce_max(dist, e2e_dt)
+
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": dt_max / a.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded King W0=6 model, Kroupa 2001 IMF; no dataset)",
+        "config": {"workload": f"King W0=6, Kroupa IMF, N={N}, plain FP64 Henon step", "N": N,
+                   "stars_at_start": n_start, "parallelism": f"replicas x{ws}",
+                   "l2": "state ~250 B/star exceeds the 129 MB L2 at this N: no flush needed"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // a.steps,
+                "d2h_bytes_per_step": d2h // a.steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "alg_bytes_per_star": ALG_BYTES[top], "ms_per_launch": ms_top / n_top},
+        "kernels": per_family,
+        "kernel_ms_per_step": step_ms,
+        "clocks": clk,
+    }
+    ctx.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--N", type=int, default=1_000_000)
+    ap.add_argument("--cpu-sample", type=int, default=100_000, help="stars per CPU-baseline process")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    if a.warmup < 3:
+        a.warmup = 3
+    rank, ws, local, dist = dist_setup()
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        procs = min(os.cpu_count() or 1, 16)
+        val, secs = cpu_baseline(a.cpu_sample, a.steps, a.warmup, procs)
+        out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+               "ms_per_step": secs / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "impl": "reference",
+               "data": "synthetic (seeded King W0=6 model, Kroupa 2001 IMF)",
+               "config": {"workload": f"King W0=6, Kroupa IMF, N={a.N}, plain FP64 Henon step", "N": a.N},
+               "cpu_baseline": {"value": val, "unit": UNIT, "cores": procs, "kind": "port",
+                                "sample": f"{procs} processes x {a.cpu_sample}-star King W0=6 Kroupa clusters, "
+                                          f"{a.steps} timed steps each (reference algorithm, taus113 draws)"},
+               "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+
+    out = run_ours(a, rank, ws, dist)
+    if rank == 0:
+        if not a.no_cpu_baseline and ws == 1:
+            val, secs = cpu_baseline(a.cpu_sample, 1, 0, 1)
+            out["cpu_baseline"] = {"value": val, "unit": UNIT, "cores": 1, "kind": "port",
+                                   "sample": f"one {a.cpu_sample}-star King W0=6 Kroupa cluster, 1 step "
+                                             f"({secs:.1f} s; reference algorithm with taus113 draws, 1 core)"}
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

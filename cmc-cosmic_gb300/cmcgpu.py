@@ -1,0 +1,310 @@
+"""Python binding of libcmcgpu.so (include/cmcgpu.h) over ctypes.
+
+This module mirrors the reference's step-level interface for tests and the
+benchmark: a :class:`Context` holds one or more clusters resident on the GPU and
+exposes the main-loop phases under the reference's names (``dynamics_apply``,
+``new_orbits_calculate``, ``qsorts_new``, ``calc_potential`` ...).  Errors
+raised on the device come back as :class:`CmcError` with the code of the
+reference's ``exit_cleanly`` site they mirror.
+
+There is no CPU fallback: constructing a Context without a usable GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libcmcgpu.so")
+HEADER = os.path.join(os.path.dirname(_HERE), "include", "cmcgpu.h")
+
+ERRORS = {
+    -1: "bad argument", -2: "CUDA error", -3: "capacity exceeded", -4: "out of device memory",
+    -5: "bad state", 1: "NaN in mass sum", 2: "NaN in potential", 3: "W = 0 in encounter",
+    4: "wp = 0 in deflection", 5: "N_TRY exceeded", 6: "vr^2 is NaN", 7: "no sign change of vr^2",
+    8: "apsis root not converged", 9: "negative residual at apsis", 10: "radius search failed",
+    11: "radius outside interval", 12: "strong encounter drawn", 20: "bounded wait gave up",
+    21: "tidal stripping did not settle",
+}
+
+
+class CmcError(RuntimeError):
+    def __init__(self, code: int, where: str = "", index: int = -1):
+        self.code = code
+        self.index = index
+        super().__init__(f"{where}: {ERRORS.get(code, 'error')} (code {code}, index {index})")
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("N_STAR", C.c_long), ("AVEKERNEL", C.c_long), ("GAMMA", C.c_double), ("THETASEMAX", C.c_double),
+        ("PERTURB", C.c_int), ("RELAXATION", C.c_int), ("TIDALLY_STRIP_STARS", C.c_int),
+        ("TIDAL_TREATMENT", C.c_int), ("orbit_r", C.c_double), ("cenma_m", C.c_double),
+        ("apsides_max_iter", C.c_long), ("apsides_precision", C.c_double),
+        ("apsides_convergence", C.c_double), ("n_try", C.c_long), ("seed", C.c_uint64),
+        ("relax_fp32", C.c_int),
+    ]
+
+
+class ICSpec(C.Structure):
+    _fields_ = [("model", C.c_int), ("N", C.c_long), ("w0", C.c_double), ("imf", C.c_int),
+                ("binary_fraction", C.c_double), ("seed", C.c_uint64)]
+
+
+class ICOut(C.Structure):
+    _fields_ = [("r", C.POINTER(C.c_double)), ("m", C.POINTER(C.c_double)), ("vr", C.POINTER(C.c_double)),
+                ("vt", C.POINTER(C.c_double)), ("id", C.POINTER(C.c_int64)), ("rtid", C.c_double)]
+
+
+PLUMMER, KING = 0, 1
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("cmcg_build", os.path.join(_HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib() -> C.CDLL:
+    """Load the in-tree shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run cmc-cosmic_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        vp, d, i, l = C.c_void_p, C.c_double, C.c_int, C.c_long
+        L.cmcg_default_params.argtypes = [C.POINTER(Params)]
+        L.cmcg_create.argtypes = [C.POINTER(vp), i, C.POINTER(l), C.POINTER(Params)]
+        L.cmcg_destroy.argtypes = [vp]
+        L.cmcg_load.argtypes = [vp, i, l, vp, vp, vp, vp, vp]
+        for name in ["cmcg_initialize", "cmcg_begin_step", "cmcg_calc_timestep", "cmcg_new_orbits_calculate",
+                     "cmcg_tidally_strip_stars", "cmcg_qsorts_new", "cmcg_calc_potential",
+                     "cmcg_energy_conservation3", "cmcg_compute_energy", "cmcg_end_step", "cmcg_step",
+                     "cmcg_synchronize"]:
+            getattr(L, name).argtypes = [vp]
+        L.cmcg_dynamics_apply.argtypes = [vp, d]
+        L.cmcg_run.argtypes = [vp, i]
+        L.cmcg_use_graph.argtypes = [vp, i]
+        L.cmcg_profile.argtypes = [vp, i]
+        L.cmcg_kernel_time.argtypes = [vp, C.c_char_p, C.POINTER(d), C.POINTER(l)]
+        L.cmcg_potential.argtypes = [vp, i, d, C.POINTER(d)]
+        L.cmcg_get_field.argtypes = [vp, i, C.c_char_p, vp, l]
+        L.cmcg_get_field.restype = l
+        L.cmcg_set_field.argtypes = [vp, i, C.c_char_p, vp, l]
+        L.cmcg_set_field.restype = l
+        L.cmcg_get_ids.argtypes = [vp, i, vp, l]
+        L.cmcg_get_ids.restype = l
+        L.cmcg_get_scalar.argtypes = [vp, i, C.c_char_p, C.POINTER(d)]
+        L.cmcg_set_scalar.argtypes = [vp, i, C.c_char_p, d]
+        L.cmcg_nstars.argtypes = [vp, i]
+        L.cmcg_nstars.restype = l
+        L.cmcg_last_error.argtypes = [vp, C.POINTER(i), C.POINTER(l)]
+        L.cmcg_launch_count.argtypes = [vp]
+        L.cmcg_launch_count.restype = l
+        L.cmcg_ic_generate.argtypes = [C.POINTER(ICSpec), C.POINTER(ICOut)]
+        L.cmcg_derive_seed.argtypes = [C.c_uint64, C.c_uint64]
+        L.cmcg_derive_seed.restype = C.c_uint64
+        L.cmcg_draw.argtypes = [C.c_uint64, l, i, C.c_int64, C.c_uint32, i]
+        L.cmcg_draw.restype = d
+        L.cmcg_put_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
+        L.cmcg_get_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
+        L.cmcg_get_stars.restype = l
+        _lib = L
+    return _lib
+
+
+def header_symbols(path: str = HEADER) -> list[str]:
+    """Function names the public header declares."""
+    text = open(path).read()
+    return sorted(set(re.findall(r"\b(cmcg_[a-z0-9_]+)\s*\(", text)))
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().cmcg_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def generate(model: int, N: int, seed: int, w0: float = 6.0, imf: int = 0, binary_fraction: float = 0.0):
+    """Seeded synthetic cluster in N-body units; returns dict of arrays + rtid."""
+    a = {k: np.zeros(N) for k in ("r", "m", "vr", "vt")}
+    ids = np.zeros(N, np.int64)
+    out = ICOut(*[a[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("r", "m", "vr", "vt")],
+                ids.ctypes.data_as(C.POINTER(C.c_int64)), 0.0)
+    rc = lib().cmcg_ic_generate(C.byref(ICSpec(model, N, w0, imf, binary_fraction, seed)), C.byref(out))
+    if rc:
+        raise CmcError(rc, "cmcg_ic_generate")
+    a["id"] = ids
+    a["rtid"] = out.rtid
+    return a
+
+
+def derive_seed(master: int, index: int) -> int:
+    return int(lib().cmcg_derive_seed(master, index))
+
+
+def draw(seed: int, tcount: int, site: int, star_id: int, n: int, word: int) -> float:
+    return float(lib().cmcg_draw(seed, tcount, site, star_id, n, word))
+
+
+class Context:
+    """Clusters resident on the GPU; phases run all of them in one launch each."""
+
+    def __init__(self, capacities, params):
+        if isinstance(params, Params):
+            params = [params] * len(capacities)
+        self.n = len(capacities)
+        caps = (C.c_long * self.n)(*capacities)
+        ps = (Params * self.n)(*params)
+        self._h = C.c_void_p()
+        rc = lib().cmcg_create(C.byref(self._h), self.n, caps, ps)
+        if rc:
+            raise CmcError(rc, "cmcg_create")
+        self.params = list(params)
+
+    def close(self):
+        if self._h:
+            lib().cmcg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- data
+    def load(self, cluster: int, r, m, vr, vt, ids=None):
+        r, m, vr, vt = (np.ascontiguousarray(x, dtype=np.float64) for x in (r, m, vr, vt))
+        idp = None
+        if ids is not None:
+            ids = np.ascontiguousarray(ids, dtype=np.int64)
+            idp = ids.ctypes.data
+        self._check(lib().cmcg_load(self._h, cluster, len(r), r.ctypes.data, m.ctypes.data, vr.ctypes.data,
+                                    vt.ctypes.data, idp), "cmcg_load")
+
+    def _check(self, rc, where):
+        if rc:
+            raise CmcError(rc, where)
+
+    def check_device(self, where="device"):
+        c, idx = C.c_int(-1), C.c_long(-1)
+        rc = lib().cmcg_last_error(self._h, C.byref(c), C.byref(idx))
+        if rc:
+            raise CmcError(rc, f"{where} (cluster {c.value})", idx.value)
+
+    def get(self, name: str, cluster: int = 0) -> np.ndarray:
+        n = self.nstars(cluster) + 2
+        out = np.zeros(max(n, 1))
+        got = lib().cmcg_get_field(self._h, cluster, name.encode(), out.ctypes.data, len(out))
+        if got < 0:
+            raise KeyError(name)
+        return out[:got].copy()
+
+    def set(self, name: str, values, cluster: int = 0):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if lib().cmcg_set_field(self._h, cluster, name.encode(), v.ctypes.data, len(v)) < 0:
+            raise KeyError(name)
+
+    def ids(self, cluster: int = 0) -> np.ndarray:
+        n = self.nstars(cluster)
+        out = np.zeros(max(n, 1), np.int64)
+        got = lib().cmcg_get_ids(self._h, cluster, out.ctypes.data, len(out))
+        return out[:got].copy()
+
+    def scalar(self, name: str, cluster: int = 0) -> float:
+        v = C.c_double()
+        self._check(lib().cmcg_get_scalar(self._h, cluster, name.encode(), C.byref(v)), f"scalar {name}")
+        return v.value
+
+    def set_scalar(self, name: str, value: float, cluster: int = 0):
+        self._check(lib().cmcg_set_scalar(self._h, cluster, name.encode(), float(value)), f"set_scalar {name}")
+
+    def nstars(self, cluster: int = 0) -> int:
+        return int(lib().cmcg_nstars(self._h, cluster))
+
+    def potential(self, r: float, cluster: int = 0) -> float:
+        v = C.c_double()
+        self._check(lib().cmcg_potential(self._h, cluster, float(r), C.byref(v)), "potential")
+        return v.value
+
+    # -- phases (reference names)
+    def initialize(self):
+        self._check(lib().cmcg_initialize(self._h), "initialize")
+
+    def begin_step(self):
+        self._check(lib().cmcg_begin_step(self._h), "begin_step")
+
+    def calc_timestep(self):
+        self._check(lib().cmcg_calc_timestep(self._h), "calc_timestep")
+
+    def dynamics_apply(self, dt: float = -1.0):
+        self._check(lib().cmcg_dynamics_apply(self._h, dt), "dynamics_apply")
+
+    def new_orbits_calculate(self):
+        self._check(lib().cmcg_new_orbits_calculate(self._h), "new_orbits_calculate")
+
+    def tidally_strip_stars(self):
+        self._check(lib().cmcg_tidally_strip_stars(self._h), "tidally_strip_stars")
+
+    def qsorts_new(self):
+        self._check(lib().cmcg_qsorts_new(self._h), "qsorts_new")
+
+    def calc_potential(self):
+        self._check(lib().cmcg_calc_potential(self._h), "calc_potential")
+
+    def energy_conservation3(self):
+        self._check(lib().cmcg_energy_conservation3(self._h), "energy_conservation3")
+
+    def compute_energy(self):
+        self._check(lib().cmcg_compute_energy(self._h), "compute_energy")
+
+    def end_step(self):
+        self._check(lib().cmcg_end_step(self._h), "end_step")
+
+    def step(self, n: int = 1):
+        self._check(lib().cmcg_run(self._h, n), "run")
+
+    def use_graph(self, on: bool = True):
+        self._check(lib().cmcg_use_graph(self._h, 1 if on else 0), "use_graph")
+
+    def profile(self, on: bool = True):
+        self._check(lib().cmcg_profile(self._h, 1 if on else 0), "profile")
+
+    def kernel_time(self, family: str):
+        ms, n = C.c_double(), C.c_long()
+        self._check(lib().cmcg_kernel_time(self._h, family.encode(), C.byref(ms), C.byref(n)), "kernel_time")
+        return ms.value, n.value
+
+    def synchronize(self):
+        self._check(lib().cmcg_synchronize(self._h), "synchronize")
+
+    def launch_count(self) -> int:
+        return int(lib().cmcg_launch_count(self._h))
+
+    def put_stars(self, cluster: int, n: int, bufs: dict):
+        """Upload host star state (arrays r, m, vr, vt, E, J, id; m already x N_STAR)."""
+        a = [bufs[k].ctypes.data for k in ("r", "m", "vr", "vt", "E", "J", "id")]
+        self._check(lib().cmcg_put_stars(self._h, cluster, n, *a), "put_stars")
+
+    def get_stars(self, cluster: int, bufs: dict) -> int:
+        cap = len(bufs["r"])
+        a = [bufs[k].ctypes.data for k in ("r", "m", "vr", "vt", "E", "J", "id")]
+        n = lib().cmcg_get_stars(self._h, cluster, cap, *a)
+        if n < 0:
+            raise CmcError(int(n), "get_stars")
+        return int(n)

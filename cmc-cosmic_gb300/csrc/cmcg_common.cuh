@@ -1,0 +1,79 @@
+// cmcg_common.cuh -- launch geometry and deterministic block reductions.
+#pragma once
+#include "cmcg_internal.cuh"
+
+namespace cmcg {
+
+// Table of tiles for one tile size: tiles[b] = (cluster, tile-in-cluster);
+// first[c], count[c] give cluster c's contiguous range of table entries.
+struct Tiles {
+    const int2 *tiles;
+    const int *first;
+    const int *count;
+    int ntiles;
+};
+
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *smem /* >= NT/32 */)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) smem[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NT / 32; ++i) s = __dadd_rn(s, smem[i]);
+    }
+    return s;  // valid in thread 0
+}
+
+template <int NT>
+__device__ __forceinline__ double block_max(double v, double *smem)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) smem[w] = v;
+    __syncthreads();
+    double s = -INFINITY;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NT / 32; ++i) s = fmax(s, smem[i]);
+    }
+    return s;
+}
+
+template <int NT>
+__device__ __forceinline__ long long block_sum_ll(long long v, long long *smem)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) smem[w] = v;
+    __syncthreads();
+    long long s = 0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NT / 32; ++i) s += smem[i];
+    }
+    return s;
+}
+
+// Last-block-done protocol.  Thread 0 of every block calls this after writing
+// its partials; it returns true in exactly one block per cluster (the last to
+// arrive), which may then read all of that cluster's partials.
+__device__ __forceinline__ bool arrive_last(unsigned int *ticket, int count)
+{
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    if (t == (unsigned int)(count - 1)) {
+        __threadfence();
+        *ticket = 0u;  // reset for the next launch
+        return true;
+    }
+    return false;
+}
+
+}  // namespace cmcg

@@ -1,0 +1,191 @@
+// cmcg_energy.cu -- step bookkeeping on the device.
+//
+// k_begin_step   cmc.c:246-257 (tallies of the previous step move to *_old)
+// k_ec3 + k_ec3_fix   set_velocities3 (cmc_utils.c:254-349).  The per-star
+//     prediction v_new^2 = vold^2 + (Uoldrold - Uoldrnew) + (Unewrold - Unewrnew)
+//     and the velocity rescaling are independent per star (k_ec3).  Only the
+//     "excess energy" carried from stars whose prediction is unphysical to the
+//     stars after them is sequential; such stars are rare, so k_ec3 records
+//     them in a list and k_ec3_fix replays exactly the reference's sequential
+//     loop from each of them until the excess is used up.
+// k_energy       compute_energy_new + ComputeEnergy (cmc_utils.c:2018-2028, 604-656)
+// k_end_step     tcount++, Prev_Dt (cmc.c:294, 390)
+#include "cmcg_kernels.cuh"
+#include "cmcgpu.h"
+
+namespace cmcg {
+
+
+static __device__ __forceinline__ double sqr(double x) { return x * x; }
+
+__global__ void k_begin_step(const Cluster *__restrict__ cls, int nclusters)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nclusters) return;
+    Scalars *sc = cls[c].sc;
+    sc->Eescaped_old = sc->Eescaped;
+    sc->Jescaped_old = sc->Jescaped;
+    sc->TidalMassLoss_old = sc->TidalMassLoss;
+    sc->Etidal_old = sc->Etidal;
+    sc->Eescaped = 0.0;
+    sc->Jescaped = 0.0;
+    sc->TidalMassLoss = 0.0;
+    sc->Etidal = 0.0;
+    sc->N_MAX_NEW = sc->N_MAX;
+    sc->tidal_done = cls[c].TIDALLY_STRIP_STARS ? 0 : 1;
+    sc->tidal_iters = 0;
+}
+
+__global__ void k_end_step(const Cluster *__restrict__ cls, int nclusters)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nclusters) return;
+    Scalars *sc = cls[c].sc;
+    sc->Prev_Dt = sc->Dt;
+    sc->tcount += 1;
+}
+
+__global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, Tiles tm, Fields f, Ec3Bufs eb)
+{
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    const long long i = 1 + (long long)ct.y * EC3_T + threadIdx.x;
+    const long long off = C.off, g = off + i;
+    if (i > sc->N_MAX_NEW) return;
+    const double invN = 1.0 / (double)sc->N_STAR;
+    const double m = f.m[g], ri = f.r[g], rold = f.rOld[g];
+    int pok = 1;
+    const double Unewrold = potential_at(f.r + off, f.phi + off, f.inv_r + off, sc->N_MAX, rold, &pok) +
+                            phi_s(rold, ri, m, invN);
+    if (!pok) set_error(sc, CMCG_ERR_FINDZERO_R, i);
+    const double Unewrnew = f.phi[g] + phi_s(ri, ri, m, invN);
+    const double q = 0.5;
+    const double vnew2 = f.ec_pre[g] + 2.0 * q * (Unewrold - Unewrnew);
+    double vr = f.vr[g], vt = f.vt[g];
+    if (vnew2 <= 0.0) {
+        eb.a[g] = 0.5 * (sqr(vr) + sqr(vt) - vnew2) * m;
+        const unsigned int slot = atomicAdd(eb.nlist + ct.x, 1u);
+        if (slot < EXCESS_CAP) eb.list[(size_t)ct.x * EXCESS_CAP + slot] = i;
+    } else {
+        eb.a[g] = -1.0;
+        const double alpha = sqrt(vnew2 / (sqr(vr) + sqr(vt)));
+        vr *= alpha;
+        vt *= alpha;
+        f.vr[g] = vr;
+        f.vt[g] = vt;
+    }
+}
+
+// One thread per cluster replays the sequential excess-energy pass from each
+// listed star in radial order (insertion-sorted list; the full sequential
+// pass if the list overflowed).
+__global__ void k_ec3_fix(const Cluster *__restrict__ cls, Fields f, Ec3Bufs eb, int nclusters)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nclusters) return;
+    const Cluster &C = cls[c];
+    Scalars *sc = C.sc;
+    const long long off = C.off, N = sc->N_MAX_NEW;
+    unsigned int n = eb.nlist[c];
+    eb.nlist[c] = 0u;
+    sc->n_excess = n;
+    if (n == 0) return;
+    const double E_dump_factor = 0.8;
+    long long *L = eb.list + (size_t)c * EXCESS_CAP;
+    const bool overflow = n > EXCESS_CAP;
+    if (!overflow) {
+        for (unsigned int a = 1; a < n; ++a) {  // insertion sort (the list is short)
+            const long long v = L[a];
+            int b = (int)a - 1;
+            while (b >= 0 && L[b] > v) {
+                L[b + 1] = L[b];
+                --b;
+            }
+            L[b + 1] = v;
+        }
+    }
+    double Eexcess = 0.0;
+    unsigned int li = 0;
+    long long i = overflow ? 1 : L[0];
+    while (i <= N) {
+        const long long g = off + i;
+        const double ai = eb.a[g];
+        if (ai >= 0.0) {
+            Eexcess += ai;
+        } else if (Eexcess > 0) {
+            const double m = f.m[g];
+            double vr = f.vr[g], vt = f.vt[g];
+            const double v2 = sqr(vr) + sqr(vt);
+            const double E_dump_capacity = E_dump_factor * 0.5 * m * v2;
+            const double E_dump = (E_dump_capacity <= Eexcess) ? E_dump_capacity : Eexcess;
+            const double exc_ratio = sqrt((v2 - 2 * E_dump / m) / v2);
+            vr *= exc_ratio;
+            vt *= exc_ratio;
+            f.vr[g] = vr;
+            f.vt[g] = vt;
+            Eexcess -= E_dump;
+        }
+        if (overflow) {
+            ++i;
+            continue;
+        }
+        if (ai >= 0.0) ++li;
+        if (Eexcess > 0) {
+            ++i;
+        } else {
+            if (li >= n) break;
+            i = L[li];
+        }
+    }
+    // on one rank the remainder is dropped (cmc_utils.c:313-348)
+}
+
+__global__ void __launch_bounds__(EN_T) k_energy(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                 double *partials, unsigned int *tickets)
+{
+    __shared__ double red[EN_T / 32];
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    const long long N = sc->N_MAX, off = C.off;
+    const long long i = 1 + (long long)ct.y * EN_T + threadIdx.x;
+    const double madhoc = sc->madhoc;
+    double K = 0.0, P = 0.0;
+    if (i <= N) {
+        const long long g = off + i;
+        const double vr = f.vr[g], vt = f.vt[g], ph = f.phi[g], m = f.m[g];
+        f.E[g] = ph + 0.5 * (sqr(vr) + sqr(vt));
+        f.J[g] = f.r[g] * vt;
+        K = 0.5 * (sqr(vr) + sqr(vt)) * m * madhoc;
+        P = ph * m * madhoc;
+        P += f.phi[off] * sc->cenma_m * madhoc / (double)N;
+    }
+    const double tK = block_sum<EN_T>(K, red);
+    const double tP = block_sum<EN_T>(P, red);
+    if (threadIdx.x == 0) {
+        double *slot = partials + (size_t)blockIdx.x * 2;
+        slot[0] = tK;
+        slot[1] = tP;
+        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
+            double aK = 0.0, aP = 0.0;
+            const int b0 = tm.first[ct.x];
+            for (int b = 0; b < tm.count[ct.x]; ++b) {
+                aK += partials[(size_t)(b0 + b) * 2];
+                aP += partials[(size_t)(b0 + b) * 2 + 1];
+            }
+            // compute_energy_new, cmc_utils.c:2020-2025
+            sc->Eescaped += sc->Eescaped_old;
+            sc->Jescaped += sc->Jescaped_old;
+            sc->Etidal += sc->Etidal_old;
+            aP *= 0.5;
+            sc->KE = aK;
+            sc->PE = aP;
+            double tot = aK + aP + 0.0 + 0.0;
+            tot += sc->cenma_E + sc->Eescaped + 0.0 + 0.0;
+            sc->Etot = tot;
+        }
+    }
+}
+
+}  // namespace cmcg

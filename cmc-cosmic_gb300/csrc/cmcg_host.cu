@@ -1,0 +1,883 @@
+// cmcg_host.cu -- the C ABI of include/cmcgpu.h: context, device memory,
+// launch geometry, the step sequence and CUDA-graph capture.
+//
+// Memory: one arena per context (a single cudaMalloc at creation), carved into
+// the structure-of-arrays fields, the sort/scan scratch and the per-tile
+// partial sums.  Nothing is allocated while stepping.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cmcg_kernels.cuh"
+#include "cmcgpu.h"
+
+using namespace cmcg;
+
+namespace {
+
+struct TileTable {
+    int2 *d_tiles = nullptr;
+    int *d_first = nullptr, *d_count = nullptr;
+    int ntiles = 0;
+    std::vector<int> first, count;
+    Tiles view() const { return Tiles{d_tiles, d_first, d_count, ntiles}; }
+};
+
+enum Family { F_BEGIN, F_TIMESTEP, F_RELAX, F_ORBIT, F_TIDAL, F_SORT, F_POT, F_EC3, F_ENERGY, F_END, F_COUNT };
+const char *kFamilyNames[F_COUNT] = {"begin", "timestep", "relax", "orbit", "tidal",
+                                     "sort",  "potential", "ec3", "energy", "end"};
+
+struct ProfRec {
+    int fam;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct cmcg_ctx {
+    int ncl = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<long long> cap, off;
+    long long total = 0;
+    std::vector<cmcg_params> params;
+    std::vector<Cluster> h_cls;
+    Cluster *d_cls = nullptr;
+    Scalars *d_sc = nullptr;
+    Fields f{};
+    double *partials = nullptr;
+    unsigned int *tickets = nullptr;
+    SortBufs sb{};
+    PotBufs pb{};
+    Ec3Bufs eb{};
+    double *d_query = nullptr;
+    TileTable t128, t256, t1024, t2048, t5120;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+    int relax_fp32 = 0;
+    // graphs
+    bool use_graph = false, graph_ready = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    long launches = 0, launches_last = 0;
+    // profiling
+    bool profile = false;
+    std::vector<ProfRec> prof;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_next = 0;
+    double fam_ms[F_COUNT] = {0};
+    long fam_n[F_COUNT] = {0};
+    int cur_fam = -1;
+    cudaEvent_t cur_a = nullptr;
+};
+
+#define CK(x)                                                                                    \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess) {                                                                 \
+            fprintf(stderr, "cmcgpu: %s failed: %s (%s:%d)\n", #x, cudaGetErrorString(e_), __FILE__, \
+                    __LINE__);                                                                   \
+            return CMCG_ERR_CUDA;                                                                \
+        }                                                                                        \
+    } while (0)
+
+static cudaEvent_t take_event(cmcg_ctx *c)
+{
+    if (c->ev_next >= c->ev_pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c->ev_pool.push_back(e);
+    }
+    return c->ev_pool[c->ev_next++];
+}
+
+static void fam_begin(cmcg_ctx *c, int fam)
+{
+    if (!c->profile) return;
+    c->cur_fam = fam;
+    c->cur_a = take_event(c);
+    cudaEventRecord(c->cur_a, c->stream);
+}
+
+static void fam_end(cmcg_ctx *c)
+{
+    if (!c->profile || c->cur_fam < 0) return;
+    cudaEvent_t b = take_event(c);
+    cudaEventRecord(b, c->stream);
+    c->prof.push_back(ProfRec{c->cur_fam, c->cur_a, b});
+    c->cur_fam = -1;
+}
+
+static int build_table(TileTable &t, const std::vector<long long> &cap, int T, std::vector<int2> &host)
+{
+    const int n = (int)cap.size();
+    t.first.assign(n, 0);
+    t.count.assign(n, 0);
+    host.clear();
+    for (int c = 0; c < n; ++c) {
+        long long k = (cap[c] + T - 1) / T;
+        if (k < 1) k = 1;
+        t.first[c] = (int)host.size();
+        t.count[c] = (int)k;
+        for (long long i = 0; i < k; ++i) host.push_back(make_int2(c, (int)i));
+    }
+    t.ntiles = (int)host.size();
+    return 0;
+}
+
+namespace {
+struct Carver {
+    char *base;
+    size_t used = 0;
+    template <class T>
+    T *take(size_t n)
+    {
+        used = (used + 255) & ~(size_t)255;
+        T *p = base ? (T *)(base + used) : nullptr;
+        used += n * sizeof(T);
+        return p;
+    }
+};
+}  // namespace
+
+static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *bytes)
+{
+    Carver cv{base};
+    const size_t tot = (size_t)c->total;
+    Fields &f = c->f;
+    double **dfields[] = {&f.r,     &f.m,     &f.phi,    &f.inv_r, &f.vr,     &f.vt,     &f.E,      &f.J,
+                          &f.vr_rel, &f.vt_rel, &f.rnew, &f.vrnew, &f.vtnew,  &f.X,      &f.Y,      &f.r_peri,
+                          &f.r_apo, &f.ec_pre, &f.rOld, &f.sigma_r, &f.sigma, &f.r2,     &f.m2,     &f.ec_pre2};
+    for (double **p : dfields) *p = cv.take<double>(tot);
+    f.id = cv.take<long long>(tot);
+    f.id2 = cv.take<long long>(tot);
+    c->sb.keys[0] = cv.take<unsigned long long>(tot);
+    c->sb.keys[1] = cv.take<unsigned long long>(tot);
+    c->sb.vals[0] = cv.take<unsigned int>(tot);
+    c->sb.vals[1] = cv.take<unsigned int>(tot);
+    size_t hist_total = 0;
+    for (int k = 0; k < c->ncl; ++k) hist_total += (size_t)RADIX * c->t2048.count[k];
+    c->sb.hist = cv.take<unsigned int>(hist_total);
+    c->sb.digit_total = cv.take<unsigned int>((size_t)c->ncl * RADIX);
+    c->sb.hist_off = cv.take<long long>(c->ncl);
+    c->sb.npass = cv.take<int>(c->ncl);
+    c->sb.kmin = cv.take<unsigned long long>(c->ncl);
+    c->sb.kmax = cv.take<unsigned long long>(c->ncl);
+    c->pb.q = cv.take<double>(tot);
+    c->pb.agg = cv.take<double>((size_t)c->t1024.ntiles * 4);
+    c->pb.carry = cv.take<double>((size_t)c->t1024.ntiles * 2);
+    c->eb.a = cv.take<double>(tot);
+    c->eb.list = cv.take<long long>((size_t)c->ncl * EXCESS_CAP);
+    c->eb.nlist = cv.take<unsigned int>(c->ncl);
+    size_t np = 0;
+    np = std::max(np, (size_t)c->t256.ntiles * RELAX_NPART);
+    np = std::max(np, (size_t)c->t128.ntiles * ORB_NPART);
+    np = std::max(np, (size_t)c->t2048.ntiles * 4);
+    np = std::max(np, (size_t)c->t256.ntiles * 2);
+    np = std::max(np, (size_t)c->t5120.ntiles * 1);
+    c->partials = cv.take<double>(np);
+    c->tickets = cv.take<unsigned int>(c->ncl);
+    c->d_sc = cv.take<Scalars>(c->ncl);
+    c->d_cls = cv.take<Cluster>(c->ncl);
+    c->d_query = cv.take<double>(2);
+    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t5120};
+    for (int i = 0; i < 5; ++i) {
+        tts[i]->d_tiles = cv.take<int2>(tabs[i].size());
+        tts[i]->d_first = cv.take<int>(c->ncl);
+        tts[i]->d_count = cv.take<int>(c->ncl);
+    }
+    *bytes = cv.used + 256;
+    return 0;
+}
+
+extern "C" {
+
+void cmcg_default_params(cmcg_params *p)
+{
+    memset(p, 0, sizeof(*p));
+    p->N_STAR = 0;
+    p->AVEKERNEL = 20;
+    p->GAMMA = 0.1;
+    p->THETASEMAX = 1.412;
+    p->PERTURB = 1;
+    p->RELAXATION = 1;
+    p->TIDALLY_STRIP_STARS = 1;
+    p->TIDAL_TREATMENT = 1;
+    p->orbit_r = 1.0e6;
+    p->cenma_m = 0.0;
+    p->apsides_max_iter = 100;
+    p->apsides_precision = 1.0e-11;
+    p->apsides_convergence = 5.0e-13;
+    p->n_try = 50000;
+    p->seed = 0;
+    p->relax_fp32 = 0;
+}
+
+int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_params *params)
+{
+    if (!out || nclusters < 1 || !capacity || !params) return CMCG_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        fprintf(stderr, "cmcgpu: no CUDA device available; this library has no CPU fallback\n");
+        return CMCG_ERR_CUDA;
+    }
+    for (int k = 0; k < nclusters; ++k) {
+        if (capacity[k] < 1) return CMCG_ERR_ARG;
+        if (params[k].AVEKERNEL < 1 || params[k].AVEKERNEL > PMAX) return CMCG_ERR_ARG;
+        if (params[k].relax_fp32 != params[0].relax_fp32) return CMCG_ERR_ARG;
+    }
+    cmcg_ctx *c = new cmcg_ctx();
+    c->ncl = nclusters;
+    c->relax_fp32 = params[0].relax_fp32;
+    c->params.assign(params, params + nclusters);
+    c->cap.resize(nclusters);
+    c->off.resize(nclusters);
+    long long tot = 0;
+    for (int k = 0; k < nclusters; ++k) {
+        c->cap[k] = capacity[k];
+        c->off[k] = tot;
+        long long stride = ((capacity[k] + 2 + 31) / 32) * 32;
+        tot += stride;
+    }
+    c->total = tot;
+    std::vector<int2> tabs[5];
+    build_table(c->t128, c->cap, ORB_T, tabs[0]);
+    build_table(c->t256, c->cap, RELAX_T, tabs[1]);
+    build_table(c->t1024, c->cap, POT_T, tabs[2]);
+    build_table(c->t2048, c->cap, SORT_T, tabs[3]);
+    build_table(c->t5120, c->cap, TS_T, tabs[4]);
+    size_t bytes = 0;
+    carve_all(c, nullptr, tabs, &bytes);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&c->arena, bytes) != cudaSuccess) {
+        fprintf(stderr, "cmcgpu: cannot allocate %zu bytes of device memory\n", bytes);
+        cudaGetLastError();
+        if (c->stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return CMCG_ERR_NOMEM;
+    }
+    c->arena_bytes = bytes;
+    carve_all(c, (char *)c->arena, tabs, &bytes);
+    CK(cudaMemsetAsync(c->arena, 0, c->arena_bytes, c->stream));
+    // cluster descriptors and tile tables
+    std::vector<long long> hist_off(nclusters);
+    long long ho = 0;
+    for (int k = 0; k < nclusters; ++k) {
+        hist_off[k] = ho;
+        ho += (long long)RADIX * c->t2048.count[k];
+    }
+    CK(cudaMemcpyAsync(c->sb.hist_off, hist_off.data(), nclusters * sizeof(long long), cudaMemcpyHostToDevice,
+                       c->stream));
+    c->h_cls.resize(nclusters);
+    for (int k = 0; k < nclusters; ++k) {
+        Cluster &C = c->h_cls[k];
+        const cmcg_params &p = params[k];
+        memset(&C, 0, sizeof(C));
+        C.off = c->off[k];
+        C.cap = c->cap[k];
+        C.sc = c->d_sc + k;
+        C.p = p.AVEKERNEL;
+        C.GAMMA = p.GAMMA;
+        C.THETASEMAX = p.THETASEMAX;
+        C.PERTURB = p.PERTURB;
+        C.RELAXATION = p.RELAXATION;
+        C.TIDALLY_STRIP_STARS = p.TIDALLY_STRIP_STARS;
+        C.TIDAL_TREATMENT = p.TIDAL_TREATMENT;
+        C.n_try = p.n_try;
+        C.apsides_max_iter = p.apsides_max_iter;
+        C.apsides_precision = p.apsides_precision;
+        C.apsides_convergence = p.apsides_convergence;
+        C.seed = p.seed;
+        C.relax_fp32 = p.relax_fp32;
+    }
+    CK(cudaMemcpyAsync(c->d_cls, c->h_cls.data(), nclusters * sizeof(Cluster), cudaMemcpyHostToDevice, c->stream));
+    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t5120};
+    for (int i = 0; i < 5; ++i) {
+        CK(cudaMemcpyAsync(tts[i]->d_tiles, tabs[i].data(), tabs[i].size() * sizeof(int2), cudaMemcpyHostToDevice,
+                           c->stream));
+        CK(cudaMemcpyAsync(tts[i]->d_first, tts[i]->first.data(), nclusters * sizeof(int), cudaMemcpyHostToDevice,
+                           c->stream));
+        CK(cudaMemcpyAsync(tts[i]->d_count, tts[i]->count.data(), nclusters * sizeof(int), cudaMemcpyHostToDevice,
+                           c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    *out = c;
+    return CMCG_OK;
+}
+
+int cmcg_destroy(cmcg_ctx *c)
+{
+    if (!c) return CMCG_ERR_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    if (c->arena) cudaFree(c->arena);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return CMCG_OK;
+}
+
+int cmcg_load(cmcg_ctx *c, int k, long N, const double *r, const double *m, const double *vr, const double *vt,
+              const int64_t *id)
+{
+    if (!c || k < 0 || k >= c->ncl || !r || !m || !vr || !vt) return CMCG_ERR_ARG;
+    if (N < 2 * c->params[k].AVEKERNEL + 2) return CMCG_ERR_ARG;
+    if (N > c->cap[k]) return CMCG_ERR_CAPACITY;
+    const long long o = c->off[k];
+    const cmcg_params &p = c->params[k];
+    const long long NSTAR = p.N_STAR > 0 ? p.N_STAR : N;
+    std::vector<double> tmp((size_t)N + 2);
+    std::vector<long long> ids((size_t)N + 2, 0);
+    // star_m: mass in N-body units times N_STAR (cmc_fits.c:99,123)
+    tmp[0] = 0.0;
+    for (long i = 0; i < N; ++i) tmp[i + 1] = m[i] * ((double)NSTAR);
+    tmp[N + 1] = 0.0;
+    CK(cudaMemcpy(c->f.m + o, tmp.data(), (N + 2) * sizeof(double), cudaMemcpyHostToDevice));
+    tmp[0] = CMCG_ZERO;
+    for (long i = 0; i < N; ++i) tmp[i + 1] = r[i];
+    tmp[N + 1] = CMCG_SF_INFINITY;
+    CK(cudaMemcpy(c->f.r + o, tmp.data(), (N + 2) * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemset(c->f.vr + o, 0, (N + 2) * sizeof(double)));
+    CK(cudaMemset(c->f.vt + o, 0, (N + 2) * sizeof(double)));
+    CK(cudaMemcpy(c->f.vr + o + 1, vr, N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->f.vt + o + 1, vt, N * sizeof(double), cudaMemcpyHostToDevice));
+    for (long i = 0; i < N; ++i) ids[i + 1] = id ? (long long)id[i] : (long long)(i + 1);
+    CK(cudaMemcpy(c->f.id + o, ids.data(), (N + 2) * sizeof(long long), cudaMemcpyHostToDevice));
+    Scalars s;
+    memset(&s, 0, sizeof(s));
+    s.N_MAX = N;
+    s.N_MAX_NEW = N;
+    s.N_STAR = NSTAR;
+    s.tcount = 1;
+    s.Mtotal = 1.0;
+    s.orbit_r = p.orbit_r;
+    s.madhoc = 1.0 / ((double)NSTAR);
+    s.cenma_m = p.cenma_m;
+    CK(cudaMemcpy(c->d_sc + k, &s, sizeof(Scalars), cudaMemcpyHostToDevice));
+    return CMCG_OK;
+}
+
+// New star count after a host upload (the sentinel r[N+1] is copied separately).
+__global__ void k_set_count(const Cluster *cls, int k, long long N)
+{
+    Scalars *sc = cls[k].sc;
+    sc->N_MAX = N;
+    sc->N_MAX_NEW = N;
+}
+
+int cmcg_put_stars(cmcg_ctx *c, int k, long N, const double *r, const double *m, const double *vr, const double *vt,
+                   const double *E, const double *J, const int64_t *id)
+{
+    if (!c || k < 0 || k >= c->ncl || !r || !m || !vr || !vt || !E || !J || !id) return CMCG_ERR_ARG;
+    if (N > c->cap[k]) return CMCG_ERR_CAPACITY;
+    if (N < 2 * c->params[k].AVEKERNEL + 2) return CMCG_ERR_ARG;
+    const long long o = c->off[k] + 1;
+    const size_t b = (size_t)N * sizeof(double);
+    CK(cudaMemcpyAsync(c->f.r + o, r, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->f.m + o, m, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->f.vr + o, vr, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->f.vt + o, vt, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->f.E + o, E, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->f.J + o, J, b, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->f.id + o, id, (size_t)N * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    static const double sentinel = CMCG_SF_INFINITY;
+    CK(cudaMemcpyAsync(c->f.r + o + N, &sentinel, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    k_set_count<<<1, 1, 0, c->stream>>>(c->d_cls, k, (long long)N);
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+long cmcg_get_stars(cmcg_ctx *c, int k, long cap, double *r, double *m, double *vr, double *vt, double *E, double *J,
+                    int64_t *id)
+{
+    if (!c || k < 0 || k >= c->ncl) return CMCG_ERR_ARG;
+    long long N = 0;
+    if (cudaMemcpyAsync(&N, &c->d_sc[k].N_MAX_NEW, sizeof(long long), cudaMemcpyDeviceToHost, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+        return CMCG_ERR_CUDA;
+    if (N > cap) return CMCG_ERR_CAPACITY;
+    const long long o = c->off[k] + 1;
+    const size_t b = (size_t)N * sizeof(double);
+    struct {
+        double *dst;
+        const double *src;
+    } t[] = {{r, c->f.r}, {m, c->f.m}, {vr, c->f.vr}, {vt, c->f.vt}, {E, c->f.E}, {J, c->f.J}};
+    for (auto &x : t)
+        if (x.dst && cudaMemcpyAsync(x.dst, x.src + o, b, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+            return CMCG_ERR_CUDA;
+    if (id && cudaMemcpyAsync(id, c->f.id + o, (size_t)N * sizeof(long long), cudaMemcpyDeviceToHost, c->stream) !=
+                  cudaSuccess)
+        return CMCG_ERR_CUDA;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return CMCG_ERR_CUDA;
+    return (long)N;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ launches ---
+static int L_pot(cmcg_ctx *c)
+{
+    fam_begin(c, F_POT);
+    k_pot_agg<<<c->t1024.ntiles, POT_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->f, c->pb);
+    k_pot_carry<<<c->ncl, POT_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->pb, c->ncl);
+    k_pot_apply<<<c->t1024.ntiles, POT_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->f, c->pb);
+    fam_end(c);
+    c->launches += 3;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_energy(cmcg_ctx *c)
+{
+    fam_begin(c, F_ENERGY);
+    k_energy<<<c->t256.ntiles, EN_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials, c->tickets);
+    fam_end(c);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_begin(cmcg_ctx *c)
+{
+    fam_begin(c, F_BEGIN);
+    k_begin_step<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
+    fam_end(c);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_end(cmcg_ctx *c)
+{
+    fam_begin(c, F_END);
+    k_end_step<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
+    fam_end(c);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_timestep(cmcg_ctx *c)
+{
+    fam_begin(c, F_TIMESTEP);
+    k_timestep<<<c->t5120.ntiles, 128, 0, c->stream>>>(c->d_cls, c->t5120.view(), c->f, c->partials, c->tickets);
+    fam_end(c);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_relax(cmcg_ctx *c, double dt)
+{
+    fam_begin(c, F_RELAX);
+    if (c->relax_fp32)
+        k_relax32<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials,
+                                                                    c->tickets, dt);
+    else
+        k_relax64<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials,
+                                                                    c->tickets, dt);
+    fam_end(c);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_orbit(cmcg_ctx *c)
+{
+    fam_begin(c, F_ORBIT);
+    k_orbit<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials, c->tickets);
+    fam_end(c);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_tidal(cmcg_ctx *c)
+{
+    fam_begin(c, F_TIDAL);
+    for (int i = 0; i < TIDAL_PASSES; ++i)
+        k_tidal<<<c->t2048.ntiles, TID_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->partials,
+                                                                 c->tickets);
+    k_tidal_check<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
+    fam_end(c);
+    c->launches += TIDAL_PASSES + 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static void swap_sorted(cmcg_ctx *c)
+{
+    std::swap(c->f.r, c->f.r2);
+    std::swap(c->f.m, c->f.m2);
+    std::swap(c->f.id, c->f.id2);
+    std::swap(c->f.ec_pre, c->f.ec_pre2);
+}
+
+static int L_sort(cmcg_ctx *c)
+{
+    fam_begin(c, F_SORT);
+    k_sort_prep<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb,
+                                                                   c->partials, c->tickets);
+    for (int p = 0; p < SORT_MAX_PASSES; ++p) {
+        k_sort_hist<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
+        k_sort_scan<<<c->ncl * RADIX, 256, 0, c->stream>>>(c->t2048.view(), c->sb, p, c->ncl);
+        k_sort_scatter<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
+    }
+    k_sort_gather<<<c->t256.ntiles, GATHER_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->sb);
+    fam_end(c);
+    c->launches += 2 + 3 * SORT_MAX_PASSES;
+    swap_sorted(c);
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+static int L_ec3(cmcg_ctx *c)
+{
+    fam_begin(c, F_EC3);
+    k_ec3<<<c->t256.ntiles, EC3_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->eb);
+    k_ec3_fix<<<(c->ncl + 31) / 32, 32, 0, c->stream>>>(c->d_cls, c->f, c->eb, c->ncl);
+    fam_end(c);
+    c->launches += 2;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+#define RUN(x)                \
+    do {                      \
+        int rc_ = (x);        \
+        if (rc_) return rc_;  \
+    } while (0)
+
+static int issue_step(cmcg_ctx *c)
+{
+    RUN(L_begin(c));
+    RUN(L_timestep(c));
+    RUN(L_relax(c, -1.0));
+    RUN(L_orbit(c));
+    RUN(L_tidal(c));
+    RUN(L_sort(c));
+    RUN(L_pot(c));
+    RUN(L_ec3(c));
+    RUN(L_energy(c));
+    RUN(L_end(c));
+    return CMCG_OK;
+}
+
+extern "C" {
+
+int cmcg_initialize(cmcg_ctx *c)
+{
+    if (!c) return CMCG_ERR_ARG;
+    RUN(L_pot(c));
+    RUN(L_energy(c));
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<Scalars> s(c->ncl);
+    CK(cudaMemcpy(s.data(), c->d_sc, c->ncl * sizeof(Scalars), cudaMemcpyDeviceToHost));
+    for (auto &x : s) x.Etot_ini = x.Etot;
+    CK(cudaMemcpy(c->d_sc, s.data(), c->ncl * sizeof(Scalars), cudaMemcpyHostToDevice));
+    return CMCG_OK;
+}
+
+int cmcg_begin_step(cmcg_ctx *c) { return c ? L_begin(c) : CMCG_ERR_ARG; }
+int cmcg_calc_timestep(cmcg_ctx *c) { return c ? L_timestep(c) : CMCG_ERR_ARG; }
+int cmcg_dynamics_apply(cmcg_ctx *c, double dt) { return c ? L_relax(c, dt) : CMCG_ERR_ARG; }
+int cmcg_new_orbits_calculate(cmcg_ctx *c) { return c ? L_orbit(c) : CMCG_ERR_ARG; }
+int cmcg_tidally_strip_stars(cmcg_ctx *c) { return c ? L_tidal(c) : CMCG_ERR_ARG; }
+int cmcg_qsorts_new(cmcg_ctx *c) { return c ? L_sort(c) : CMCG_ERR_ARG; }
+int cmcg_calc_potential(cmcg_ctx *c) { return c ? L_pot(c) : CMCG_ERR_ARG; }
+int cmcg_energy_conservation3(cmcg_ctx *c) { return c ? L_ec3(c) : CMCG_ERR_ARG; }
+int cmcg_compute_energy(cmcg_ctx *c) { return c ? L_energy(c) : CMCG_ERR_ARG; }
+int cmcg_end_step(cmcg_ctx *c) { return c ? L_end(c) : CMCG_ERR_ARG; }
+
+int cmcg_use_graph(cmcg_ctx *c, int enable)
+{
+    if (!c) return CMCG_ERR_ARG;
+    c->use_graph = enable != 0;
+    return CMCG_OK;
+}
+
+static int capture_pair(cmcg_ctx *c)
+{
+    const bool prof = c->profile;
+    c->profile = false;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const long l0 = c->launches;
+    int rc = issue_step(c);
+    if (!rc) rc = issue_step(c);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->profile = prof;
+    c->launches = l0;
+    if (rc) return rc;
+    if (e != cudaSuccess) return CMCG_ERR_CUDA;
+    c->graph = g;
+    CK(cudaGraphInstantiate(&c->gexec, g, 0));
+    c->graph_ready = true;
+    return CMCG_OK;
+}
+
+int cmcg_step(cmcg_ctx *c) { return cmcg_run(c, 1); }
+
+int cmcg_run(cmcg_ctx *c, int nsteps)
+{
+    if (!c || nsteps < 0) return CMCG_ERR_ARG;
+    const long l0 = c->launches;
+    int done = 0;
+    if (c->use_graph && !c->profile && nsteps >= 2) {
+        if (!c->graph_ready) RUN(capture_pair(c));
+        // one graph holds two steps: the sort's buffer swap alternates the field pointers
+        long per_pair = 0;
+        {
+            // count the launches of a pair once (same as issuing two steps)
+            per_pair = 2 * (1 + 1 + 1 + 1 + (TIDAL_PASSES + 1) + (2 + 3 * SORT_MAX_PASSES) + 3 + 2 + 1 + 1);
+        }
+        while (nsteps - done >= 2) {
+            CK(cudaGraphLaunch(c->gexec, c->stream));
+            c->launches += per_pair;
+            done += 2;
+        }
+    }
+    for (; done < nsteps; ++done) RUN(issue_step(c));
+    c->launches_last = c->launches - l0;
+    return CMCG_OK;
+}
+
+int cmcg_synchronize(cmcg_ctx *c)
+{
+    if (!c) return CMCG_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    return CMCG_OK;
+}
+
+long cmcg_launch_count(cmcg_ctx *c) { return c ? c->launches_last : -1; }
+
+int cmcg_profile(cmcg_ctx *c, int enable)
+{
+    if (!c) return CMCG_ERR_ARG;
+    c->profile = enable != 0;
+    return CMCG_OK;
+}
+
+int cmcg_kernel_time(cmcg_ctx *c, const char *family, double *ms_total, long *launches)
+{
+    if (!c || !family) return CMCG_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    for (const ProfRec &p : c->prof) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        c->fam_ms[p.fam] += ms;
+        c->fam_n[p.fam] += 1;
+    }
+    c->prof.clear();
+    c->ev_next = 0;
+    if (!strcmp(family, "reset")) {
+        for (int i = 0; i < F_COUNT; ++i) {
+            c->fam_ms[i] = 0.0;
+            c->fam_n[i] = 0;
+        }
+        return CMCG_OK;
+    }
+    for (int i = 0; i < F_COUNT; ++i) {
+        if (!strcmp(family, kFamilyNames[i])) {
+            if (ms_total) *ms_total = c->fam_ms[i];
+            if (launches) *launches = c->fam_n[i];
+            return CMCG_OK;
+        }
+    }
+    return CMCG_ERR_ARG;
+}
+
+int cmcg_potential(cmcg_ctx *c, int k, double r, double *out)
+{
+    if (!c || k < 0 || k >= c->ncl || !out) return CMCG_ERR_ARG;
+    k_potential_query<<<1, 1, 0, c->stream>>>(c->d_cls, c->f, k, r, c->d_query);
+    double h[2];
+    CK(cudaMemcpyAsync(h, c->d_query, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *out = h[0];
+    return h[1] != 0.0 ? CMCG_ERR_FINDZERO_R : CMCG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ field access
+static double *star_field(cmcg_ctx *c, const char *name, bool *global)
+{
+    *global = false;
+    Fields &f = c->f;
+    struct {
+        const char *n;
+        double *p;
+        bool g;
+    } tab[] = {{"r", f.r, false},         {"m", f.m, false},           {"vr", f.vr, false},
+               {"vt", f.vt, false},       {"E", f.E, false},           {"J", f.J, false},
+               {"vr_rel", f.vr_rel, false}, {"vt_rel", f.vt_rel, false}, {"rnew", f.rnew, false},
+               {"vrnew", f.vrnew, false}, {"vtnew", f.vtnew, false},   {"X", f.X, false},
+               {"Y", f.Y, false},         {"r_peri", f.r_peri, false}, {"r_apo", f.r_apo, false},
+               {"rOld", f.rOld, false},   {"ec_pre", f.ec_pre, false}, {"phi", f.phi, false},
+               {"star_r", f.r, true},     {"star_m", f.m, true},       {"star_phi", f.phi, true},
+               {"sigma_r", f.sigma_r, true}, {"sigma", f.sigma, true}, {"inv_r", f.inv_r, true}};
+    for (auto &t : tab)
+        if (!strcmp(name, t.n)) {
+            *global = t.g;
+            return t.p;
+        }
+    return nullptr;
+}
+
+static int read_scalars(cmcg_ctx *c, int k, Scalars *s)
+{
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(s, c->d_sc + k, sizeof(Scalars), cudaMemcpyDeviceToHost));
+    return CMCG_OK;
+}
+
+extern "C" {
+
+long cmcg_nstars(cmcg_ctx *c, int k)
+{
+    if (!c || k < 0 || k >= c->ncl) return -1;
+    Scalars s;
+    if (read_scalars(c, k, &s)) return -1;
+    return (long)s.N_MAX_NEW;
+}
+
+long cmcg_get_field(cmcg_ctx *c, int k, const char *name, double *out, long cap)
+{
+    if (!c || k < 0 || k >= c->ncl || !name || !out) return -1;
+    bool g;
+    double *p = star_field(c, name, &g);
+    if (!p) return -1;
+    Scalars s;
+    if (read_scalars(c, k, &s)) return -1;
+    long n = g ? (long)s.N_MAX + 2 : (long)s.N_MAX_NEW;
+    if (n > cap) n = cap;
+    const long long o = c->off[k] + (g ? 0 : 1);
+    if (cudaMemcpy(out, p + o, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return n;
+}
+
+long cmcg_set_field(cmcg_ctx *c, int k, const char *name, const double *in, long n)
+{
+    if (!c || k < 0 || k >= c->ncl || !name || !in) return -1;
+    bool g;
+    double *p = star_field(c, name, &g);
+    if (!p) return -1;
+    if (n > c->cap[k] + (g ? 2 : 0)) n = c->cap[k] + (g ? 2 : 0);
+    const long long o = c->off[k] + (g ? 0 : 1);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return -1;
+    if (cudaMemcpy(p + o, in, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+    return n;
+}
+
+long cmcg_get_ids(cmcg_ctx *c, int k, int64_t *out, long cap)
+{
+    if (!c || k < 0 || k >= c->ncl || !out) return -1;
+    Scalars s;
+    if (read_scalars(c, k, &s)) return -1;
+    long n = (long)s.N_MAX_NEW;
+    if (n > cap) n = cap;
+    if (cudaMemcpy(out, c->f.id + c->off[k] + 1, n * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return -1;
+    return n;
+}
+
+#define SCALAR_TABLE(X)                                                                                    \
+    X(Mtotal) X(Rtidal) X(orbit_r) X(madhoc) X(cenma_m) X(cenma_E) X(Dt) X(Prev_Dt) X(TotalTime) X(max_r)    \
+        X(TidalMassLoss) X(TidalMassLoss_old) X(OldTidalMassLoss) X(DTidalMassLoss) X(Eescaped) X(Jescaped) \
+            X(Etidal) X(Eoops) X(Eescaped_old) X(Jescaped_old) X(Etidal_old) X(Etot) X(KE) X(PE) X(Etot_ini) \
+                X(phi_rtidal)
+
+int cmcg_get_scalar(cmcg_ctx *c, int k, const char *name, double *out)
+{
+    if (!c || k < 0 || k >= c->ncl || !name || !out) return CMCG_ERR_ARG;
+    Scalars s;
+    RUN(read_scalars(c, k, &s));
+#define X(n)                  \
+    if (!strcmp(name, #n)) {  \
+        *out = (double)s.n;   \
+        return CMCG_OK;       \
+    }
+    SCALAR_TABLE(X)
+#undef X
+    struct {
+        const char *n;
+        double v;
+    } ints[] = {{"N_MAX", (double)s.N_MAX},         {"N_MAX_NEW", (double)s.N_MAX_NEW},
+                {"N_STAR", (double)s.N_STAR},       {"tcount", (double)s.tcount},
+                {"Nrel", (double)s.Nrel},           {"Nrelbeta0", (double)s.Nrelbeta[0]},
+                {"Nrelbeta1", (double)s.Nrelbeta[1]}, {"Nrelbeta2", (double)s.Nrelbeta[2]},
+                {"Nrelbeta3", (double)s.Nrelbeta[3]}, {"n_excess", (double)s.n_excess},
+                {"tidal_iters", (double)s.tidal_iters}, {"err", (double)s.err},
+                {"qaverelbeta0", s.qaverelbeta[0]}, {"maverelbeta0", s.maverelbeta[0]},
+                {"raverelbeta0", s.raverelbeta[0]}};
+    for (auto &t : ints)
+        if (!strcmp(name, t.n)) {
+            *out = t.v;
+            return CMCG_OK;
+        }
+    return CMCG_ERR_ARG;
+}
+
+int cmcg_set_scalar(cmcg_ctx *c, int k, const char *name, double v)
+{
+    if (!c || k < 0 || k >= c->ncl || !name) return CMCG_ERR_ARG;
+    Scalars s;
+    RUN(read_scalars(c, k, &s));
+    bool hit = false;
+#define X(n)                  \
+    if (!strcmp(name, #n)) {  \
+        s.n = v;              \
+        hit = true;           \
+    }
+    SCALAR_TABLE(X)
+#undef X
+    if (!strcmp(name, "tcount")) {
+        s.tcount = (long long)v;
+        hit = true;
+    }
+    if (!hit) return CMCG_ERR_ARG;
+    CK(cudaMemcpy(c->d_sc + k, &s, sizeof(Scalars), cudaMemcpyHostToDevice));
+    return CMCG_OK;
+}
+
+int cmcg_last_error(cmcg_ctx *c, int *cluster, long *index)
+{
+    if (!c) return CMCG_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "cmcgpu: stream error: %s\n", cudaGetErrorString(e));
+        return CMCG_ERR_CUDA;
+    }
+    std::vector<Scalars> s(c->ncl);
+    CK(cudaMemcpy(s.data(), c->d_sc, c->ncl * sizeof(Scalars), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < c->ncl; ++k) {
+        if (s[k].err) {
+            const int code = s[k].err;
+            if (cluster) *cluster = k;
+            if (index) *index = (long)s[k].err_index;
+            s[k].err = 0;
+            s[k].err_index = 0;
+            CK(cudaMemcpy(c->d_sc + k, &s[k], sizeof(Scalars), cudaMemcpyHostToDevice));
+            return code;
+        }
+    }
+    return CMCG_OK;
+}
+
+// Host copy of the device's counter-based draw (same keying as the kernels).
+double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, int word)
+{
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32) ^ (uint32_t)tcount;
+    uint64_t uid = (uint64_t)id;
+    uint32_t c0 = (uint32_t)uid, c1 = (uint32_t)(uid >> 32), c2 = (uint32_t)site, c3 = n;
+    for (int i = 0; i < 10; ++i) {
+        if (i > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0;
+        c1 = (uint32_t)p1;
+        c2 = n2;
+        c3 = (uint32_t)p0;
+    }
+    const uint32_t w[4] = {c0, c1, c2, c3};
+    return w[word & 3] / 4294967296.0;
+}
+
+}  // extern "C"

@@ -1,0 +1,267 @@
+// cmcg_internal.cuh -- device data layout and shared device helpers.
+//
+// Layout in HBM.  Every cluster of a context owns a contiguous slice of each
+// structure-of-arrays field: element k of cluster c lives at off[c] + k, with
+// k = 0 and k = N+1 the reference's sentinels (star_r[0] = 1e-20,
+// star_r[N+1] = 1e10) and stars at 1..N in radial order.  Slices start on
+// 256-byte boundaries so a tile of doubles is one aligned 128-bit-vector run.
+// Kernels map blocks to (cluster, tile) pairs through a per-tile-size table,
+// so one launch covers an ensemble of clusters with uneven N and no tile ever
+// straddles two clusters.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CMCG_SF_INFINITY 1.0e10      /* include/cmc/cmc.h:58 */
+#define CMCG_ZERO 1.0e-20            /* include/cmc/cmc.h:60 */
+#define CMCG_PI 3.14159265358979323  /* include/cmc/cmc.h:62 */
+#define CMCG_DBL_EPSILON 2.2204460492503131e-16
+#define CMCG_DBL_MIN 2.2250738585072014e-308
+
+// Bounded waits: every cross-block spin gives up after this many polls and
+// records CMCG_ERR_SPIN instead of hanging the GPU.
+#define CMCG_SPIN_LIMIT (1 << 22)
+
+namespace cmcg {
+
+// Per-cluster scalar state (the reference's globals for one cluster).
+struct Scalars {
+    long long N_MAX, N_MAX_NEW, N_STAR, tcount;
+    double Mtotal, Rtidal, orbit_r, madhoc, cenma_m, cenma_E;
+    double Dt, Prev_Dt, TotalTime, max_r;
+    double TidalMassLoss, TidalMassLoss_old, OldTidalMassLoss, DTidalMassLoss;
+    double Eescaped, Jescaped, Etidal, Eoops, Eescaped_old, Jescaped_old, Etidal_old;
+    double Etot, KE, PE, Etot_ini;
+    long long Nrel, Nrelbeta[4];
+    double qaverelbeta[4], maverelbeta[4], raverelbeta[4];
+    double phi_rtidal, gierszalpha;
+    int tidal_done, tidal_iters;
+    int err;
+    int pad0;
+    long long err_index;
+    // sort bookkeeping
+    long long n_bound;     // stars kept after the sort (r < SF_INFINITY)
+    // set_velocities3 bookkeeping
+    long long n_excess;    // stars whose predicted v^2 <= 0
+};
+
+// Per-cluster constant description (built on the host, read-only on device).
+struct Cluster {
+    long long off;         // element offset of index 0 (sentinel) of this cluster
+    long long cap;         // capacity in stars
+    Scalars *sc;
+    // parameters (.ini keys)
+    long long p;           // AVEKERNEL
+    double GAMMA, THETASEMAX;
+    int PERTURB, RELAXATION, TIDALLY_STRIP_STARS, TIDAL_TREATMENT;
+    long long n_try, apsides_max_iter;
+    double apsides_precision, apsides_convergence;
+    unsigned long long seed;
+    int relax_fp32;
+    int pad1;
+};
+
+// Device-resident fields (all concatenated over clusters).
+struct Fields {
+    double *r, *m, *phi, *inv_r;       // star_r, star_m, star_phi, 1/star_r
+    double *vr, *vt, *E, *J;           // star[].vr, .vt, .E, .J
+    double *vr_rel, *vt_rel;           // velocities after relaxation (star[].vr/.vt then)
+    double *rnew, *vrnew, *vtnew;      // star[].rnew, .vrnew, .vtnew
+    double *X, *Y, *r_peri, *r_apo;    // star[].X, .Y, .r_peri, .r_apo
+    double *ec_pre;                    // vold^2 + (Uoldrold - Uoldrnew), see set_velocities3
+    double *rOld;                      // star[].rOld after the sort
+    double *sigma_r, *sigma;           // sigma_array.r, sigma_array.sigma
+    long long *id;                     // star[].id
+    // second buffers for the sort's gather (swapped on the host)
+    double *r2, *m2, *ec_pre2;
+    long long *id2;
+};
+
+// Block -> (cluster, tile) table entry for one tile size.
+struct TileMap {
+    const int2 *tiles;   // .x = cluster, .y = tile index within the cluster
+    int ntiles;
+};
+
+// Deterministic cross-block reductions: each block writes its partials to a
+// slot, the last block to arrive (atomic ticket) combines them in block order.
+struct Partials {
+    double *d;           // [ntiles][nd]
+    unsigned int *ticket;// one counter per cluster
+};
+
+__device__ __forceinline__ void set_error(Scalars *sc, int code, long long idx)
+{
+    if (atomicCAS(&sc->err, 0, code) == 0) sc->err_index = idx;
+}
+
+// ---------------------------------------------------------------- Philox --
+// Philox4x32-10 (Salmon et al., SC'11).  The same keying as the oracle:
+// key = (seed lo, seed hi ^ tcount), counter = (id lo, id hi, site, n).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
+{
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        if (i > 0) {
+            k.x += 0x9E3779B9u;
+            k.y += 0xBB67AE85u;
+        }
+        unsigned int hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        unsigned int hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+
+enum { SITE_Y = 1, SITE_PENC = 2, SITE_PSI = 3, SITE_TRIAL = 4, SITE_SIGN = 5 };
+
+__device__ __forceinline__ uint4 draw_block(unsigned long long seed, long long tcount, int site,
+                                            long long id, unsigned int n)
+{
+    uint2 key = make_uint2((unsigned int)seed, (unsigned int)(seed >> 32) ^ (unsigned int)tcount);
+    unsigned long long uid = (unsigned long long)id;
+    return philox4x32_10(make_uint4((unsigned int)uid, (unsigned int)(uid >> 32), (unsigned int)site, n), key);
+}
+
+// u32 -> [0,1) with the reference's 32-bit resolution (taus113-v2.c:186)
+__device__ __forceinline__ double u01(unsigned int u) { return (double)u / 4294967296.0; }
+
+// ------------------------------------------------------- double-double --
+// Error-free transformations (Knuth two-sum, FMA two-product) used to
+// evaluate function_q with more precision than the reference's long double,
+// so that the sign tests of its bisections agree.
+struct dd {
+    double hi, lo;
+};
+__device__ __forceinline__ dd two_sum(double a, double b)
+{
+    double s = __dadd_rn(a, b);
+    double bb = __dsub_rn(s, a);
+    double err = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+    return {s, err};
+}
+__device__ __forceinline__ dd quick_two_sum(double a, double b)
+{
+    double s = __dadd_rn(a, b);
+    return {s, __dsub_rn(b, __dsub_rn(s, a))};
+}
+__device__ __forceinline__ dd dd_add(dd a, dd b)
+{
+    dd s = two_sum(a.hi, b.hi);
+    dd t = two_sum(a.lo, b.lo);
+    s.lo = __dadd_rn(s.lo, t.hi);
+    s = quick_two_sum(s.hi, s.lo);
+    s.lo = __dadd_rn(s.lo, t.lo);
+    return quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ dd dd_neg(dd a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ dd dd_mul_d(dd a, double b)
+{
+    double p = __dmul_rn(a.hi, b);
+    double e = __fma_rn(a.hi, b, -p);
+    e = __fma_rn(a.lo, b, e);
+    return quick_two_sum(p, e);
+}
+// a / b for doubles a, b, to double-double accuracy
+__device__ __forceinline__ dd dd_div_dd(double a, double b)
+{
+    double q1 = __ddiv_rn(a, b);
+    double r = __fma_rn(-q1, b, a);       // exact remainder a - q1*b
+    double q2 = __ddiv_rn(r, b);
+    return quick_two_sum(q1, q2);
+}
+// (long double)a / (long double)b where b is given as double-double
+__device__ __forceinline__ dd dd_div_d_dd(double a, dd b)
+{
+    double q1 = __ddiv_rn(a, b.hi);
+    // r = a - q1*b (to dd)
+    double p = __dmul_rn(q1, b.hi);
+    double pe = __fma_rn(q1, b.hi, -p);
+    pe = __fma_rn(q1, b.lo, pe);
+    double r = __dsub_rn(__dsub_rn(a, p), pe);
+    double q2 = __ddiv_rn(r, b.hi);
+    return quick_two_sum(q1, q2);
+}
+
+// ------------------------------------------------------ table lookups ---
+// Orders positive doubles by their bit patterns (integer compare, no FP64 pipe).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+// FindZero_r, cmc_nr.c:62-82: largest k in [kmin,kmax] with r[k] < x (x > 0),
+// for kmin < kmax (the only way the reference calls it).  The bisection
+// halves a range of at most 2^63, so 64 rounds bound it.
+__device__ __forceinline__ long long find_zero_r(const double *__restrict__ r, long long kmin, long long kmax,
+                                                 double x)
+{
+    const long long xb = dbits(x);
+    for (int it = 0; it < 64 && kmax != kmin; ++it) {
+        long long ktry = (kmin + kmax + 1) >> 1;
+        if (dbits(__ldg(r + ktry)) < xb)
+            kmin = ktry;
+        else
+            kmax = ktry - 1;
+    }
+    return kmin;
+}
+
+// potential(r), cmc_utils.c:112-164 with SEARCH_GRID = 0.  inv_r[k] holds the
+// correctly rounded 1.0/r[k], so the Henon interpolation performs exactly the
+// reference's divisions with two of the three precomputed.
+__device__ __forceinline__ double potential_at(const double *__restrict__ r, const double *__restrict__ phi,
+                                               const double *__restrict__ inv_r, long long N_MAX, double x,
+                                               int *ok)
+{
+    if (x == 0.0) return __ldg(phi);
+    const double r1 = __ldg(r + 1);
+    if (x < r1) {
+        double p0 = __ldg(phi), p1 = __ldg(phi + 1);
+        return __dsub_rn(p0, __ddiv_rn(__dmul_rn(__dsub_rn(p0, p1), r1), x));
+    }
+    long long i = (N_MAX == 1) ? 1 : find_zero_r(r, 1, N_MAX + 1, x);
+    if (i > N_MAX) {  // x beyond the r = SF_INFINITY sentinel: the reference's check fails too
+        *ok = 0;
+        return 0.0;
+    }
+    const double ri = __ldg(r + i), ri1 = __ldg(r + i + 1);
+    if (ri > x || ri1 < x) {
+        *ok = 0;
+        return 0.0;
+    }
+    if (i == 0) return __ldg(phi + 1);
+    const double pi = __ldg(phi + i), pi1 = __ldg(phi + i + 1);
+    const double ii = __ldg(inv_r + i), ii1 = __ldg(inv_r + i + 1);
+    return __dadd_rn(pi, __ddiv_rn(__dmul_rn(__dsub_rn(pi1, pi), __dsub_rn(ii, __ddiv_rn(1.0, x))),
+                                   __dsub_rn(ii, ii1)));
+}
+
+// MPI_PHI_S(rad, j), cmc.h:2175
+__device__ __forceinline__ double phi_s(double rad, double rj, double mj, double invN)
+{
+    double t = (rad >= rj) ? __ddiv_rn(mj, rad) : __ddiv_rn(mj, rj);
+    return __dmul_rn(t, invN);
+}
+
+// function_q, cmc_utils.c:1654-1662, which the reference evaluates in long
+// double (SQR rounds J/r to double first, cmc.h:2030).  Evaluated here in
+// double-double and rounded once to double.
+__device__ __forceinline__ double function_q_dd(double r, double pot, double E, double J, double rj, double mj,
+                                                double invN)
+{
+    const double q = __ddiv_rn(J, r);              // (double)(J/r)
+    const double Jr = (q == 0.0) ? 0.0 : __dmul_rn(q, q);
+    dd phis;
+    if (r >= rj) {
+        phis = dd_div_dd(mj, r);                    // m_j / r in extended precision
+    } else {
+        phis = {__ddiv_rn(mj, rj), 0.0};            // double division, then widened
+    }
+    phis = dd_mul_d(phis, invN);                    // * (1.0/N_STAR)
+    dd t = dd_add({pot, 0.0}, phis);                // pot + phis
+    dd u = dd_add({E, 0.0}, dd_neg(t));             // E - (pot + phis)
+    u.hi *= 2.0;
+    u.lo *= 2.0;
+    dd res = dd_add(u, {-Jr, 0.0});                 // 2(E - ...) - Jr
+    return __dadd_rn(res.hi, res.lo);
+}
+
+}  // namespace cmcg

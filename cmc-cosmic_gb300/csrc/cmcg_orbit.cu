@@ -1,0 +1,516 @@
+// cmcg_orbit.cu -- new orbits (get_positions) and tidal stripping.
+//
+// k_orbit restates get_positions_loop (cmc_evolution_thr.c:784-937) with
+// calc_orbit_new (cmc_orbit.c:413-540), get_positive_Q_index (30-59),
+// find_zero_Q (cmc_nr.c:316-383), set_a_b (cmc_orbit.c:722-740), and replaces
+// the GSL Brent search of find_root_vr (cmc_nr.c:500-603) by a safeguarded
+// Newton/bisection iteration with the same bracket, tolerance and residual
+// checks.  One thread owns one star; the Q sign tests of the bisections are
+// evaluated in double-double because the reference evaluates them in long
+// double.  It also folds in energy_conservation1/2 (cmc_utils.c:2153-2228):
+// the one quantity set_velocities3 later needs from them,
+//   ec_pre = vold^2 + 2(1-q)(Uoldrold - Uoldrnew),  q = 1/2,
+// is formed here, evaluated exactly as the reference's first partial sum.
+//
+// k_tidal restates one pass of the iteration in tidally_strip_stars
+// (cmc_evolution_thr.c:443-646); the host launches a bounded number of passes
+// and each exits at once after the cluster has settled.
+#include "cmcg_kernels.cuh"
+#include "cmcgpu.h"
+
+namespace cmcg {
+
+constexpr int BISECT_LIMIT = 80;
+
+struct OrbitCtx {
+    const double *__restrict__ r, *__restrict__ phi, *__restrict__ inv_r;
+    long long N_MAX;
+    double E, J, rj, mj, invN, cenma_m, madhoc;
+};
+
+static __device__ __forceinline__ double fq(const OrbitCtx &o, long long k)
+{
+    return function_q_dd(__ldg(o.r + k), __ldg(o.phi + k), o.E, o.J, o.rj, o.mj, o.invN);
+}
+
+// find_zero_Q, cmc_nr.c:316-383 (bounded; returns -1 if it does not terminate)
+static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long long kmax)
+{
+    const double qmin = fq(o, kmin), qmax = fq(o, kmax);
+    int it = 0;
+    if (qmin < qmax) {
+        do {
+            const long long ktry = (kmin + kmax + 1) / 2;
+            if (fq(o, ktry) < 0.0)
+                kmin = ktry;
+            else
+                kmax = ktry - 1;
+            if (++it > BISECT_LIMIT) return -1;
+        } while (kmax != kmin);
+    } else {
+        do {
+            const long long ktry = (kmin + kmax + 1) / 2;
+            if (fq(o, ktry) > 0.0)
+                kmin = ktry;
+            else
+                kmax = ktry - 1;
+            if (++it > BISECT_LIMIT) return -1;
+        } while (kmax != kmin);
+    }
+    return kmin;
+}
+
+// set_a_b, cmc_orbit.c:722-740; 1/r from the reciprocal table (same rounding)
+static __device__ __forceinline__ void set_a_b(const OrbitCtx &o, long long k, double *a, double *b)
+{
+    if (k == 0) {
+        *a = -o.cenma_m * o.madhoc;
+        *b = o.phi[1] + o.cenma_m * o.madhoc / o.r[1] + o.mj * o.madhoc / o.rj;
+    } else {
+        const double rk = o.r[k], rk1 = o.r[k + 1];
+        const double Uk = o.phi[k] + phi_s(rk, o.rj, o.mj, o.invN);
+        const double Uk1 = o.phi[k + 1] + phi_s(rk1, o.rj, o.mj, o.invN);
+        const double den = o.inv_r[k + 1] - o.inv_r[k];
+        *a = (Uk1 - Uk) / den;
+        *b = (Uk / rk1 - Uk1 / rk) / den;
+    }
+}
+
+// calc_pot_within_interval, cmc_nr.c:230-259
+static __device__ __forceinline__ double pot_within(const OrbitCtx &o, double x, long long k, bool *ok)
+{
+    const double rk = o.r[k], rk1 = o.r[k + 1];
+    if (x < (rk - CMCG_DBL_EPSILON) || x > rk1 + CMCG_DBL_EPSILON) {
+        *ok = false;
+        return 0.0;
+    }
+    if (fabs(x - rk) < CMCG_DBL_EPSILON) return o.phi[k];
+    if (fabs(x - rk1) < CMCG_DBL_EPSILON) return o.phi[k + 1];
+    if (x < o.r[1]) return o.phi[0] - o.cenma_m * o.madhoc / x;
+    return o.phi[k] + (o.phi[k + 1] - o.phi[k]) * (o.inv_r[k] - 1.0 / x) / (o.inv_r[k] - o.inv_r[k + 1]);
+}
+
+// vr^2 within interval k (calc_vr_within_interval, cmc_nr.c:267-278)
+static __device__ __forceinline__ double vr2_in(const OrbitCtx &o, double x, long long k, bool *ok)
+{
+    const double pot = pot_within(o, x, k, ok);
+    return function_q_dd(x, pot, o.E, o.J, o.rj, o.mj, o.invN);
+}
+
+// d(vr^2)/dr inside interval k, for the Newton step
+static __device__ __forceinline__ double dvr2_in(const OrbitCtx &o, double x, long long k)
+{
+    const double ix = 1.0 / x;
+    double dpot;
+    if (x < o.r[1])
+        dpot = o.cenma_m * o.madhoc * ix * ix;
+    else
+        dpot = (o.phi[k + 1] - o.phi[k]) / (o.inv_r[k] - o.inv_r[k + 1]) * ix * ix;
+    const double dphis = (x >= o.rj) ? -o.mj * o.invN * ix * ix : 0.0;
+    return -2.0 * (dpot + dphis) + 2.0 * o.J * o.J * ix * ix * ix;
+}
+
+// Root of vr^2 in [r_k, r_k+1]: safeguarded Newton with bisection fallback,
+// converged when the bracket satisfies |hi-lo| < eps + eps*min(|lo|,|hi|)
+// (the gsl_root_test_interval criterion of cmc_nr.c:535), then the residual
+// checks of cmc_nr.c:584-597.
+static __device__ double find_root_vr(const OrbitCtx &o, long long k, double prec, long long maxit, int *err)
+{
+    bool ok = true;
+    double lo = o.r[k], hi = o.r[k + 1];
+    double flo = vr2_in(o, lo, k, &ok), fhi = vr2_in(o, hi, k, &ok);
+    if (!ok) {
+        *err = CMCG_ERR_POT_INTERVAL;
+        return 0.0;
+    }
+    if ((flo >= 0.0 ? 1 : -1) == (fhi >= 0.0 ? 1 : -1)) {
+        *err = CMCG_ERR_ROOT_SIGNS;
+        return 0.0;
+    }
+    const double a0 = lo, b0 = hi;
+    double x = (fabs(flo) < fabs(fhi)) ? lo : hi, fx = (fabs(flo) < fabs(fhi)) ? flo : fhi;
+    bool conv = false;
+    for (long long it = 0; it < maxit; ++it) {
+        if (fabs(hi - lo) < prec + prec * fmin(fabs(lo), fabs(hi))) {
+            conv = true;
+            break;
+        }
+        const double d = dvr2_in(o, x, k);
+        double xn = (d != 0.0) ? x - fx / d : 0.5 * (lo + hi);
+        // bisect when Newton leaves the bracket or lands on an end
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        // close the bracket from the far side once Newton steps become tiny
+        const double tol = 0.25 * (prec + prec * fmin(fabs(lo), fabs(hi)));
+        if (fabs(xn - x) < tol) xn = (fabs(xn - lo) < fabs(hi - xn)) ? fmin(xn + tol, 0.5 * (xn + hi)) : fmax(xn - tol, 0.5 * (xn + lo));
+        x = xn;
+        fx = vr2_in(o, x, k, &ok);
+        if (!ok) {
+            *err = CMCG_ERR_POT_INTERVAL;
+            return 0.0;
+        }
+        if (fx == 0.0) {
+            lo = hi = x;
+            conv = true;
+            break;
+        }
+        if ((fx >= 0.0) == (flo >= 0.0)) {
+            lo = x;
+            flo = fx;
+        } else {
+            hi = x;
+            fhi = fx;
+        }
+    }
+    if (!conv) {
+        *err = CMCG_ERR_ROOT_NOCONV;
+        return 0.0;
+    }
+    (void)a0;
+    (void)b0;
+    double apsis = x;
+    if (vr2_in(o, apsis, k, &ok) < 0.0) {
+        if (vr2_in(o, lo, k, &ok) < 0.0) apsis = hi;
+        if (vr2_in(o, hi, k, &ok) < 0.0) apsis = lo;
+    }
+    if (vr2_in(o, apsis, k, &ok) < 0.0) {
+        *err = CMCG_ERR_ROOT_NEG;
+        return 0.0;
+    }
+    return apsis;
+}
+
+struct OrbitRs {
+    double rp, ra, dQdrp, dQdra;
+    int circular;
+};
+
+// calc_orbit_new, cmc_orbit.c:413-540
+static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, double prec, long long maxit, int *err)
+{
+    OrbitRs res;
+    res.circular = 1;
+    res.rp = res.ra = o.rj;
+    res.dQdrp = res.dQdra = 0.0;
+    // get_positive_Q_index, cmc_orbit.c:30-59
+    long long ktemp = j;
+    double Qtemp = fq(o, ktemp);
+    if (Qtemp <= 0.0) {
+        ktemp = -1;
+        do {
+            ktemp++;
+            Qtemp = fq(o, ktemp);
+        } while (Qtemp <= 0.0 && ktemp <= o.N_MAX);
+        if (ktemp >= o.N_MAX) return res;
+    }
+    const long long kmin = find_zero_Q(o, 0, ktemp);
+    const long long kmax = find_zero_Q(o, ktemp, o.N_MAX + 1);
+    if (kmin < 0 || kmax < 0 || kmin > o.N_MAX || kmax > o.N_MAX) {
+        *err = CMCG_ERR_ROOT_NOCONV;
+        return res;
+    }
+    const double rkmin = o.r[kmin], rk1min = o.r[kmin + 1], rkmax = o.r[kmax], rk1max = o.r[kmax + 1];
+    const double E = o.E, J = o.J;
+    double a, b, rmin, rmax, inside_sqrt;
+    set_a_b(o, kmin, &a, &b);
+    inside_sqrt = a * a - 2.0 * J * J * (b - E);
+    if (inside_sqrt < 0.0) {
+        rmin = -1.0 * J * J / a;
+        if ((rmin < rkmin) || (rmin > rk1min)) {
+            rmin = find_root_vr(o, kmin, prec, maxit, err);
+            if (*err) return res;
+        }
+    } else {
+        rmin = J * J / (-a + sqrt(inside_sqrt));
+    }
+    const double dQdr_min = 2.0 * J * J / (rmin * rmin * rmin) + 2.0 * a / (rmin * rmin);
+    set_a_b(o, kmax, &a, &b);
+    inside_sqrt = a * a - 2.0 * J * J * (b - E);
+    if (inside_sqrt < 0.0) {
+        rmax = -a / (2.0 * (b - E));
+        if ((rmax < rkmax) || (rmax > rk1max)) {
+            rmax = find_root_vr(o, kmax, prec, maxit, err);
+            if (*err) return res;
+        }
+    } else {
+        rmax = (-a + sqrt(inside_sqrt)) / (2.0 * (b - E));
+    }
+    const double dQdr_max = 2.0 * J * J / (rmax * rmax * rmax) + 2.0 * a / (rmax * rmax);
+    if ((rmin > rmax) || (dQdr_min <= 0.) || (dQdr_max >= 0.)) return res;
+    res.circular = 0;
+    res.rp = rmin;
+    res.ra = rmax;
+    res.dQdrp = dQdr_min;
+    res.dQdra = dQdr_max;
+    return res;
+}
+
+// destroy_obj (cmc_dynamics_helper.c:131-150) on the device arrays: zero the
+// record, keep r and phi, send the star to SF_INFINITY with mass DBL_MIN.
+static __device__ __forceinline__ void destroy_obj(const Fields &f, long long g)
+{
+    f.E[g] = 0.0;
+    f.J[g] = 0.0;
+    f.X[g] = 0.0;
+    f.Y[g] = 0.0;
+    f.r_peri[g] = 0.0;
+    f.r_apo[g] = 0.0;
+    f.id[g] = 0;
+    f.ec_pre[g] = 0.0;
+    f.rnew[g] = CMCG_SF_INFINITY;
+    f.vrnew[g] = 0.0;
+    f.vtnew[g] = 0.0;
+    f.m[g] = CMCG_DBL_MIN;
+}
+
+__global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                 double *partials, unsigned int *tickets)
+{
+    __shared__ double red[ORB_T / 32];
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    const long long off = C.off;
+    const long long N_MAX = sc->N_MAX, N_NEW = sc->N_MAX_NEW;
+    const double invN = 1.0 / (double)sc->N_STAR;
+    const double Rtidal = sc->Rtidal;
+    const long long j = 1 + (long long)ct.y * ORB_T + threadIdx.x;
+    const long long g = off + j;
+
+    double acc_E = 0.0, acc_J = 0.0, acc_M = 0.0, acc_Et = 0.0, max_rad = 0.0;
+    if (j <= N_NEW) {
+        const double Ej = f.E[g], Jj = f.J[g], rj = f.r[g], mj = f.m[g], phij = f.phi[g];
+        const double vr0 = f.vr_rel[g], vt0 = f.vt_rel[g];
+        const long long idj = f.id[g];
+        const double ps = phi_s(rj, rj, mj, invN);
+        const double E = Ej + ps;
+        const double J = Jj;
+        // energy_conservation1: vtold, vrold, Uoldrold
+        const double Uoldrold = phij + ps;
+        const double vold2 = vt0 * vt0 + vr0 * vr0;
+        if (mj < CMCG_ZERO) {
+            destroy_obj(f, g);
+        } else if (E >= 0.0) {
+            // remove_star, cmc_evolution_thr.c:655-716
+            acc_E = Ej * mj / (double)sc->N_STAR;
+            acc_J = Jj * mj / (double)sc->N_STAR;
+            acc_M = mj / (double)sc->N_STAR;
+            acc_Et = Ej * mj / (double)sc->N_STAR;
+            destroy_obj(f, g);
+        } else {
+            OrbitCtx o;
+            o.r = f.r + off;
+            o.phi = f.phi + off;
+            o.inv_r = f.inv_r + off;
+            o.N_MAX = N_MAX;
+            o.E = E;
+            o.J = J;
+            o.rj = rj;
+            o.mj = mj;
+            o.invN = invN;
+            o.cenma_m = sc->cenma_m;
+            o.madhoc = sc->madhoc;
+            int err = 0;
+            const OrbitRs orb = calc_orbit_new(o, j, C.apsides_precision, C.apsides_max_iter, &err);
+            if (err) {
+                set_error(sc, err, j);
+            } else if (orb.circular) {
+                // cmc_evolution_thr.c:835-840: position and velocities unchanged
+                f.rnew[g] = rj;
+                f.vrnew[g] = vr0;
+                f.vtnew[g] = vt0;
+                bool ok = true;
+                int pok = 1;
+                const double Uoldrnew = potential_at(o.r, o.phi, o.inv_r, N_MAX, rj, &pok) + phi_s(rj, rj, mj, invN);
+                ok = pok;
+                if (!ok) set_error(sc, CMCG_ERR_FINDZERO_R, j);
+                f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - Uoldrnew);
+            } else if (orb.ra >= Rtidal) {
+                acc_E = Ej * mj / (double)sc->N_STAR;
+                acc_J = Jj * mj / (double)sc->N_STAR;
+                acc_M = mj / (double)sc->N_STAR;
+                acc_Et = Ej * mj / (double)sc->N_STAR;
+                destroy_obj(f, g);
+            } else {
+                const double rmin = orb.rp, rmax = orb.ra;
+                const double g1 = sqrt(3.0 * (rmax - rmin) / orb.dQdrp);
+                const double g2 = sqrt(-3.0 * (rmax - rmin) / orb.dQdra);
+                const double F = 1.2 * (g1 >= g2 ? g1 : g2);
+                double r = 0.0, vr = 0.0, X = 0.0, pot = 0.0;
+                long long k;
+                const long long tcount = sc->tcount;
+                bool bad = false;
+                for (k = 1; k <= C.n_try; k++) {
+                    const uint4 u = draw_block(C.seed, tcount, SITE_TRIAL, idj, (unsigned int)(k - 1));
+                    X = u01(u.x);
+                    const double s0 = 2.0 * X - 1.0;
+                    const double g0 = F * u01(u.y);
+                    r = 0.5 * (rmin + rmax) + 0.25 * (rmax - rmin) * (3.0 * s0 - s0 * s0 * s0);
+                    int pok = 1;
+                    pot = potential_at(o.r, o.phi, o.inv_r, N_MAX, r, &pok) + phi_s(r, rj, mj, invN);
+                    if (!pok) {
+                        set_error(sc, CMCG_ERR_FINDZERO_R, j);
+                        bad = true;
+                        break;
+                    }
+                    const double drds = 0.25 * (rmax - rmin) * (3.0 - 3.0 * s0 * s0);
+                    const double Q = 2.0 * E - 2.0 * pot - J * J / r / r;
+                    if (Q >= 0.0) {
+                        vr = sqrt(Q);
+                    } else {
+                        if (isnan(Q)) {
+                            set_error(sc, CMCG_ERR_Q_NAN, j);
+                            bad = true;
+                            break;
+                        }
+                        vr = 0;
+                    }
+                    if (g0 < 1.0 / vr * drds) break;
+                }
+                if (!bad && k == C.n_try + 1) {
+                    set_error(sc, CMCG_ERR_NTRY, j);
+                    bad = true;
+                }
+                if (!bad) {
+                    f.X[g] = X;
+                    f.r_peri[g] = rmin;
+                    f.r_apo[g] = rmax;
+                    if (u01(draw_block(C.seed, tcount, SITE_SIGN, idj, 0u).x) < 0.5) vr = -vr;
+                    const double vt = J / r;
+                    f.rnew[g] = r;
+                    f.vrnew[g] = vr;
+                    f.vtnew[g] = vt;
+                    if (r > max_rad) max_rad = r;
+                    // energy_conservation2: Uoldrnew = potential(rnew) + PHI_S(rnew)
+                    f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - pot);
+                }
+            }
+        }
+    }
+    const double tE = block_sum<ORB_T>(acc_E, red);
+    const double tJ = block_sum<ORB_T>(acc_J, red);
+    const double tM = block_sum<ORB_T>(acc_M, red);
+    const double tEt = block_sum<ORB_T>(acc_Et, red);
+    const double tmax = block_max<ORB_T>(max_rad, red);
+    if (threadIdx.x == 0) {
+        double *slot = partials + (size_t)blockIdx.x * ORB_NPART;
+        slot[0] = tE;
+        slot[1] = tJ;
+        slot[2] = tM;
+        slot[3] = tEt;
+        slot[4] = tmax;
+        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
+            double a[ORB_NPART] = {0.0, 0.0, 0.0, 0.0, 0.0};
+            const int b0 = tm.first[ct.x];
+            for (int b = 0; b < tm.count[ct.x]; ++b) {
+                const double *s = partials + (size_t)(b0 + b) * ORB_NPART;
+                a[0] += s[0];
+                a[1] += s[1];
+                a[2] += s[2];
+                a[3] += s[3];
+                a[4] = fmax(a[4], s[4]);
+            }
+            // new_orbits_calculate, cmc_utils.c:2197-2210
+            sc->OldTidalMassLoss = sc->TidalMassLoss_old;
+            sc->Eescaped += a[0];
+            sc->Jescaped += a[1];
+            sc->TidalMassLoss += a[2];
+            sc->Etidal += a[3];
+            sc->max_r = a[4];
+            sc->TidalMassLoss += sc->TidalMassLoss_old;
+        }
+    }
+}
+
+// One pass of tidally_strip_stars, cmc_evolution_thr.c:459-622.
+__global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                       double *partials, unsigned int *tickets)
+{
+    __shared__ double red[TID_THREADS / 32];
+    __shared__ double s_phi_rt, s_Rtidal;
+    __shared__ int s_ok;
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    if (sc->tidal_done) return;
+    const long long off = C.off;
+    const double NSTAR = (double)sc->N_STAR;
+    if (threadIdx.x == 0) {
+        const double Rt = sc->orbit_r * pow(sc->Mtotal - (sc->TidalMassLoss - sc->OldTidalMassLoss), 1.0 / 3.0);
+        int pok = 1;
+        s_phi_rt = potential_at(f.r + off, f.phi + off, f.inv_r + off, sc->N_MAX, Rt, &pok);
+        s_ok = pok;
+        s_Rtidal = Rt;
+    }
+    __syncthreads();
+    const double phi_rtidal = s_phi_rt, Rtidal = s_Rtidal;
+    const double gierszalpha = 1.5 - 3.0 * pow(log(C.GAMMA * NSTAR) / NSTAR, 0.25);
+    double aE = 0.0, aJ = 0.0, aM = 0.0, aEt = 0.0;
+    const long long N_NEW = sc->N_MAX_NEW;
+    for (int it = 0; it < TID_T / TID_THREADS; ++it) {
+        const long long i = 1 + (long long)ct.y * TID_T + it * TID_THREADS + threadIdx.x;
+        if (i > N_NEW) break;
+        const long long g = off + i;
+        const double rn = f.rnew[g];
+        bool strip;
+        if (C.TIDAL_TREATMENT == 0)
+            strip = (f.r_apo[g] > Rtidal && rn < 1000000);
+        else
+            strip = (f.E[g] > gierszalpha * phi_rtidal && rn < 1000000);
+        if (strip) {
+            const double m = f.m[g], E = f.E[g], J = f.J[g];
+            aE += E * m / NSTAR;
+            aJ += J * m / NSTAR;
+            aM += m / NSTAR;
+            aEt += E * m / NSTAR;
+            destroy_obj(f, g);
+        }
+    }
+    const double tE = block_sum<TID_THREADS>(aE, red);
+    const double tJ = block_sum<TID_THREADS>(aJ, red);
+    const double tM = block_sum<TID_THREADS>(aM, red);
+    const double tEt = block_sum<TID_THREADS>(aEt, red);
+    if (threadIdx.x == 0) {
+        double *slot = partials + (size_t)blockIdx.x * TID_NPART;
+        slot[0] = tE;
+        slot[1] = tJ;
+        slot[2] = tM;
+        slot[3] = tEt;
+        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
+            double a[TID_NPART] = {0.0, 0.0, 0.0, 0.0};
+            const int b0 = tm.first[ct.x];
+            for (int b = 0; b < tm.count[ct.x]; ++b)
+                for (int q = 0; q < TID_NPART; ++q) a[q] += partials[(size_t)(b0 + b) * TID_NPART + q];
+            if (!s_ok) set_error(sc, CMCG_ERR_FINDZERO_R, 0);
+            if (sc->tidal_iters == 0) sc->Etidal = 0.0;  // cmc_evolution_thr.c:452
+            sc->Rtidal = Rtidal;
+            sc->phi_rtidal = phi_rtidal;
+            sc->Eescaped += a[0];
+            sc->Jescaped += a[1];
+            sc->Etidal += a[3];
+            sc->DTidalMassLoss = a[2];
+            sc->TidalMassLoss += a[2];
+            sc->tidal_iters += 1;
+            if (!(a[2] > 0)) sc->tidal_done = 1;
+        }
+    }
+}
+
+// After the bounded passes: a cluster still shedding stars is an error.
+__global__ void k_tidal_check(const Cluster *__restrict__ cls, int nclusters)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nclusters) return;
+    Scalars *sc = cls[c].sc;
+    if (!sc->tidal_done) set_error(sc, CMCG_ERR_TIDAL_ITER, sc->tidal_iters);
+}
+
+// potential(r) for one radius of cluster c (host queries, energy bookkeeping).
+__global__ void k_potential_query(const Cluster *__restrict__ cls, Fields f, int c, double x, double *out)
+{
+    const Cluster &C = cls[c];
+    int ok = 1;
+    out[0] = potential_at(f.r + C.off, f.phi + C.off, f.inv_r + C.off, C.sc->N_MAX, x, &ok);
+    out[1] = ok ? 0.0 : 1.0;
+}
+
+}  // namespace cmcg

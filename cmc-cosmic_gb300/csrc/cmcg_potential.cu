@@ -1,0 +1,234 @@
+// cmcg_potential.cu -- potential_calculate (cmc_utils.c:675-736) as a scan.
+//
+// The reference walks k = N..1 with
+//     Phi_k = Phi_{k+1} - M_k (1/r_k - 1/r_{k+1}),   M_{k-1} = M_k - m_k/N_STAR,
+// starting from M_N = Mtotal.  Written as sums:
+//     M_k   = Mtotal - sum_{j>k} q_j,                 q_j = m_j / N_STAR
+//     Phi_k = -sum_{j>=k} M_j d_j,                    d_j = 1/r_j - 1/r_{j+1}
+// Tiles of 1024 stars are taken from the outside in.  A tile's effect on the
+// running (Q, D) = (sum q, sum M d) is linear in the Q entering it, so each
+// tile is summarised by (q_T, Delta_T, C_T) = (sum q, sum d, sum Qin_p d_p)
+// with the associative combine (outer A, inner B) ->
+//     (q_A + q_B, Delta_A + Delta_B, C_A + C_B + q_A Delta_B),
+// and the D entering a tile is Mtotal * Delta_before - C_before.
+//   k_pot_agg    per tile: q_j, 1/r_j (stored), the triple, and sum m_j
+//   k_pot_carry  per cluster: Mtotal, Rtidal, scan of the triples over tiles
+//   k_pot_apply  per tile: M_k, Phi_k, sentinels (Phi_0, Phi_{N+1}, r_{N+1})
+#include "cmcg_kernels.cuh"
+
+namespace cmcg {
+
+
+static __device__ __forceinline__ double r_at(const double *r, long long k, long long N)
+{
+    return k == N + 1 ? CMCG_SF_INFINITY : r[k];
+}
+
+// inclusive block scan (blocked arrangement: thread t holds items t*4..t*4+3)
+template <int NT>
+static __device__ __forceinline__ double block_excl_prefix(double tsum, double *s_w)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) s_w[w] = x;
+    __syncthreads();
+    double b = 0.0;
+    for (int q = 0; q < w; ++q) b += s_w[q];
+    return b + x - tsum;  // exclusive prefix of this thread
+}
+
+__global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                          PotBufs pb)
+{
+    __shared__ double s_w[POT_THREADS / 32];
+    __shared__ double s_lastinv[POT_THREADS / 32];
+    __shared__ double red[POT_THREADS / 32];
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    const long long N = sc->N_MAX, off = C.off;
+    const double NSTAR = (double)sc->N_STAR;
+    const long long kstart = N - (long long)ct.y * POT_T;  // largest k of this tile
+    const double *r = f.r + off, *m = f.m + off;
+    double q[POT_ITEMS], inv[POT_ITEMS], mm[POT_ITEMS];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        if (k >= 1) {
+            mm[i] = m[k];
+            q[i] = mm[i] / NSTAR;
+            inv[i] = __drcp_rn(r[k]);
+            pb.q[off + k] = q[i];
+            f.inv_r[off + k] = inv[i];
+        } else {
+            mm[i] = q[i] = inv[i] = 0.0;
+        }
+    }
+    // inv of k+1 for item 0 comes from the previous thread's item 3
+    double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
+    if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
+    __syncthreads();
+    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : __drcp_rn(r_at(r, kstart + 1, N));
+    double d[POT_ITEMS];
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        const double innext = (i == 0) ? up : inv[i - 1];
+        d[i] = (k >= 1) ? inv[i] - innext : 0.0;
+    }
+    // exclusive prefix of q in processing order -> C = sum Qexcl * d
+    double tq = 0.0;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) tq += q[i];
+    const double qex = block_excl_prefix<POT_THREADS>(tq, s_w);
+    double run = qex, tc = 0.0, td = 0.0, tm_ = 0.0;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        tc += run * d[i];
+        run += q[i];
+        td += d[i];
+        tm_ += mm[i];
+    }
+    const double Sq = block_sum<POT_THREADS>(tq, red);
+    const double Sd = block_sum<POT_THREADS>(td, red);
+    const double Sc = block_sum<POT_THREADS>(tc, red);
+    const double Sm = block_sum<POT_THREADS>(tm_, red);
+    if (t == 0) {
+        double *a = pb.agg + (size_t)blockIdx.x * 4;
+        a[0] = Sq;
+        a[1] = Sd;
+        a[2] = Sc;
+        a[3] = Sm;
+    }
+}
+
+// One block per cluster: Mtotal, Rtidal and the carries entering each tile.
+__global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__restrict__ cls, Tiles tm, PotBufs pb,
+                                                            int nclusters)
+{
+    __shared__ double s_a[POT_THREADS][3];
+    __shared__ double s_m[POT_THREADS];
+    const int c = blockIdx.x;
+    if (c >= nclusters) return;
+    const Cluster &C = cls[c];
+    Scalars *sc = C.sc;
+    const int ntiles = tm.count[c], b0 = tm.first[c];
+    const long long N = sc->N_MAX;
+    const int t = threadIdx.x;
+    const int per = (ntiles + POT_THREADS - 1) / POT_THREADS;
+    const int lo = t * per, hi = min(ntiles, lo + per);
+    // chunk aggregate (outer tiles first) and mass sum
+    double q = 0.0, D = 0.0, Cc = 0.0, sm = 0.0;
+    for (int i = lo; i < hi; ++i) {
+        const double *a = pb.agg + (size_t)(b0 + i) * 4;
+        Cc = Cc + a[2] + q * a[1];
+        q += a[0];
+        D += a[1];
+        sm += a[3];
+    }
+    s_a[t][0] = q;
+    s_a[t][1] = D;
+    s_a[t][2] = Cc;
+    s_m[t] = sm;
+    __syncthreads();
+    if (t == 0) {
+        // mass: sum over tiles (N_MAX unchanged: every kept star has r < SF_INFINITY)
+        double msum = 0.0;
+        for (int i = 0; i < POT_THREADS; ++i) msum += s_m[i];
+        sc->cenma_m += 0.0;  // cenma.m_new is always zero on this path
+        sc->Mtotal = msum * sc->madhoc + sc->cenma_m * sc->madhoc;
+        sc->Rtidal = sc->orbit_r * pow(sc->Mtotal, 1.0 / 3.0);
+        // exclusive scan of the chunk triples
+        double eq = 0.0, eD = 0.0, eC = 0.0;
+        for (int i = 0; i < POT_THREADS; ++i) {
+            const double aq = s_a[i][0], aD = s_a[i][1], aC = s_a[i][2];
+            s_a[i][0] = eq;
+            s_a[i][1] = eD;
+            s_a[i][2] = eC;
+            eC = eC + aC + eq * aD;
+            eq += aq;
+            eD += aD;
+        }
+    }
+    __syncthreads();
+    const double Mtot = sc->Mtotal;
+    double eq = s_a[t][0], eD = s_a[t][1], eC = s_a[t][2];
+    for (int i = lo; i < hi; ++i) {
+        const double *a = pb.agg + (size_t)(b0 + i) * 4;
+        double *cr = pb.carry + (size_t)(b0 + i) * 2;
+        cr[0] = eq;
+        cr[1] = Mtot * eD - eC;
+        eC = eC + a[2] + eq * a[1];
+        eq += a[0];
+        eD += a[1];
+    }
+    (void)N;
+}
+
+__global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                            PotBufs pb)
+{
+    __shared__ double s_w[POT_THREADS / 32];
+    __shared__ double s_lastinv[POT_THREADS / 32];
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    const long long N = sc->N_MAX, off = C.off;
+    const long long kstart = N - (long long)ct.y * POT_T;
+    double *r = f.r + off, *phi = f.phi + off, *inv_r = f.inv_r + off;
+    const double Mtot = sc->Mtotal;
+    const double Qin = pb.carry[(size_t)blockIdx.x * 2], Din = pb.carry[(size_t)blockIdx.x * 2 + 1];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    double q[POT_ITEMS], inv[POT_ITEMS];
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        q[i] = (k >= 1) ? pb.q[off + k] : 0.0;
+        inv[i] = (k >= 1) ? inv_r[k] : 0.0;
+    }
+    double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
+    if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
+    __syncthreads();
+    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : __drcp_rn(r_at(r, kstart + 1, N));
+    double tq = 0.0;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) tq += q[i];
+    const double qex = block_excl_prefix<POT_THREADS>(tq, s_w);
+    double dk[POT_ITEMS], run = qex, td = 0.0;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        const double innext = (i == 0) ? up : inv[i - 1];
+        const double Mk = (Mtot - Qin) - run;  // mprev when the reference reaches k
+        dk[i] = (k >= 1) ? Mk * (inv[i] - innext) : 0.0;
+        run += q[i];
+        td += dk[i];
+    }
+    const double dex = block_excl_prefix<POT_THREADS>(td, s_w);
+    double acc = Din + dex;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        acc += dk[i];
+        if (k >= 1) {
+            const double ph = -acc;
+            phi[k] = ph;
+            if (k == 1) phi[0] = ph + sc->cenma_m * sc->madhoc / r[1];
+        }
+    }
+    if (ct.y == 0 && t == 0) {
+        r[N + 1] = CMCG_SF_INFINITY;
+        phi[N + 1] = 0.0;
+        inv_r[N + 1] = __drcp_rn(CMCG_SF_INFINITY);
+        inv_r[0] = __drcp_rn(r[0]);
+    }
+}
+
+}  // namespace cmcg

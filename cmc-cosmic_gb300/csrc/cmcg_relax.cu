@@ -1,0 +1,381 @@
+// cmcg_relax.cu -- time step and the fused relaxation kernel.
+//
+// k_timestep restates simul_relax_new (cmc_dynamics_helper.c:2526-2579) and
+// calc_timestep (cmc_utils.c:2132-2148): one thread per 2p-star block, the
+// block sums taken in the reference's order, so Dt is bit-identical.
+//
+// k_relax restates dynamics_apply (cmc_dynamics.c:17-542, relaxation branch
+// 427-497) with calc_encounter_dyns, calc_n_local and set_star_EJ
+// (cmc_dynamics_helper.c:768-882) and calc_sigma_r (2821-2986) in one pass:
+// a block owns 256 consecutive stars (128 neighbour pairs (2k-1, 2k) in the
+// reference's 1-based numbering), stages m*v^2 and m of its stars plus a p-star
+// halo in shared memory to form the sliding-window sigma, then relaxes its
+// pairs.  Velocities after relaxation go to separate arrays so that no block
+// ever reads a neighbour's updated velocities in its sigma halo.
+#include "cmcg_kernels.cuh"
+#include "cmcgpu.h"
+
+namespace cmcg {
+
+
+static __device__ __forceinline__ double sqr(double x) { return x * x; }
+static __device__ __forceinline__ double cub(double x) { return x * x * x; }
+
+// calc_n_local, cmc_dynamics_helper.c:768-786
+static __device__ __forceinline__ double n_local_at(const double *__restrict__ r, long long k, long long p,
+                                                    long long N_LIMIT)
+{
+    long long kmin = k - p, kmax = k + p;
+    if (kmin < 0) {
+        kmin = 0;
+        kmax = 2 * p + 1;
+    } else if (kmax > N_LIMIT) {
+        kmax = N_LIMIT;
+        kmin = N_LIMIT - 2 * p - 1;
+    }
+    return (2.0 * ((double)p)) * 3.0 / (4.0 * CMCG_PI * (cub(r[kmax]) - cub(r[kmin])));
+}
+
+// ------------------------------------------------------------ time step --
+__global__ void __launch_bounds__(128) k_timestep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                  double *partials, unsigned int *tickets)
+{
+    __shared__ double red[4];
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    const long long N = sc->N_MAX, p = C.p;
+    const double madhoc = sc->madhoc;
+    const double *r = f.r + C.off, *m = f.m + C.off, *vr = f.vr + C.off, *vt = f.vt + C.off;
+    double dtmin = INFINITY;
+    if (C.RELAXATION && N >= 2 * p + 2) {
+        // windows si = 1 + p + 2p w whose si lies in this block's star range
+        const long long s_lo = 1 + (long long)ct.y * TS_T, s_hi = s_lo + TS_T;
+        long long w0 = (s_lo - 1 - p + 2 * p - 1) / (2 * p);
+        if (s_lo - 1 - p < 0) w0 = 0;
+        for (long long w = w0 + threadIdx.x;; w += blockDim.x) {
+            const long long si = 1 + p + 2 * p * w;
+            if (si >= s_hi || !(si < N + 1 - p)) break;
+            if (si < s_lo) continue;
+            const long long simin = si - p, simax = simin + (2 * p - 1);
+            double Mv2ave = 0.0, Mave = 0.0, M2ave = 0.0;
+            for (long long k = simin; k <= simax; k++) {
+                const double tmp = m[k] * madhoc;
+                Mv2ave += tmp * (sqr(vr[k]) + sqr(vt[k]));
+                Mave += tmp;
+                M2ave += sqr(tmp);
+            }
+            Mv2ave /= (double)(2 * p);
+            Mave /= (double)(2 * p);
+            M2ave /= (double)(2 * p);
+            const double sigma = sqrt(Mv2ave / Mave);
+            const double W = 4.0 * sigma / sqrt(3.0 * CMCG_PI);
+            const double nl = n_local_at(r, si, p, N);
+            const double dt = sqr(2.0 * C.THETASEMAX / CMCG_PI) * (CMCG_PI / 32.0) * cub(W) /
+                              (((double)sc->N_STAR) * nl * (4.0 * M2ave));
+            dtmin = fmin(dtmin, dt);
+        }
+    }
+    // exact min over blocks (min is order independent)
+    const double bmin = -block_max<128>(-dtmin, red);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bmin;
+        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
+            double Dt = INFINITY;
+            const int b0 = tm.first[ct.x];
+            for (int b = 0; b < tm.count[ct.x]; ++b) Dt = fmin(Dt, partials[b0 + b]);
+            if (!C.RELAXATION) Dt = INFINITY;
+            // GetTimeStep, cmc_evolution_thr.c:420: all other time scales are infinite
+            if (isinf(Dt)) Dt = 0.001;
+            // calc_timestep, cmc_utils.c:2138-2144
+            if ((sc->TidalMassLoss_old - sc->OldTidalMassLoss) > 0.01) {
+                Dt = sc->Prev_Dt * 0.8;
+            } else if (Dt > 1.1 * sc->Prev_Dt && sc->Prev_Dt > 0 &&
+                       (sc->TidalMassLoss - sc->OldTidalMassLoss) > 0.02) {
+                Dt = sc->Prev_Dt * 1.1;
+            }
+            sc->Dt = Dt;
+            sc->TotalTime += Dt;
+        }
+    }
+}
+
+// ------------------------------------------------------------ relaxation --
+template <bool FP32>
+static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                  double *partials, unsigned int *tickets, double dt_override)
+{
+    __shared__ double s_w[RELAX_T + 3 * PMAX + 8];
+    __shared__ double s_m[RELAX_T + 3 * PMAX + 8];
+    __shared__ double s_tot[2][RELAX_THREADS / 32];
+    __shared__ double red[RELAX_THREADS / 32];
+
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    Scalars *sc = C.sc;
+    const long long N = sc->N_MAX, p = C.p;
+    const double madhoc = sc->madhoc, NSTAR = (double)sc->N_STAR;
+    const double dt = dt_override >= 0.0 ? dt_override : sc->Dt;
+    const long long tcount = sc->tcount;
+    const long long off = C.off;
+    const double *__restrict__ r = f.r + off, *__restrict__ m = f.m + off, *__restrict__ phi = f.phi + off;
+    const double *__restrict__ vr = f.vr + off, *__restrict__ vt = f.vt + off;
+    const long long *__restrict__ id = f.id + off;
+    const long long t0 = 1 + (long long)ct.y * RELAX_T;
+    const int tid = threadIdx.x;
+
+    // ---- sliding-window sigma (calc_sigma_r): prefix sums over the staged range
+    // the reference's windows assume at least 2p+2 stars; below that they index
+    // outside the star array, so such a cluster is left unrelaxed
+    const bool live = (t0 <= N) && (N >= 2 * p + 2);
+    long long lo_load = 1, hi_load = 0;
+    if (live) {
+        lo_load = t0 - p;
+        if (N - 2 * p + 1 < lo_load) lo_load = N - 2 * p + 1;
+        if (lo_load < 1) lo_load = 1;
+        hi_load = t0 + RELAX_T - 1 + p - 1;
+        if (hi_load < 2 * p) hi_load = 2 * p;
+        if (hi_load > N) hi_load = N;
+    }
+    const int L = (int)(hi_load - lo_load + 1);
+    const int chunk = (L + RELAX_THREADS - 1) / RELAX_THREADS;
+    double accw = 0.0, accm = 0.0;
+    for (int i = tid * chunk; i < L && i < (tid + 1) * chunk; ++i) {
+        const long long k = lo_load + i;
+        const double vrk = vr[k], vtk = vt[k];
+        const double mm = m[k] * madhoc;
+        const double w = mm * (sqr(vrk) + sqr(vtk));
+        accw += w;
+        accm += mm;
+        s_w[i] = accw;
+        s_m[i] = accm;
+    }
+    // exclusive scan of the per-thread totals
+    {
+        double xw = accw, xm = accm;
+        const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double yw = __shfl_up_sync(0xffffffffu, xw, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
+            if (lane >= o) {
+                xw += yw;
+                xm += ym;
+            }
+        }
+        if (lane == 31) {
+            s_tot[0][wid] = xw;
+            s_tot[1][wid] = xm;
+        }
+        __syncthreads();
+        double bw = 0.0, bm = 0.0;
+        for (int q = 0; q < wid; ++q) {
+            bw += s_tot[0][q];
+            bm += s_tot[1][q];
+        }
+        const double ew = bw + xw - accw, em = bm + xm - accm;  // exclusive offsets
+        for (int i = tid * chunk; i < L && i < (tid + 1) * chunk; ++i) {
+            s_w[i] += ew;
+            s_m[i] += em;
+        }
+    }
+    __syncthreads();
+
+    double part[RELAX_NPART];
+#pragma unroll
+    for (int i = 0; i < RELAX_NPART; ++i) part[i] = 0.0;
+
+    if (live) {
+        double *sig_r = f.sigma_r + off, *sig = f.sigma + off;
+        for (int h = 0; h < 2; ++h) {
+            const long long si = t0 + 2 * tid + h;
+            if (si > N) break;
+            long long lo = si - p, hi = lo + (2 * p - 1);
+            if (lo < 1) {
+                lo = 1;
+                hi = 2 * p;
+            } else if (hi > N) {
+                hi = N;
+                lo = hi - (2 * p - 1);
+            }
+            const int a = (int)(lo - lo_load) - 1, b = (int)(hi - lo_load);
+            const double Mv2 = s_w[b] - (a >= 0 ? s_w[a] : 0.0);
+            const double Mm = s_m[b] - (a >= 0 ? s_m[a] : 0.0);
+            sig_r[si] = r[si];
+            sig[si] = sqrt(Mv2 / Mm);
+        }
+    }
+
+    // ---- neighbour pairs (k, k+1), k = t0 + 2 tid
+    const long long k = t0 + 2 * tid, kp = k + 1;
+    double *vr_o = f.vr_rel + off, *vt_o = f.vt_rel + off;
+    if (k <= N) {
+        if (!C.PERTURB || !(k <= N - N % 2 - 1) || N < 2 * p + 2) {
+            // unpaired last star (odd N) or no perturbation: velocities unchanged
+            vr_o[k] = vr[k];
+            vt_o[k] = vt[k];
+            if (kp <= N) {
+                vr_o[kp] = vr[kp];
+                vt_o[kp] = vt[kp];
+            }
+        } else {
+            const double vtk = vt[k], vrk = vr[k], vtkp = vt[kp], vrkp = vr[kp];
+            const double mass_k = m[k], mass_kp = m[kp];
+            const long long idk = id[k];
+            // calc_encounter_dyns, cmc_dynamics_helper.c:831-871
+            const double Y = u01(draw_block(C.seed, tcount, SITE_Y, idk, 0u).x);
+            f.Y[off + k] = Y;
+            f.Y[off + kp] = Y;
+            double v1 = vtk, v2 = 0.0, v3 = vrk, vp1, vp2, vp3 = vrkp, w1, w2, w3, W;
+            double vr_k, vt_k, vr_kp, vt_kp;
+            bool ok = true;
+            if (!FP32) {
+                const double ang = Y * 2.0 * CMCG_PI;
+                double sa, ca;
+                sincos(ang, &sa, &ca);
+                vp1 = vtkp * ca;
+                vp2 = vtkp * sa;
+                w1 = vp1 - v1;
+                w2 = vp2 - v2;
+                w3 = vp3 - v3;
+                W = sqrt(sqr(w1) + sqr(w2) + sqr(w3));
+            } else {
+                const float ang = (float)Y * 2.0f * (float)CMCG_PI;
+                float sa, ca;
+                sincosf(ang, &sa, &ca);
+                vp1 = (double)((float)vtkp * ca);
+                vp2 = (double)((float)vtkp * sa);
+                w1 = (double)((float)vp1 - (float)v1);
+                w2 = (double)((float)vp2);
+                w3 = (double)((float)vp3 - (float)v3);
+                W = (double)sqrtf((float)(w1 * w1 + w2 * w2 + w3 * w3));
+            }
+            if (W == 0.0) {
+                set_error(sc, CMCG_ERR_W_ZERO, k);
+                ok = false;
+            }
+            const double rcm = (m[k] * r[k] + m[kp] * r[kp]) / (m[k] + m[kp]);
+            const double n_local = n_local_at(r, k, p, N);
+            // S = 0: single-single with SS_COLLISION off, so P_enc = 0 and the
+            // encounter draw (cmc_dynamics.c:406) can never succeed.
+            double beta = 0.0;
+            if (ok && C.RELAXATION) {
+                const double Trel12 = (CMCG_PI / 32.0) * cub(W) / (NSTAR * n_local * sqr((mass_k + mass_kp) * madhoc));
+                beta = (CMCG_PI / 2.0) * sqrt(dt / Trel12);
+                const double relbeta[4] = {CMCG_PI / 2.0, CMCG_PI / 4.0, CMCG_PI / 8.0, CMCG_PI / 16.0};
+                part[0] += 1.0;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (beta > relbeta[i]) {
+                        part[1 + i] += 1.0;
+                        part[5 + i] += fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
+                        part[9 + i] += (mass_k + mass_kp) / 2.0;
+                        part[13 + i] += rcm;
+                    }
+                }
+                if (beta > CMCG_PI / 2.0) beta = CMCG_PI / 2.0;
+                const double psi = u01(draw_block(C.seed, tcount, SITE_PSI, idk, 0u).x) * 2 * CMCG_PI;
+                if (!FP32) {
+                    const double wp = sqrt(sqr(w1) + sqr(w2));
+                    if (wp == 0.0) {
+                        set_error(sc, CMCG_ERR_WP_ZERO, k);
+                        ok = false;
+                    } else {
+                        const double a1 = -w2 * W / wp, a2 = w1 * W / wp, a3 = 0.0;
+                        const double b1 = -w1 * w3 / wp, b2 = -w2 * w3 / wp, b3 = wp;
+                        double sb, cb, sp, cp;
+                        sincos(beta, &sb, &cb);
+                        sincos(psi, &sp, &cp);
+                        const double wn1 = w1 * cb + a1 * sb * cp + b1 * sb * sp;
+                        const double wn2 = w2 * cb + a2 * sb * cp + b2 * sb * sp;
+                        const double wn3 = w3 * cb + a3 * sb * cp + b3 * sb * sp;
+                        const double fk = mass_kp / (mass_k + mass_kp), fkp = mass_k / (mass_k + mass_kp);
+                        const double vn1 = v1 - fk * (wn1 - w1), vn2 = v2 - fk * (wn2 - w2), vn3 = v3 - fk * (wn3 - w3);
+                        const double pn1 = vp1 + fkp * (wn1 - w1), pn2 = vp2 + fkp * (wn2 - w2), pn3 = vp3 + fkp * (wn3 - w3);
+                        vr_k = vn3;
+                        vt_k = sqrt(sqr(vn1) + sqr(vn2));
+                        vr_kp = pn3;
+                        vt_kp = sqrt(sqr(pn1) + sqr(pn2));
+                    }
+                } else {
+                    const float fw1 = (float)w1, fw2 = (float)w2, fw3 = (float)w3, fW = (float)W;
+                    const float wp = sqrtf(fw1 * fw1 + fw2 * fw2);
+                    if (wp == 0.0f) {
+                        set_error(sc, CMCG_ERR_WP_ZERO, k);
+                        ok = false;
+                    } else {
+                        const float iwp = 1.0f / wp;
+                        const float a1 = -fw2 * fW * iwp, a2 = fw1 * fW * iwp;
+                        const float b1 = -fw1 * fw3 * iwp, b2 = -fw2 * fw3 * iwp, b3 = wp;
+                        float sb, cb, sp, cp;
+                        sincosf((float)beta, &sb, &cb);
+                        sincosf((float)psi, &sp, &cp);
+                        const float d1 = fw1 * (cb - 1.0f) + a1 * sb * cp + b1 * sb * sp;
+                        const float d2 = fw2 * (cb - 1.0f) + a2 * sb * cp + b2 * sb * sp;
+                        const float d3 = fw3 * (cb - 1.0f) + b3 * sb * sp;
+                        const float fk = (float)(mass_kp / (mass_k + mass_kp)), fkp = 1.0f - fk;
+                        const float vn1 = (float)v1 - fk * d1, vn2 = -fk * d2, vn3 = (float)v3 - fk * d3;
+                        const float pn1 = (float)vp1 + fkp * d1, pn2 = (float)vp2 + fkp * d2, pn3 = (float)vp3 + fkp * d3;
+                        vr_k = (double)vn3;
+                        vt_k = (double)sqrtf(vn1 * vn1 + vn2 * vn2);
+                        vr_kp = (double)pn3;
+                        vt_kp = (double)sqrtf(pn1 * pn1 + pn2 * pn2);
+                    }
+                }
+                if (ok) {
+                    vr_o[k] = vr_k;
+                    vt_o[k] = vt_k;
+                    vr_o[kp] = vr_kp;
+                    vt_o[kp] = vt_kp;
+                    // set_star_EJ, cmc_dynamics_helper.c:878-882 (FP64 energies)
+                    f.E[off + k] = phi[k] + 0.5 * (sqr(vr_k) + sqr(vt_k));
+                    f.J[off + k] = r[k] * vt_k;
+                    f.E[off + kp] = phi[kp] + 0.5 * (sqr(vr_kp) + sqr(vt_kp));
+                    f.J[off + kp] = r[kp] * vt_kp;
+                }
+            }
+            if (!ok || !C.RELAXATION) {
+                vr_o[k] = vrk;
+                vt_o[k] = vtk;
+                vr_o[kp] = vrkp;
+                vt_o[kp] = vtkp;
+            }
+        }
+    }
+
+    // ---- statistics (cmc_dynamics.c:430-440), deterministic block order
+    double tot[RELAX_NPART];
+#pragma unroll
+    for (int i = 0; i < RELAX_NPART; ++i) tot[i] = block_sum<RELAX_THREADS>(part[i], red);
+    if (tid == 0) {
+        double *slot = partials + (size_t)blockIdx.x * RELAX_NPART;
+        for (int i = 0; i < RELAX_NPART; ++i) slot[i] = tot[i];
+        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
+            double acc[RELAX_NPART];
+            for (int i = 0; i < RELAX_NPART; ++i) acc[i] = 0.0;
+            const int b0 = tm.first[ct.x];
+            for (int b = 0; b < tm.count[ct.x]; ++b)
+                for (int i = 0; i < RELAX_NPART; ++i) acc[i] += partials[(size_t)(b0 + b) * RELAX_NPART + i];
+            sc->Nrel = (long long)acc[0];
+            for (int i = 0; i < 4; ++i) {
+                sc->Nrelbeta[i] = (long long)acc[1 + i];
+                sc->qaverelbeta[i] = acc[5 + i];
+                sc->maverelbeta[i] = acc[9 + i];
+                sc->raverelbeta[i] = acc[13 + i];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(RELAX_THREADS) k_relax64(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                           double *partials, unsigned int *tickets, double dt)
+{
+    relax_body<false>(cls, tm, f, partials, tickets, dt);
+}
+
+__global__ void __launch_bounds__(RELAX_THREADS) k_relax32(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                           double *partials, unsigned int *tickets, double dt)
+{
+    relax_body<true>(cls, tm, f, partials, tickets, dt);
+}
+
+}  // namespace cmcg

@@ -1,0 +1,178 @@
+/*
+ * cmcgpu.h -- C ABI of libcmcgpu.so: CMC's Henon relaxation step on one GB300.
+ *
+ * The library keeps one or more star clusters resident in GPU memory as
+ * structure-of-arrays (FP64 radius, mass, velocities, energies, potential) and
+ * runs the reference's per-step hot path on them with hand-written sm_103a
+ * kernels: radius sort, potential prefix scan, fused relaxation, new orbits.
+ * The host glue between those phases (time step, Stodolkiewicz energy
+ * conservation, tidal stripping, energy sums) runs on the device as well, so a
+ * whole step needs no host round trip.
+ *
+ * Each phase entry point corresponds to one function of the reference's main
+ * loop (src/cmc/cmc.c:240-407); its comment names the reference definition it
+ * replaces.  The reference-named drop-in symbols (qsorts_new, dynamics_apply,
+ * get_positions, ...) that bind a host `star[]` array live in cmc_dropin.h.
+ *
+ * Conventions
+ *  - All functions return 0 (CMCG_OK) or a negative host error, or a positive
+ *    physics error raised on the device (the same conditions on which the
+ *    reference calls exit_cleanly(); the codes are listed below).
+ *  - Per-star arrays passed in or out are 0-based over the N current stars in
+ *    radial order; the library's internal arrays keep the reference's 1-based
+ *    layout with sentinels at 0 and N+1.
+ *  - Masses are passed in N-body units (total 1) and stored x N_STAR, as the
+ *    reference does (src/cmc/cmc_fits.c:99,123).
+ *  - A context is used from one host thread; calls are asynchronous on the
+ *    context's CUDA stream except where they return data.
+ *  - There is no CPU fallback: without a usable GPU, cmcg_create fails.
+ */
+#ifndef CMCGPU_H
+#define CMCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status ---- */
+enum {
+    CMCG_OK = 0,
+    CMCG_ERR_ARG = -1,
+    CMCG_ERR_CUDA = -2,
+    CMCG_ERR_CAPACITY = -3,
+    CMCG_ERR_NOMEM = -4,
+    CMCG_ERR_STATE = -5,
+    /* device-side physics errors; the reference site each one mirrors: */
+    CMCG_ERR_NAN_MASS = 1,      /* cmc_utils.c:688   NaN in the mass sum        */
+    CMCG_ERR_NAN_PHI = 2,       /* cmc_utils.c:718   NaN in the potential       */
+    CMCG_ERR_W_ZERO = 3,        /* cmc_dynamics_helper.c:858  W = 0             */
+    CMCG_ERR_WP_ZERO = 4,       /* cmc_dynamics.c:450  wp = 0                   */
+    CMCG_ERR_NTRY = 5,          /* cmc_evolution_thr.c:890  N_TRY exceeded      */
+    CMCG_ERR_Q_NAN = 6,         /* cmc_evolution_thr.c:877  vr^2 is NaN         */
+    CMCG_ERR_ROOT_SIGNS = 7,    /* cmc_nr.c:515   no sign change of vr^2        */
+    CMCG_ERR_ROOT_NOCONV = 8,   /* cmc_nr.c:572   apsis root not converged      */
+    CMCG_ERR_ROOT_NEG = 9,      /* cmc_nr.c:594   negative residual at apsis    */
+    CMCG_ERR_FINDZERO_R = 10,   /* cmc_utils.c:146  radius search failed        */
+    CMCG_ERR_POT_INTERVAL = 11, /* cmc_nr.c:240   radius outside interval       */
+    CMCG_ERR_ENCOUNTER = 12,    /* a strong-encounter draw hit (host physics)   */
+    CMCG_ERR_SPIN = 20,         /* a bounded cross-block wait gave up           */
+    CMCG_ERR_TIDAL_ITER = 21    /* tidal stripping did not settle               */
+};
+
+/* ------------------------------------------------------- parameters ----- */
+typedef struct {
+    long N_STAR;               /* clus.N_STAR; 0 = the N of the loaded model      */
+    long AVEKERNEL;            /* sliding-window half width p (default 20)        */
+    double GAMMA;              /* Coulomb logarithm factor (default 0.1)          */
+    double THETASEMAX;         /* max deflection for the time step (1.412)        */
+    int PERTURB, RELAXATION;   /* default 1, 1                                    */
+    int TIDALLY_STRIP_STARS;   /* default 1                                       */
+    int TIDAL_TREATMENT;       /* 0 = apocentre cut, 1 = Giersz energy cut (1)    */
+    double orbit_r;            /* R_MAX, the initial tidal radius                 */
+    double cenma_m;            /* central mass, stored x N (0)                    */
+    long apsides_max_iter;     /* APSIDES_MAX_ITER (100)                          */
+    double apsides_precision;  /* APSIDES_PRECISION (1e-11)                       */
+    double apsides_convergence;/* APSIDES_CONVERGENCE (5e-13)                     */
+    long n_try;                /* N_TRY (50000)                                   */
+    uint64_t seed;             /* IDUM: keys the counter-based draws              */
+    int relax_fp32;            /* 1 = FP32 relaxation kinematics, FP64 energies   */
+} cmcg_params;
+
+void cmcg_default_params(cmcg_params *p);
+
+/* ----------------------------------------------- synthetic clusters ----- */
+enum { CMCG_MODEL_PLUMMER = 0, CMCG_MODEL_KING = 1 };
+typedef struct {
+    int model;                 /* CMCG_MODEL_PLUMMER or CMCG_MODEL_KING           */
+    long N;                    /* number of objects                               */
+    double w0;                 /* King concentration W0                           */
+    int imf;                   /* 0 = equal masses, 1 = Kroupa (2001)             */
+    double binary_fraction;    /* fraction of composite (m1 + m2) objects         */
+    uint64_t seed;
+} cmcg_ic_spec;
+typedef struct {
+    double *r, *m, *vr, *vt;   /* caller-allocated, N each; sorted by r on return */
+    int64_t *id;               /* caller-allocated or NULL; ids 1..N              */
+    double rtid;               /* tidal radius of the model (R_MAX)               */
+} cmcg_ic;
+
+/* Seeded initial model in N-body units (E = -1/4). Host only, no GPU needed. */
+int cmcg_ic_generate(const cmcg_ic_spec *spec, cmcg_ic *out);
+/* Per-cluster seed for cluster `index` of an ensemble drawn from one master seed. */
+uint64_t cmcg_derive_seed(uint64_t master, uint64_t index);
+
+/* ---------------------------------------------------------- context ----- */
+typedef struct cmcg_ctx cmcg_ctx;
+
+/* One context holds `nclusters` independent clusters; every phase call runs
+ * all of them in one launch per kernel.  capacity[c] bounds cluster c's N. */
+int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_params *params);
+int cmcg_destroy(cmcg_ctx *ctx);
+/* Copies a model (host memory, pinned or pageable) into cluster c. */
+int cmcg_load(cmcg_ctx *ctx, int cluster, long N, const double *r, const double *m, const double *vr,
+              const double *vt, const int64_t *id);
+/* Start-up sequence of cmc.c:152-167: potential, then E, J and energies. */
+int cmcg_initialize(cmcg_ctx *ctx);
+/* Host-owned star state for cluster c, as the reference's host loop keeps it:
+ * per star r (star_r), m (star_m, i.e. x N_STAR), vr, vt, E, J, id; 0-based, N
+ * stars.  put replaces the device copy (scalars are kept), get reads it back
+ * and returns N.  Both are asynchronous when the buffers are pinned; get
+ * synchronises before returning. */
+int cmcg_put_stars(cmcg_ctx *ctx, int cluster, long N, const double *r, const double *m, const double *vr,
+                   const double *vt, const double *E, const double *J, const int64_t *id);
+long cmcg_get_stars(cmcg_ctx *ctx, int cluster, long cap, double *r, double *m, double *vr, double *vt, double *E,
+                    double *J, int64_t *id);
+
+/* ------------------------------------------------ step phases (all clusters) */
+int cmcg_begin_step(cmcg_ctx *ctx);                /* cmc.c:246-257 tallies      */
+int cmcg_calc_timestep(cmcg_ctx *ctx);             /* cmc_utils.c:2132 calc_timestep */
+/* cmc_dynamics.c:17 dynamics_apply; dt < 0 uses the device time step. */
+int cmcg_dynamics_apply(cmcg_ctx *ctx, double dt);
+/* cmc_utils.c:2194 new_orbits_calculate (get_positions, cmc_evolution_thr.c:944)
+ * fused with energy_conservation1/2 (cmc_utils.c:2153, 2218). */
+int cmcg_new_orbits_calculate(cmcg_ctx *ctx);
+int cmcg_tidally_strip_stars(cmcg_ctx *ctx);       /* cmc_evolution_thr.c:443    */
+/* ComputeIntermediateEnergy's transfer (cmc_utils.c:368) + qsorts_new
+ * (cmc_utils.c:2232) + post_sort_comm (cmc_utils.c:2259). */
+int cmcg_qsorts_new(cmcg_ctx *ctx);
+int cmcg_calc_potential(cmcg_ctx *ctx);            /* cmc_utils.c:675 potential_calculate */
+int cmcg_energy_conservation3(cmcg_ctx *ctx);      /* cmc_utils.c:254 set_velocities3 */
+int cmcg_compute_energy(cmcg_ctx *ctx);            /* cmc_utils.c:2018 compute_energy_new */
+int cmcg_end_step(cmcg_ctx *ctx);                  /* tcount++                    */
+/* One whole step in main-loop order; with graphs enabled it replays a captured
+ * CUDA graph of the whole step. */
+int cmcg_step(cmcg_ctx *ctx);
+int cmcg_run(cmcg_ctx *ctx, int nsteps);
+int cmcg_use_graph(cmcg_ctx *ctx, int enable);
+int cmcg_synchronize(cmcg_ctx *ctx);
+
+/* ------------------------------------------------------------ queries --- */
+/* potential(r) of cmc_utils.c:112 for cluster c (synchronous). */
+int cmcg_potential(cmcg_ctx *ctx, int cluster, double r, double *out);
+/* Copies a per-star field (0-based, N_MAX_NEW values) or a global array
+ * ("star_r", "star_m", "star_phi", "sigma_r", "sigma": indices 0..N_MAX+1). */
+long cmcg_get_field(cmcg_ctx *ctx, int cluster, const char *name, double *out, long cap);
+long cmcg_set_field(cmcg_ctx *ctx, int cluster, const char *name, const double *in, long n);
+long cmcg_get_ids(cmcg_ctx *ctx, int cluster, int64_t *out, long cap);
+int cmcg_get_scalar(cmcg_ctx *ctx, int cluster, const char *name, double *out);
+int cmcg_set_scalar(cmcg_ctx *ctx, int cluster, const char *name, double v);
+long cmcg_nstars(cmcg_ctx *ctx, int cluster);
+/* First device error since the last call (0 if none), with cluster and star index. */
+int cmcg_last_error(cmcg_ctx *ctx, int *cluster, long *index);
+/* Kernel launches issued by the last cmcg_step / cmcg_run (graph nodes count). */
+long cmcg_launch_count(cmcg_ctx *ctx);
+/* Duration of the last launch of one kernel family, from CUDA events on the
+ * context stream ("sort", "potential", "relax", "orbit", ...); needs
+ * cmcg_profile(ctx, 1) before the step. */
+int cmcg_profile(cmcg_ctx *ctx, int enable);
+int cmcg_kernel_time(cmcg_ctx *ctx, const char *family, double *ms_total, long *launches);
+/* Counter-based uniform draw the kernels use (site, star id, n, word). */
+double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, int word);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

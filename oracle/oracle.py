@@ -1,0 +1,202 @@
+"""ctypes binding of the CPU oracle (TEST INFRASTRUCTURE).
+
+The oracle (cmc_oracle.c) restates the reference's single-rank Henon step in C
+and is the parity checker for the GPU kernels.  Only the tests, the smoke
+check and bench.py's CPU-baseline leg use it.
+
+``build()`` compiles it (and, where the reference tree is present, its own
+taus113 generator into oracle/_ref for pinning); the products go to
+oracle/_build and oracle/_ref, both outside version control.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libcmcoracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_TAUS = os.path.join(REF_DIR, "libtaus113ref.so")
+REFERENCE_ROOT = os.environ.get("CMC_REFERENCE_ROOT", "/root/reference")
+
+DRAW_COUNTER, DRAW_TAUS113 = 0, 1
+SITE_Y, SITE_PENC, SITE_PSI, SITE_TRIAL, SITE_SIGN = 1, 2, 3, 4, 5
+CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=gnu11"]
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "cmc_oracle.c")
+    hdr = os.path.join(HERE, "cmc_oracle.h")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        subprocess.check_call(["gcc", *CFLAGS, "-shared", "-o", LIB, src, "-lm"])
+    return LIB
+
+
+def build_ref() -> str | None:
+    """Compile the reference's own taus113-v2.c in place into oracle/_ref (pinning
+    the oracle's generator); returns None when the reference tree is absent."""
+    src = os.path.join(REFERENCE_ROOT, "src", "libs", "taus113-v2.c")
+    inc = os.path.join(REFERENCE_ROOT, "include", "common")
+    if not os.path.exists(src):
+        return None
+    os.makedirs(REF_DIR, exist_ok=True)
+    if not os.path.exists(REF_TAUS) or os.path.getmtime(REF_TAUS) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-I", inc, "-o", REF_TAUS, src])
+    return REF_TAUS
+
+
+class OParams(C.Structure):
+    _fields_ = [
+        ("N_STAR", C.c_long), ("AVEKERNEL", C.c_long), ("GAMMA", C.c_double), ("THETASEMAX", C.c_double),
+        ("PERTURB", C.c_int), ("RELAXATION", C.c_int), ("TIDALLY_STRIP_STARS", C.c_int),
+        ("TIDAL_TREATMENT", C.c_int), ("orbit_r", C.c_double), ("cenma_m", C.c_double),
+        ("apsides_max_iter", C.c_long), ("apsides_precision", C.c_double),
+        ("apsides_convergence", C.c_double), ("n_try", C.c_long), ("seed", C.c_uint64), ("draw_mode", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp = C.c_void_p
+        L.ocmc_default_params.argtypes = [C.POINTER(OParams)]
+        L.ocmc_create.argtypes = [C.POINTER(OParams), C.c_long, vp, vp, vp, vp, vp]
+        L.ocmc_create.restype = vp
+        L.ocmc_destroy.argtypes = [vp]
+        for n in ["ocmc_initialize", "ocmc_begin_step", "ocmc_calc_timestep", "ocmc_energy_conservation1",
+                  "ocmc_new_orbits_calculate", "ocmc_energy_conservation2", "ocmc_tidally_strip_stars",
+                  "ocmc_compute_intermediate_energy", "ocmc_qsorts_new", "ocmc_calc_potential",
+                  "ocmc_energy_conservation3", "ocmc_compute_energy", "ocmc_end_step", "ocmc_step",
+                  "ocmc_last_error", "ocmc_nstars"]:
+            getattr(L, n).argtypes = [vp]
+        L.ocmc_nstars.restype = C.c_long
+        L.ocmc_dynamics_apply.argtypes = [vp, C.c_double]
+        L.ocmc_potential.argtypes = [vp, C.c_double]
+        L.ocmc_potential.restype = C.c_double
+        L.ocmc_get_field.argtypes = [vp, C.c_char_p, vp, C.c_long]
+        L.ocmc_get_field.restype = C.c_long
+        L.ocmc_set_field.argtypes = [vp, C.c_char_p, vp, C.c_long]
+        L.ocmc_set_field.restype = C.c_long
+        L.ocmc_get_ids.argtypes = [vp, vp, C.c_long]
+        L.ocmc_get_ids.restype = C.c_long
+        L.ocmc_get_scalar.argtypes = [vp, C.c_char_p]
+        L.ocmc_get_scalar.restype = C.c_double
+        L.ocmc_set_scalar.argtypes = [vp, C.c_char_p, C.c_double]
+        L.ocmc_last_error_index.argtypes = [vp]
+        L.ocmc_last_error_index.restype = C.c_long
+        L.ocmc_draw.argtypes = [vp, C.c_int, C.c_int64, C.c_uint32, C.c_int]
+        L.ocmc_draw.restype = C.c_double
+        L.ocmc_philox4x32_10.argtypes = [vp, vp, vp]
+        L.ocmc_taus113_seed.argtypes = [vp, C.c_ulong]
+        L.ocmc_taus113_next.argtypes = [vp]
+        L.ocmc_taus113_next.restype = C.c_uint32
+        _lib = L
+    return _lib
+
+
+def default_params(**kw) -> OParams:
+    p = OParams()
+    lib().ocmc_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, where, index):
+        self.code, self.index = code, index
+        super().__init__(f"oracle {where}: error {code} at {index}")
+
+
+class Oracle:
+    """One cluster stepped by the CPU restatement of the reference."""
+
+    def __init__(self, ic: dict, params: OParams):
+        r, m, vr, vt = (np.ascontiguousarray(ic[k], dtype=np.float64) for k in ("r", "m", "vr", "vt"))
+        ids = np.ascontiguousarray(ic.get("id", np.arange(1, len(r) + 1)), dtype=np.int64)
+        self.params = params
+        self._h = lib().ocmc_create(C.byref(params), len(r), r.ctypes.data, m.ctypes.data, vr.ctypes.data,
+                                    vt.ctypes.data, ids.ctypes.data)
+        if not self._h:
+            raise ValueError("ocmc_create failed")
+
+    def close(self):
+        if self._h:
+            lib().ocmc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name, *args):
+        rc = getattr(lib(), name)(self._h, *args)
+        if rc:
+            raise OracleError(rc, name, lib().ocmc_last_error_index(self._h))
+
+    def __getattr__(self, item):
+        fn = "ocmc_" + item
+        if item.startswith("_") or not hasattr(lib(), fn):
+            raise AttributeError(item)
+        return lambda *a: self._call(fn, *a)
+
+    def get(self, name: str) -> np.ndarray:
+        n = lib().ocmc_nstars(self._h) + 2
+        out = np.zeros(n)
+        got = lib().ocmc_get_field(self._h, name.encode(), out.ctypes.data, n)
+        if got < 0:
+            raise KeyError(name)
+        return out[:got].copy()
+
+    def set(self, name: str, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if lib().ocmc_set_field(self._h, name.encode(), v.ctypes.data, len(v)) < 0:
+            raise KeyError(name)
+
+    def ids(self) -> np.ndarray:
+        n = lib().ocmc_nstars(self._h)
+        out = np.zeros(max(n, 1), np.int64)
+        got = lib().ocmc_get_ids(self._h, out.ctypes.data, len(out))
+        return out[:got].copy()
+
+    def scalar(self, name: str) -> float:
+        return float(lib().ocmc_get_scalar(self._h, name.encode()))
+
+    def set_scalar(self, name: str, v: float):
+        if lib().ocmc_set_scalar(self._h, name.encode(), float(v)):
+            raise KeyError(name)
+
+    def potential(self, r: float) -> float:
+        return float(lib().ocmc_potential(self._h, float(r)))
+
+    def nstars(self) -> int:
+        return int(lib().ocmc_nstars(self._h))
+
+    def draw(self, site, star_id, n, word):
+        return float(lib().ocmc_draw(self._h, site, star_id, n, word))
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().ocmc_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def taus113_stream(seed: int, n: int) -> np.ndarray:
+    z = (C.c_uint32 * 4)()
+    lib().ocmc_taus113_seed(z, seed)
+    return np.array([lib().ocmc_taus113_next(z) for _ in range(n)], dtype=np.uint64)

@@ -1,0 +1,177 @@
+"""Phase-by-phase parity of the sm_103a kernels against the CPU oracle.
+
+Each test brings the GPU context to the oracle's exact state, runs one phase
+on both, and compares: bit-exact where the arithmetic is a fixed sequence of
+IEEE operations (sort permutation, pairing, time step), within the stated
+relative tolerances elsewhere (see parity_util)."""
+import numpy as np
+import pytest
+
+import cmcgpu
+from parity_util import TOL_ORBIT, TOL_PHI, TOL_SIGMA, TOL_SUM, make_pair, max_rel, sync_state
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    pytest.param(cmcgpu.PLUMMER, 6000, 0, id="plummer-eq"),
+    pytest.param(cmcgpu.KING, 6000, 1, id="king6-kroupa"),
+    pytest.param(cmcgpu.PLUMMER, 4001, 1, id="plummer-kroupa-odd"),
+]
+
+
+def _init(model, N, imf):
+    ic, o, g = make_pair(model, N, seed=N + imf, imf=imf)
+    o.initialize()
+    g.initialize()
+    return ic, o, g
+
+
+@pytest.mark.parametrize("model,N,imf", CASES)
+def test_potential(gpulib, orc, model, N, imf):
+    ic, o, g = _init(model, N, imf)
+    assert max_rel(g.get("star_phi"), o.get("star_phi")) <= TOL_PHI
+    for s in ("Mtotal", "Rtidal"):
+        assert max_rel(g.scalar(s), o.scalar(s)) <= TOL_PHI
+    assert max_rel(g.get("E"), o.get("E")) <= TOL_PHI
+    assert max_rel(g.get("J"), o.get("J")) <= TOL_PHI
+    for s in ("KE", "PE", "Etot"):
+        assert max_rel(g.scalar(s), o.scalar(s)) <= TOL_SUM
+    for r in (0.0, 1e-3, 0.5, 3.0, 1e3):
+        assert max_rel(g.potential(r), o.potential(r)) <= TOL_PHI
+
+
+@pytest.mark.parametrize("model,N,imf", CASES)
+def test_timestep_and_dynamics(gpulib, orc, model, N, imf):
+    ic, o, g = _init(model, N, imf)
+    sync_state(o, g, star=[("E", "E"), ("J", "J")])
+    o.begin_step()
+    g.begin_step()
+    o.calc_timestep()
+    g.calc_timestep()
+    assert g.scalar("Dt") == o.scalar("Dt")  # bit-exact: same sums in the same order
+    dt = o.scalar("Dt")
+    o.dynamics_apply(dt)
+    g.dynamics_apply(dt)
+    g.check_device("dynamics_apply")
+    assert np.array_equal(g.get("Y"), o.get("Y"))  # pairing and draws
+    # velocity components against the star's speed: libm's sin/cos in the
+    # deflection differ from CUDA's by an ulp, which a component near zero
+    # would otherwise turn into a large relative error
+    vro, vto = o.get("vr"), o.get("vt")
+    speed = np.sqrt(vro * vro + vto * vto)
+    assert np.max(np.abs(g.get("vr_rel") - vro) / speed) <= TOL_PHI
+    assert np.max(np.abs(g.get("vt_rel") - vto) / speed) <= TOL_PHI
+    assert max_rel(g.get("E"), o.get("E")) <= TOL_PHI
+    assert max_rel(g.get("J"), o.get("J")) <= TOL_PHI
+    n = o.nstars()
+    assert max_rel(g.get("sigma")[1:n + 1], o.get("sigma")[1:n + 1]) <= TOL_SIGMA
+    assert np.array_equal(g.get("sigma_r")[1:n + 1], o.get("sigma_r")[1:n + 1])
+    assert g.scalar("Nrel") == o.scalar("Nrel")
+    for i in range(4):
+        assert g.scalar(f"Nrelbeta{i}") == o.scalar(f"Nrelbeta{i}")
+
+
+def _to_orbits(model, N, imf):
+    ic, o, g = _init(model, N, imf)
+    sync_state(o, g, star=[("E", "E"), ("J", "J")])
+    o.begin_step()
+    g.begin_step()
+    o.calc_timestep()
+    dt = o.scalar("Dt")
+    o.dynamics_apply(dt)
+    o.energy_conservation1()
+    # GPU starts the orbit phase from the oracle's post-relaxation state
+    sync_state(o, g, star=[("vr", "vr_rel"), ("vt", "vt_rel"), ("E", "E"), ("J", "J")],
+               scalars=("Rtidal", "Mtotal"))
+    o.new_orbits_calculate()
+    o.energy_conservation2()
+    g.new_orbits_calculate()
+    g.check_device("new_orbits_calculate")
+    return ic, o, g
+
+
+@pytest.mark.parametrize("model,N,imf", CASES)
+def test_new_orbits(gpulib, orc, model, N, imf):
+    ic, o, g = _to_orbits(model, N, imf)
+    rn_o, rn_g = o.get("rnew"), g.get("rnew")
+    esc_o, esc_g = rn_o == 1e10, rn_g == 1e10
+    assert np.array_equal(esc_o, esc_g)
+    keep = ~esc_o
+    assert max_rel(rn_g[keep], rn_o[keep]) <= TOL_ORBIT
+    assert max_rel(g.get("vrnew")[keep], o.get("vrnew")[keep]) <= TOL_ORBIT
+    assert max_rel(g.get("vtnew")[keep], o.get("vtnew")[keep]) <= TOL_ORBIT
+    # peri/apocentre and the accepted X where an orbit was sampled this step
+    sampled = keep & (o.get("r_apo") > 0)
+    assert max_rel(g.get("r_peri")[sampled], o.get("r_peri")[sampled]) <= TOL_ORBIT
+    assert max_rel(g.get("r_apo")[sampled], o.get("r_apo")[sampled]) <= TOL_ORBIT
+    assert np.array_equal(g.get("X")[sampled], o.get("X")[sampled])
+    # energy_conservation1/2 folded into ec_pre
+    vro, vto = o.get("vrold"), o.get("vtold")
+    ec = (vto * vto + vro * vro) + 1.0 * (o.get("Uoldrold") - o.get("Uoldrnew"))
+    assert max_rel(g.get("ec_pre")[keep], ec[keep]) <= TOL_ORBIT
+    for s in ("TidalMassLoss", "Eescaped", "Jescaped"):
+        assert max_rel(g.scalar(s), o.scalar(s)) <= 1e-10
+    assert max_rel(g.scalar("max_r"), o.scalar("max_r")) <= TOL_ORBIT
+
+
+@pytest.mark.parametrize("model,N,imf", CASES)
+def test_tidal_sort_potential_ec3_energy(gpulib, orc, model, N, imf):
+    ic, o, g = _to_orbits(model, N, imf)
+    # identical inputs for the tail of the step: the oracle's orbit outputs
+    sync_state(o, g, star=[("rnew", "rnew"), ("vrnew", "vrnew"), ("vtnew", "vtnew"), ("E", "E"), ("J", "J"),
+                           ("r_apo", "r_apo")],
+               scalars=("TidalMassLoss", "OldTidalMassLoss", "Mtotal"))
+    vro, vto = o.get("vrold"), o.get("vtold")
+    g.set("ec_pre", (vto * vto + vro * vro) + 1.0 * (o.get("Uoldrold") - o.get("Uoldrnew")))
+    o.tidally_strip_stars()
+    g.tidally_strip_stars()
+    g.check_device("tidally_strip_stars")
+    assert np.array_equal(g.get("rnew") == 1e10, o.get("rnew") == 1e10)
+    assert max_rel(g.scalar("Rtidal"), o.scalar("Rtidal")) <= TOL_PHI
+    # sort: bit-exact permutation and payload
+    o.compute_intermediate_energy()
+    o.qsorts_new()
+    g.qsorts_new()
+    g.check_device("qsorts_new")
+    assert g.nstars() == o.nstars()
+    assert np.array_equal(g.ids(), o.ids())
+    for gn, on in (("r", "r"), ("m", "m"), ("vr", "vr"), ("vt", "vt"), ("rOld", "rOld")):
+        assert np.array_equal(g.get(gn), o.get(on)), gn
+    # potential of the new order
+    o.calc_potential()
+    g.calc_potential()
+    assert max_rel(g.get("star_phi"), o.get("star_phi")) <= TOL_PHI
+    # set_velocities3 from the same potential
+    sync_state(o, g, fields=("star_phi",))
+    o.energy_conservation3()
+    g.energy_conservation3()
+    g.check_device("energy_conservation3")
+    assert max_rel(g.get("vr"), o.get("vr")) <= TOL_PHI
+    assert max_rel(g.get("vt"), o.get("vt")) <= TOL_PHI
+    o.compute_energy()
+    sync_state(o, g, scalars=("Eescaped", "Jescaped", "Etidal"))
+    g.set_scalar("Eescaped_old", 0.0)
+    g.set_scalar("Jescaped_old", 0.0)
+    g.set_scalar("Etidal_old", 0.0)
+    g.compute_energy()
+    assert max_rel(g.get("E"), o.get("E")) <= TOL_PHI
+    assert max_rel(g.get("J"), o.get("J")) <= TOL_PHI
+    assert max_rel(g.scalar("Etot"), o.scalar("Etot")) <= TOL_SUM
+
+
+@pytest.mark.parametrize("model,N,imf", CASES[:2])
+def test_free_running_steps(gpulib, orc, model, N, imf):
+    """Whole steps with no state injection: the trajectories stay together and
+    the per-step energy change matches the oracle's."""
+    ic, o, g = _init(model, N, imf)
+    e0o, e0g = o.scalar("Etot"), g.scalar("Etot")
+    for step in range(4):
+        o.step()
+        g.step()
+        g.check_device(f"step {step}")
+        assert g.nstars() == o.nstars()
+        assert np.array_equal(g.ids(), o.ids())
+        assert max_rel(g.get("r"), o.get("r")) <= TOL_ORBIT
+        de_o = o.scalar("Etot") - e0o
+        de_g = g.scalar("Etot") - e0g
+        assert abs(de_g - de_o) <= 1e-9 * abs(e0o) + 1e-3 * abs(de_o)

@@ -302,7 +302,16 @@ def main():
     ap.add_argument("--N", type=int, default=1_000_000)
     ap.add_argument("--cpu-sample", type=int, default=100_000, help="stars per CPU-baseline process")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--probe-rates", action="store_true",
+                    help="build and run the FP64/FP32/INT64 pipe-rate probe, then exit")
     a = ap.parse_args()
+    if a.probe_rates:
+        src = os.path.join(ROOT, "cmc-cosmic_gb300", "csrc", "probe_rates.cu")
+        exe = os.path.join(ROOT, "cmc-cosmic_gb300", "_build", "probe_rates")
+        os.makedirs(os.path.dirname(exe), exist_ok=True)
+        subprocess.check_call(["nvcc", "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-o", exe, src])
+        subprocess.check_call([exe])
+        return
     if a.warmup < 3:
         a.warmup = 3
     rank, ws, local, dist = dist_setup()

@@ -30,6 +30,7 @@ CUDA_SOURCES = [
     "cmcg_sort.cu",
     "cmcg_potential.cu",
     "cmcg_energy.cu",
+    "cmcg_noalloc.cu",
 ]
 C_SOURCES = ["cmcg_ic.c"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"

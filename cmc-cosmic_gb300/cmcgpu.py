@@ -112,6 +112,7 @@ def lib() -> C.CDLL:
         L.cmcg_derive_seed.restype = C.c_uint64
         L.cmcg_draw.argtypes = [C.c_uint64, l, i, C.c_int64, C.c_uint32, i]
         L.cmcg_draw.restype = d
+        L.cmcg_sort_radii_noalloc.argtypes = [vp, l, vp, C.POINTER(l), vp]
         L.cmcg_put_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.cmcg_get_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.cmcg_get_stars.restype = l

@@ -1,0 +1,156 @@
+// cmcg_noalloc.cu -- radius sort that allocates nothing.
+//
+// Some callers cannot allocate device memory once they are running: a host
+// code that embeds this library in a process whose GPU memory is owned by
+// another runtime (a framework allocator that reserved the device up front),
+// or a long run on a shared GPU that must not risk a failed allocation in the
+// middle of a simulation.  cmcg_sort_radii_noalloc gives them the stable
+// radius sort of qsorts_new without any allocation: its working memory is a
+// file-scope __device__ array of fixed size, so the caller passes only the
+// input radii and the output permutation.
+//
+// The array is held by every GPU that loads the library until the process
+// exits (about 34 MB for the 2^20-star maximum).  Its device address is looked
+// up once per device, on the first call made with that device current; make
+// that first call before any stream capture.  All calls share the one array
+// and it keeps the previous call's contents: the parts that must start from
+// zero are cleared on every call, and calls that overlap on the GPU (on
+// different streams, or from different host threads) race on it.
+#include <cstdio>
+#include <mutex>
+
+#include "cmcg_kernels.cuh"
+#include "cmcgpu.h"
+
+namespace cmcg {
+
+constexpr long long NA_MAX = CMCG_NOALLOC_MAX_STARS;
+constexpr long long NA_TILES = (NA_MAX + SORT_T - 1) / SORT_T;
+
+// byte layout of the scratch array (every part 256-byte aligned)
+constexpr size_t na_align(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t NA_R = 0;                                                          // radii, 1-based
+constexpr size_t NA_K0 = na_align(NA_R + sizeof(double) * (NA_MAX + 2));
+constexpr size_t NA_K1 = na_align(NA_K0 + sizeof(unsigned long long) * NA_MAX);
+constexpr size_t NA_V0 = na_align(NA_K1 + sizeof(unsigned long long) * NA_MAX);
+constexpr size_t NA_V1 = na_align(NA_V0 + sizeof(unsigned int) * NA_MAX);
+constexpr size_t NA_HIST = na_align(NA_V1 + sizeof(unsigned int) * NA_MAX);
+constexpr size_t NA_DTOT = na_align(NA_HIST + sizeof(unsigned int) * RADIX * NA_TILES);
+constexpr size_t NA_MISC = na_align(NA_DTOT + sizeof(unsigned int) * RADIX);        // hist_off, npass, kmin, kmax
+constexpr size_t NA_PART = na_align(NA_MISC + 64);
+constexpr size_t NA_TICK = na_align(NA_PART + sizeof(double) * 3 * NA_TILES);
+constexpr size_t NA_SC = na_align(NA_TICK + sizeof(unsigned int));
+constexpr size_t NA_CL = na_align(NA_SC + sizeof(Scalars));
+constexpr size_t NA_TILE = na_align(NA_CL + sizeof(Cluster));
+constexpr size_t NA_FC = na_align(NA_TILE + sizeof(int2) * NA_TILES);             // first, count
+constexpr size_t NA_BYTES = na_align(NA_FC + 2 * sizeof(int));
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+// Describe one cluster of n keys to the shared sort kernels.
+__global__ void k_na_setup(unsigned char *base, long long n, int ntiles)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int2 *tiles = (int2 *)(base + NA_TILE);
+    if (i < ntiles) tiles[i] = make_int2(0, i);
+    if (i == 0) {
+        Scalars *sc = (Scalars *)(base + NA_SC);
+        Cluster *cl = (Cluster *)(base + NA_CL);
+        int *fc = (int *)(base + NA_FC);
+        long long *hist_off = (long long *)(base + NA_MISC);
+        sc->N_MAX = n;
+        sc->N_MAX_NEW = n;
+        sc->err = 0;
+        sc->err_index = 0;
+        cl->off = 0;
+        cl->cap = NA_MAX;
+        cl->sc = sc;
+        fc[0] = 0;
+        fc[1] = ntiles;
+        hist_off[0] = 0;
+        *(unsigned int *)(base + NA_TICK) = 0u;
+    }
+}
+
+// Output: perm[i] = 0-based input position of the i-th smallest radius.
+__global__ void k_na_perm(unsigned char *base, long long n, unsigned int *perm)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int np = *(const int *)(base + NA_MISC + 8);
+    const unsigned int *v = (np & 1) ? (const unsigned int *)(base + NA_V1) : (const unsigned int *)(base + NA_V0);
+    perm[i] = (np == 0) ? (unsigned int)i : v[i];
+}
+
+}  // namespace cmcg
+
+using namespace cmcg;
+
+static std::mutex g_na_mutex;
+static unsigned char *g_na_addr[64];  // device address of the scratch array, per device ordinal
+
+extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_perm, long *n_bound, void *stream)
+{
+    if (!d_r || !d_perm || n < 1) return CMCG_ERR_ARG;
+    if (n > NA_MAX) {
+        fprintf(stderr, "cmcg_sort_radii_noalloc: %ld stars exceed the fixed maximum of %lld\n", n, NA_MAX);
+        return CMCG_ERR_CAPACITY;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CMCG_ERR_CUDA;
+    unsigned char *base;
+    {
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (!g_na_addr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                fprintf(stderr, "cmcg_sort_radii_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+                return CMCG_ERR_CUDA;
+            }
+            g_na_addr[dev] = (unsigned char *)p;
+        }
+        base = g_na_addr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int ntiles = (int)((n + SORT_T - 1) / SORT_T);
+    // radii into slots 1..n (the sort kernels read the reference's 1-based layout)
+    if (cudaMemcpyAsync(base + NA_R + sizeof(double), d_r, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice,
+                        s) != cudaSuccess)
+        return CMCG_ERR_CUDA;
+    k_na_setup<<<(ntiles + 255) / 256, 256, 0, s>>>(base, n, ntiles);
+    Fields f{};
+    f.rnew = (double *)(base + NA_R);
+    SortBufs sb{};
+    sb.keys[0] = (unsigned long long *)(base + NA_K0);
+    sb.keys[1] = (unsigned long long *)(base + NA_K1);
+    sb.vals[0] = (unsigned int *)(base + NA_V0);
+    sb.vals[1] = (unsigned int *)(base + NA_V1);
+    sb.hist = (unsigned int *)(base + NA_HIST);
+    sb.digit_total = (unsigned int *)(base + NA_DTOT);
+    sb.hist_off = (long long *)(base + NA_MISC);
+    sb.npass = (int *)(base + NA_MISC + 8);
+    sb.kmin = (unsigned long long *)(base + NA_MISC + 16);
+    sb.kmax = (unsigned long long *)(base + NA_MISC + 24);
+    const Cluster *cls = (const Cluster *)(base + NA_CL);
+    Tiles tm{(const int2 *)(base + NA_TILE), (const int *)(base + NA_FC), (const int *)(base + NA_FC) + 1, ntiles};
+    double *partials = (double *)(base + NA_PART);
+    unsigned int *tickets = (unsigned int *)(base + NA_TICK);
+    k_sort_prep<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, partials, tickets);
+    for (int p = 0; p < SORT_MAX_PASSES; ++p) {
+        k_sort_hist<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, p);
+        k_sort_scan<<<RADIX, 256, 0, s>>>(tm, sb, p, 1);
+        k_sort_scatter<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, p);
+    }
+    k_na_perm<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(base, n, d_perm);
+    if (cudaGetLastError() != cudaSuccess) return CMCG_ERR_CUDA;
+    if (n_bound) {
+        long long nb = 0;
+        const Scalars *sc = (const Scalars *)(base + NA_SC);
+        if (cudaMemcpyAsync(&nb, &sc->n_bound, sizeof(nb), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return CMCG_ERR_CUDA;
+        *n_bound = (long)nb;
+    }
+    return CMCG_OK;
+}

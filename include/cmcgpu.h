@@ -172,6 +172,27 @@ int cmcg_kernel_time(cmcg_ctx *ctx, const char *family, double *ms_total, long *
 /* Counter-based uniform draw the kernels use (site, star id, n, word). */
 double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, int word);
 
+/* --------------------------------------------- allocation-free variant ---
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory once running -- a host code embedding this library in a process
+ * whose GPU memory another runtime owns, or a long run on a shared GPU that
+ * must not risk a failed allocation mid-simulation -- this is the stable
+ * radius sort of cmcg_qsorts_new on caller-provided device arrays, with its
+ * working memory in a fixed file-scope device array instead of the heap.
+ *   d_r      device pointer, n radii (escapers at SF_INFINITY = 1e10 sort last)
+ *   d_perm   device pointer, n outputs: 0-based input position of the i-th
+ *            smallest radius (ties keep input order)
+ *   n_bound  optional host pointer: count of radii below SF_INFINITY (the call
+ *            then waits for the sort to finish)
+ *   stream   a cudaStream_t, or NULL for the default stream
+ * n may not exceed CMCG_NOALLOC_MAX_STARS (CMCG_ERR_CAPACITY otherwise).  The
+ * first call on each device looks up the array's device address and must come
+ * before any stream capture; every GPU that loads the library holds the
+ * array (about 34 MB) until the process exits.  All calls share it, so calls
+ * that overlap on the GPU race. */
+#define CMCG_NOALLOC_MAX_STARS (1L << 20)
+int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_perm, long *n_bound, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

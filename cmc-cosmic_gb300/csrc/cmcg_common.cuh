@@ -76,4 +76,35 @@ __device__ __forceinline__ bool arrive_last(unsigned int *ticket, int count)
     return false;
 }
 
+// Whole-block form: every thread calls it after thread 0 has written the
+// block's partials; returns the same answer in all threads of the block.
+__device__ __forceinline__ bool block_arrive_last(unsigned int *ticket, int count, int *s_flag)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) *s_flag = arrive_last(ticket, count) ? 1 : 0;
+    __syncthreads();
+    return *s_flag != 0;
+}
+
+// In the last block: sum of column `col` of a cluster's [count][width]
+// partials, all threads striding over tiles in a fixed order, then a fixed
+// tree (deterministic).  Loads bypass L1: the partials come from other SMs.
+template <int NT>
+__device__ __forceinline__ double reduce_partials_sum(const double *partials, int b0, int count, int width, int col,
+                                                      double *red)
+{
+    double v = 0.0;
+    for (int b = threadIdx.x; b < count; b += NT) v += __ldcg(partials + (size_t)(b0 + b) * width + col);
+    return block_sum<NT>(v, red);
+}
+
+template <int NT>
+__device__ __forceinline__ double reduce_partials_max(const double *partials, int b0, int count, int width, int col,
+                                                      double *red)
+{
+    double v = -INFINITY;
+    for (int b = threadIdx.x; b < count; b += NT) v = fmax(v, __ldcg(partials + (size_t)(b0 + b) * width + col));
+    return block_max<NT>(v, red);
+}
+
 }  // namespace cmcg

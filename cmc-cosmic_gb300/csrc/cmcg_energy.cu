@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
 {
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long i = 1 + (long long)ct.y * EC3_T + threadIdx.x;
     const long long off = C.off, g = off + i;
@@ -77,34 +78,53 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     }
 }
 
-// One thread per cluster replays the sequential excess-energy pass from each
-// listed star in radial order (insertion-sorted list; the full sequential
-// pass if the list overflowed).
-__global__ void k_ec3_fix(const Cluster *__restrict__ cls, Fields f, Ec3Bufs eb, int nclusters)
+// One block per cluster: the listed stars are put in radial order with a
+// shared-memory bitonic sort, then one thread replays the sequential
+// excess-energy pass from each of them; beyond the list's capacity the whole
+// sequential pass is replayed.
+__global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__restrict__ cls, Fields f, Ec3Bufs eb,
+                                                             int nclusters)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ long long L[EXCESS_CAP];
+    const int c = blockIdx.x;
     if (c >= nclusters) return;
     const Cluster &C = cls[c];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long off = C.off, N = sc->N_MAX_NEW;
-    unsigned int n = eb.nlist[c];
-    eb.nlist[c] = 0u;
-    sc->n_excess = n;
+    const unsigned int n = eb.nlist[c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        eb.nlist[c] = 0u;
+        sc->n_excess = n;
+    }
     if (n == 0) return;
-    const double E_dump_factor = 0.8;
-    long long *L = eb.list + (size_t)c * EXCESS_CAP;
     const bool overflow = n > EXCESS_CAP;
     if (!overflow) {
-        for (unsigned int a = 1; a < n; ++a) {  // insertion sort (the list is short)
-            const long long v = L[a];
-            int b = (int)a - 1;
-            while (b >= 0 && L[b] > v) {
-                L[b + 1] = L[b];
-                --b;
+        unsigned int P = 1;
+        while (P < n) P <<= 1;
+        const long long *G = eb.list + (size_t)c * EXCESS_CAP;
+        for (unsigned int i = threadIdx.x; i < P; i += blockDim.x) L[i] = (i < n) ? G[i] : LLONG_MAX;
+        __syncthreads();
+        for (unsigned int k = 2; k <= P; k <<= 1) {
+            for (unsigned int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (unsigned int i = threadIdx.x; i < P; i += blockDim.x) {
+                    const unsigned int l = i ^ jj;
+                    if (l > i) {
+                        const bool up = (i & k) == 0;
+                        const long long a = L[i], b = L[l];
+                        if ((a > b) == up) {
+                            L[i] = b;
+                            L[l] = a;
+                        }
+                    }
+                }
+                __syncthreads();
             }
-            L[b + 1] = v;
         }
     }
+    if (threadIdx.x != 0) return;
+    const double E_dump_factor = 0.8;
     double Eexcess = 0.0;
     unsigned int li = 0;
     long long i = overflow ? 1 : L[0];
@@ -147,6 +167,7 @@ __global__ void __launch_bounds__(EN_T) k_energy(const Cluster *__restrict__ cls
     __shared__ double red[EN_T / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX, off = C.off;
     const long long i = 1 + (long long)ct.y * EN_T + threadIdx.x;
@@ -163,17 +184,17 @@ __global__ void __launch_bounds__(EN_T) k_energy(const Cluster *__restrict__ cls
     }
     const double tK = block_sum<EN_T>(K, red);
     const double tP = block_sum<EN_T>(P, red);
+    __shared__ int s_last;
     if (threadIdx.x == 0) {
         double *slot = partials + (size_t)blockIdx.x * 2;
         slot[0] = tK;
         slot[1] = tP;
-        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
-            double aK = 0.0, aP = 0.0;
-            const int b0 = tm.first[ct.x];
-            for (int b = 0; b < tm.count[ct.x]; ++b) {
-                aK += partials[(size_t)(b0 + b) * 2];
-                aP += partials[(size_t)(b0 + b) * 2 + 1];
-            }
+    }
+    if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
+        const double sK = reduce_partials_sum<EN_T>(partials, tm.first[ct.x], tm.count[ct.x], 2, 0, red);
+        const double sP = reduce_partials_sum<EN_T>(partials, tm.first[ct.x], tm.count[ct.x], 2, 1, red);
+        if (threadIdx.x == 0) {
+            double aK = sK, aP = sP;
             // compute_energy_new, cmc_utils.c:2020-2025
             sc->Eescaped += sc->Eescaped_old;
             sc->Jescaped += sc->Jescaped_old;

@@ -60,7 +60,7 @@ struct cmcg_ctx {
     bool use_graph = false, graph_ready = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    long launches = 0, launches_last = 0;
+    long launches = 0, launches_last = 0, graph_launches = 0;
     // profiling
     bool profile = false;
     std::vector<ProfRec> prof;
@@ -152,6 +152,7 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     for (double **p : dfields) *p = cv.take<double>(tot);
     f.id = cv.take<long long>(tot);
     f.id2 = cv.take<long long>(tot);
+    f.rphif = cv.take<float2>(tot);
     c->sb.keys[0] = cv.take<unsigned long long>(tot);
     c->sb.keys[1] = cv.take<unsigned long long>(tot);
     c->sb.vals[0] = cv.take<unsigned int>(tot);
@@ -360,6 +361,18 @@ int cmcg_load(cmcg_ctx *c, int k, long N, const double *r, const double *m, cons
     return CMCG_OK;
 }
 
+// Tables derived from star_r and star_phi (1/r and the FP32 copy), rebuilt
+// after the host overwrites either array.
+__global__ void k_refresh_tables(const Cluster *cls, Fields f, int k, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n + 1) return;
+    const long long g = cls[k].off + i;
+    const double r = f.r[g];
+    f.inv_r[g] = __drcp_rn(r);
+    f.rphif[g] = make_float2((float)r, (float)f.phi[g]);
+}
+
 // New star count after a host upload (the sentinel r[N+1] is copied separately).
 __global__ void k_set_count(const Cluster *cls, int k, long long N)
 {
@@ -519,8 +532,9 @@ static int L_sort(cmcg_ctx *c)
         k_sort_scatter<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
     }
     k_sort_gather<<<c->t256.ntiles, GATHER_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->sb);
+    k_sort_commit<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
     fam_end(c);
-    c->launches += 2 + 3 * SORT_MAX_PASSES;
+    c->launches += 3 + 3 * SORT_MAX_PASSES;
     swap_sorted(c);
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
@@ -529,7 +543,7 @@ static int L_ec3(cmcg_ctx *c)
 {
     fam_begin(c, F_EC3);
     k_ec3<<<c->t256.ntiles, EC3_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->eb);
-    k_ec3_fix<<<(c->ncl + 31) / 32, 32, 0, c->stream>>>(c->d_cls, c->f, c->eb, c->ncl);
+    k_ec3_fix<<<c->ncl, EC3_FIX_THREADS, 0, c->stream>>>(c->d_cls, c->f, c->eb, c->ncl);
     fam_end(c);
     c->launches += 2;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
@@ -600,6 +614,7 @@ static int capture_pair(cmcg_ctx *c)
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->profile = prof;
+    c->graph_launches = c->launches - l0;  // kernel nodes in the two-step graph
     c->launches = l0;
     if (rc) return rc;
     if (e != cudaSuccess) return CMCG_ERR_CUDA;
@@ -619,14 +634,9 @@ int cmcg_run(cmcg_ctx *c, int nsteps)
     if (c->use_graph && !c->profile && nsteps >= 2) {
         if (!c->graph_ready) RUN(capture_pair(c));
         // one graph holds two steps: the sort's buffer swap alternates the field pointers
-        long per_pair = 0;
-        {
-            // count the launches of a pair once (same as issuing two steps)
-            per_pair = 2 * (1 + 1 + 1 + 1 + (TIDAL_PASSES + 1) + (2 + 3 * SORT_MAX_PASSES) + 3 + 2 + 1 + 1);
-        }
         while (nsteps - done >= 2) {
             CK(cudaGraphLaunch(c->gexec, c->stream));
-            c->launches += per_pair;
+            c->launches += c->graph_launches;
             done += 2;
         }
     }
@@ -760,6 +770,11 @@ long cmcg_set_field(cmcg_ctx *c, int k, const char *name, const double *in, long
     const long long o = c->off[k] + (g ? 0 : 1);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return -1;
     if (cudaMemcpy(p + o, in, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+    if (g && (p == c->f.r || p == c->f.phi)) {
+        const long long nn = n - 2;  // global arrays span 0..N+1
+        k_refresh_tables<<<(unsigned)((nn + 2 + 255) / 256), 256, 0, c->stream>>>(c->d_cls, c->f, k, nn);
+        if (cudaStreamSynchronize(c->stream) != cudaSuccess) return -1;
+    }
     return n;
 }
 

@@ -71,6 +71,7 @@ struct Fields {
     double *ec_pre;                    // vold^2 + (Uoldrold - Uoldrnew), see set_velocities3
     double *rOld;                      // star[].rOld after the sort
     double *sigma_r, *sigma;           // sigma_array.r, sigma_array.sigma
+    float2 *rphif;                     // (float r_k, float Phi_k): table for certified FP32 sign tests
     long long *id;                     // star[].id
     // second buffers for the sort's gather (swapped on the host)
     double *r2, *m2, *ec_pre2;
@@ -93,6 +94,19 @@ struct Partials {
 __device__ __forceinline__ void set_error(Scalars *sc, int code, long long idx)
 {
     if (atomicCAS(&sc->err, 0, code) == 0) sc->err_index = idx;
+}
+
+// Every kernel checks the star counts it will index with against the
+// cluster's capacity before touching memory (code 22 = CMCG_ERR_BOUNDS).
+__device__ __forceinline__ bool counts_ok(const Cluster &C)
+{
+    const Scalars *sc = C.sc;
+    const long long a = sc->N_MAX, b = sc->N_MAX_NEW;
+    if (a < 0 || a > C.cap || b < 0 || b > C.cap) {
+        set_error(C.sc, 22, a > C.cap || a < 0 ? a : b);
+        return false;
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------- Philox --
@@ -262,6 +276,32 @@ __device__ __forceinline__ double function_q_dd(double r, double pot, double E, 
     u.lo *= 2.0;
     dd res = dd_add(u, {-Jr, 0.0});                 // 2(E - ...) - Jr
     return __dadd_rn(res.hi, res.lo);
+}
+
+// Certified FP32 sign of function_q at a table point (r, Phi given as the
+// round-to-nearest floats of the FP64 table).  Every input conversion,
+// reciprocal, product and difference contributes at most a few units of 2^-24;
+// summed, |Q_f32 - Q| <= 12.2u(|E|+|Phi|+|phis|) + 10.1u (J/r)^2 (u = 2^-24),
+// and the threshold below is twice that.  Beyond it the FP32 sign is the exact
+// sign, hence also the sign of the reference's long double evaluation.
+// Returns +1, -1, or 0 when the caller must evaluate in double-double.
+struct QF32 {
+    float E, J, mjN, pj;  // E, J, m_j/N_STAR, (m_j/r_j)/N_STAR as floats
+    double rj;            // r_j: the self-potential branch is chosen in FP64
+};
+
+__device__ __forceinline__ int fq_sign_f32(const QF32 &s, float2 rp, bool ge)
+{
+    const float ir = __frcp_rn(rp.x);
+    const float phis = ge ? s.mjN * ir : s.pj;
+    const float A = (s.E - rp.y) - phis;
+    const float q = s.J * ir;
+    const float B = q * q;
+    const float Q = 2.0f * A - B;
+    const float bound = 1.5e-6f * (2.0f * (fabsf(s.E) + fabsf(rp.y) + fabsf(phis)) + B);
+    if (Q > bound) return 1;
+    if (Q < -bound) return -1;
+    return 0;
 }
 
 }  // namespace cmcg

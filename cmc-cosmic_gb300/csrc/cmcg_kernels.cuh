@@ -13,7 +13,8 @@ constexpr int SORT_THREADS = 256, SORT_ITEMS = 8, SORT_T = SORT_THREADS * SORT_I
 constexpr int GATHER_T = 256;
 constexpr int POT_THREADS = 256, POT_ITEMS = 4, POT_T = POT_THREADS * POT_ITEMS;
 constexpr int EC3_T = 256, EN_T = 256;
-constexpr int EXCESS_CAP = 65536;
+constexpr int EXCESS_CAP = 4096;      // listed unphysical predictions per cluster (else full replay)
+constexpr int EC3_FIX_THREADS = 512;
 constexpr int SORT_MAX_PASSES = 8;
 constexpr int TIDAL_PASSES = 32;  // passes after the cluster settles exit at once
 
@@ -54,6 +55,7 @@ __global__ void k_sort_hist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb,
 __global__ void k_sort_scan(Tiles tm, SortBufs sb, int pass, int nclusters);
 __global__ void k_sort_scatter(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, int pass);
 __global__ void k_sort_gather(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
+__global__ void k_sort_commit(const Cluster *cls, int nclusters);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);
 __global__ void k_pot_carry(const Cluster *cls, Tiles tm, PotBufs pb, int nclusters);
 __global__ void k_pot_apply(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);

@@ -24,8 +24,10 @@ constexpr int BISECT_LIMIT = 80;
 
 struct OrbitCtx {
     const double *__restrict__ r, *__restrict__ phi, *__restrict__ inv_r;
-    long long N_MAX;
+    const float2 *__restrict__ rphif;
+    long long N_MAX, j;
     double E, J, rj, mj, invN, cenma_m, madhoc;
+    QF32 s;
 };
 
 static __device__ __forceinline__ double fq(const OrbitCtx &o, long long k)
@@ -33,7 +35,19 @@ static __device__ __forceinline__ double fq(const OrbitCtx &o, long long k)
     return function_q_dd(__ldg(o.r + k), __ldg(o.phi + k), o.E, o.J, o.rj, o.mj, o.invN);
 }
 
-// find_zero_Q, cmc_nr.c:316-383 (bounded; returns -1 if it does not terminate)
+// Sign of function_q at table point k: certified FP32 first, double-double
+// only when the FP32 value lies within its error bound.
+static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
+{
+    const int s = fq_sign_f32(o.s, __ldg(o.rphif + k), k >= o.j);
+    if (s) return s;
+    const double q = fq(o, k);
+    return (q > 0.0) - (q < 0.0);
+}
+
+// find_zero_Q, cmc_nr.c:316-383 (bounded; returns -1 if it does not terminate).
+// The end-point values decide the branch and are taken in double-double; the
+// bisection only needs signs.
 static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long long kmax)
 {
     const double qmin = fq(o, kmin), qmax = fq(o, kmax);
@@ -41,7 +55,7 @@ static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long 
     if (qmin < qmax) {
         do {
             const long long ktry = (kmin + kmax + 1) / 2;
-            if (fq(o, ktry) < 0.0)
+            if (fq_sign(o, ktry) < 0)
                 kmin = ktry;
             else
                 kmax = ktry - 1;
@@ -50,7 +64,7 @@ static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long 
     } else {
         do {
             const long long ktry = (kmin + kmax + 1) / 2;
-            if (fq(o, ktry) > 0.0)
+            if (fq_sign(o, ktry) > 0)
                 kmin = ktry;
             else
                 kmax = ktry - 1;
@@ -196,10 +210,11 @@ static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, double 
     double Qtemp = fq(o, ktemp);
     if (Qtemp <= 0.0) {
         ktemp = -1;
+        int sgn;
         do {
             ktemp++;
-            Qtemp = fq(o, ktemp);
-        } while (Qtemp <= 0.0 && ktemp <= o.N_MAX);
+            sgn = fq_sign(o, ktemp);
+        } while (sgn <= 0 && ktemp <= o.N_MAX);
         if (ktemp >= o.N_MAX) return res;
     }
     const long long kmin = find_zero_Q(o, 0, ktemp);
@@ -268,6 +283,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
     __shared__ double red[ORB_T / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long off = C.off;
     const long long N_MAX = sc->N_MAX, N_NEW = sc->N_MAX_NEW;
@@ -301,7 +317,9 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
             o.r = f.r + off;
             o.phi = f.phi + off;
             o.inv_r = f.inv_r + off;
+            o.rphif = f.rphif + off;
             o.N_MAX = N_MAX;
+            o.j = j;
             o.E = E;
             o.J = J;
             o.rj = rj;
@@ -309,6 +327,11 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
             o.invN = invN;
             o.cenma_m = sc->cenma_m;
             o.madhoc = sc->madhoc;
+            o.s.E = (float)E;
+            o.s.J = (float)J;
+            o.s.mjN = (float)(mj * invN);
+            o.s.pj = (float)((mj / rj) * invN);
+            o.s.rj = rj;
             int err = 0;
             const OrbitRs orb = calc_orbit_new(o, j, C.apsides_precision, C.apsides_max_iter, &err);
             if (err) {
@@ -391,6 +414,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
     const double tM = block_sum<ORB_T>(acc_M, red);
     const double tEt = block_sum<ORB_T>(acc_Et, red);
     const double tmax = block_max<ORB_T>(max_rad, red);
+    __shared__ int s_last;
     if (threadIdx.x == 0) {
         double *slot = partials + (size_t)blockIdx.x * ORB_NPART;
         slot[0] = tE;
@@ -398,17 +422,13 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
         slot[2] = tM;
         slot[3] = tEt;
         slot[4] = tmax;
-        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
-            double a[ORB_NPART] = {0.0, 0.0, 0.0, 0.0, 0.0};
-            const int b0 = tm.first[ct.x];
-            for (int b = 0; b < tm.count[ct.x]; ++b) {
-                const double *s = partials + (size_t)(b0 + b) * ORB_NPART;
-                a[0] += s[0];
-                a[1] += s[1];
-                a[2] += s[2];
-                a[3] += s[3];
-                a[4] = fmax(a[4], s[4]);
-            }
+    }
+    if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
+        double a[ORB_NPART];
+        const int b0 = tm.first[ct.x], nb = tm.count[ct.x];
+        for (int q = 0; q < 4; ++q) a[q] = reduce_partials_sum<ORB_T>(partials, b0, nb, ORB_NPART, q, red);
+        a[4] = reduce_partials_max<ORB_T>(partials, b0, nb, ORB_NPART, 4, red);
+        if (threadIdx.x == 0) {
             // new_orbits_calculate, cmc_utils.c:2197-2210
             sc->OldTidalMassLoss = sc->TidalMassLoss_old;
             sc->Eescaped += a[0];
@@ -430,6 +450,7 @@ __global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict
     __shared__ int s_ok;
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     if (sc->tidal_done) return;
     const long long off = C.off;
@@ -469,17 +490,19 @@ __global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict
     const double tJ = block_sum<TID_THREADS>(aJ, red);
     const double tM = block_sum<TID_THREADS>(aM, red);
     const double tEt = block_sum<TID_THREADS>(aEt, red);
+    __shared__ int s_last;
     if (threadIdx.x == 0) {
         double *slot = partials + (size_t)blockIdx.x * TID_NPART;
         slot[0] = tE;
         slot[1] = tJ;
         slot[2] = tM;
         slot[3] = tEt;
-        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
-            double a[TID_NPART] = {0.0, 0.0, 0.0, 0.0};
-            const int b0 = tm.first[ct.x];
-            for (int b = 0; b < tm.count[ct.x]; ++b)
-                for (int q = 0; q < TID_NPART; ++q) a[q] += partials[(size_t)(b0 + b) * TID_NPART + q];
+    }
+    if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
+        double a[TID_NPART];
+        for (int q = 0; q < TID_NPART; ++q)
+            a[q] = reduce_partials_sum<TID_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], TID_NPART, q, red);
+        if (threadIdx.x == 0) {
             if (!s_ok) set_error(sc, CMCG_ERR_FINDZERO_R, 0);
             if (sc->tidal_iters == 0) sc->Etidal = 0.0;  // cmc_evolution_thr.c:452
             sc->Rtidal = Rtidal;
@@ -508,6 +531,11 @@ __global__ void k_tidal_check(const Cluster *__restrict__ cls, int nclusters)
 __global__ void k_potential_query(const Cluster *__restrict__ cls, Fields f, int c, double x, double *out)
 {
     const Cluster &C = cls[c];
+    if (!counts_ok(C)) {
+        out[0] = 0.0;
+        out[1] = 1.0;
+        return;
+    }
     int ok = 1;
     out[0] = potential_at(f.r + C.off, f.phi + C.off, f.inv_r + C.off, C.sc->N_MAX, x, &ok);
     out[1] = ok ? 0.0 : 1.0;

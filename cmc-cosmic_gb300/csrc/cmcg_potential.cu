@@ -24,6 +24,15 @@ static __device__ __forceinline__ double r_at(const double *r, long long k, long
     return k == N + 1 ? CMCG_SF_INFINITY : r[k];
 }
 
+// 1/r of the star just outside a tile whose largest index is kstart.  A tile
+// map sized for the capacity has tiles lying wholly below star 1 once N has
+// shrunk (kstart < 1); they hold no stars and must not read r at all.
+static __device__ __forceinline__ double r_next_inv(const double *r, long long kstart, long long N)
+{
+    if (kstart < 1 || kstart > N) return 0.0;
+    return __drcp_rn(r_at(r, kstart + 1, N));
+}
+
 // inclusive block scan (blocked arrangement: thread t holds items t*4..t*4+3)
 template <int NT>
 static __device__ __forceinline__ double block_excl_prefix(double tsum, double *s_w)
@@ -51,6 +60,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
     __shared__ double red[POT_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX, off = C.off;
     const double NSTAR = (double)sc->N_STAR;
@@ -75,7 +85,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
     double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
     if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
     __syncthreads();
-    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : __drcp_rn(r_at(r, kstart + 1, N));
+    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : r_next_inv(r, kstart, N);
     double d[POT_ITEMS];
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) {
@@ -118,6 +128,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__rest
     const int c = blockIdx.x;
     if (c >= nclusters) return;
     const Cluster &C = cls[c];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const int ntiles = tm.count[c], b0 = tm.first[c];
     const long long N = sc->N_MAX;
@@ -179,10 +190,12 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__rest
     __shared__ double s_lastinv[POT_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX, off = C.off;
     const long long kstart = N - (long long)ct.y * POT_T;
     double *r = f.r + off, *phi = f.phi + off, *inv_r = f.inv_r + off;
+    float2 *rphif = f.rphif + off;
     const double Mtot = sc->Mtotal;
     const double Qin = pb.carry[(size_t)blockIdx.x * 2], Din = pb.carry[(size_t)blockIdx.x * 2 + 1];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -196,7 +209,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__rest
     double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
     if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
     __syncthreads();
-    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : __drcp_rn(r_at(r, kstart + 1, N));
+    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : r_next_inv(r, kstart, N);
     double tq = 0.0;
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) tq += q[i];
@@ -220,7 +233,12 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__rest
         if (k >= 1) {
             const double ph = -acc;
             phi[k] = ph;
-            if (k == 1) phi[0] = ph + sc->cenma_m * sc->madhoc / r[1];
+            rphif[k] = make_float2((float)r[k], (float)ph);
+            if (k == 1) {
+                const double p0 = ph + sc->cenma_m * sc->madhoc / r[1];
+                phi[0] = p0;
+                rphif[0] = make_float2((float)r[0], (float)p0);
+            }
         }
     }
     if (ct.y == 0 && t == 0) {
@@ -228,6 +246,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__rest
         phi[N + 1] = 0.0;
         inv_r[N + 1] = __drcp_rn(CMCG_SF_INFINITY);
         inv_r[0] = __drcp_rn(r[0]);
+        rphif[N + 1] = make_float2((float)CMCG_SF_INFINITY, 0.0f);
     }
 }
 

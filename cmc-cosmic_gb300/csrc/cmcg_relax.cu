@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(128) k_timestep(const Cluster *__restrict__ cl
     __shared__ double red[4];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX, p = C.p;
     const double madhoc = sc->madhoc;
@@ -77,14 +78,14 @@ __global__ void __launch_bounds__(128) k_timestep(const Cluster *__restrict__ cl
         }
     }
     // exact min over blocks (min is order independent)
+    __shared__ int s_last;
     const double bmin = -block_max<128>(-dtmin, red);
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x] = bmin;
-        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
-            double Dt = INFINITY;
-            const int b0 = tm.first[ct.x];
-            for (int b = 0; b < tm.count[ct.x]; ++b) Dt = fmin(Dt, partials[b0 + b]);
-            if (!C.RELAXATION) Dt = INFINITY;
+    // min over blocks as the negated max of negated block minima (order independent)
+    if (threadIdx.x == 0) partials[blockIdx.x] = -bmin;
+    if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
+        const double Dtmin = -reduce_partials_max<128>(partials, tm.first[ct.x], tm.count[ct.x], 1, 0, red);
+        if (threadIdx.x == 0) {
+            double Dt = C.RELAXATION ? Dtmin : INFINITY;
             // GetTimeStep, cmc_evolution_thr.c:420: all other time scales are infinite
             if (isinf(Dt)) Dt = 0.001;
             // calc_timestep, cmc_utils.c:2138-2144
@@ -112,6 +113,7 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
 
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX, p = C.p;
     const double madhoc = sc->madhoc, NSTAR = (double)sc->N_STAR;
@@ -343,18 +345,19 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
     }
 
     // ---- statistics (cmc_dynamics.c:430-440), deterministic block order
+    __shared__ int s_last;
     double tot[RELAX_NPART];
 #pragma unroll
     for (int i = 0; i < RELAX_NPART; ++i) tot[i] = block_sum<RELAX_THREADS>(part[i], red);
     if (tid == 0) {
         double *slot = partials + (size_t)blockIdx.x * RELAX_NPART;
         for (int i = 0; i < RELAX_NPART; ++i) slot[i] = tot[i];
-        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
-            double acc[RELAX_NPART];
-            for (int i = 0; i < RELAX_NPART; ++i) acc[i] = 0.0;
-            const int b0 = tm.first[ct.x];
-            for (int b = 0; b < tm.count[ct.x]; ++b)
-                for (int i = 0; i < RELAX_NPART; ++i) acc[i] += partials[(size_t)(b0 + b) * RELAX_NPART + i];
+    }
+    if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
+        double acc[RELAX_NPART];
+        for (int i = 0; i < RELAX_NPART; ++i)
+            acc[i] = reduce_partials_sum<RELAX_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], RELAX_NPART, i, red);
+        if (tid == 0) {
             sc->Nrel = (long long)acc[0];
             for (int i = 0; i < 4; ++i) {
                 sc->Nrelbeta[i] = (long long)acc[1 + i];

@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
     __shared__ long long s_cnt[SORT_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX_NEW;
     const unsigned long long inf_bits = (unsigned long long)__double_as_longlong(CMCG_SF_INFINITY);
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_hist(const Cluster *__res
     __shared__ unsigned int h[SORT_THREADS / 32][RADIX];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     if (pass >= sb.npass[ct.x]) return;
     const long long N = C.sc->N_MAX_NEW;
     const int w = threadIdx.x >> 5;
@@ -177,6 +179,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const Cluster *__
     __shared__ unsigned int sv[SORT_T];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     if (pass >= sb.npass[ct.x]) return;
     const long long N = C.sc->N_MAX_NEW;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -294,13 +297,22 @@ __global__ void __launch_bounds__(256) k_sort_gather(const Cluster *__restrict__
 {
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long nb = sc->n_bound;
     const int np = sb.npass[ct.x];
     const long long i = (long long)ct.y * 256 + threadIdx.x;  // 0-based output position
     const long long off = C.off;
+    if (nb < 0 || nb > sc->N_MAX_NEW) {
+        if (i == 0) set_error(sc, CMCG_ERR_BOUNDS, nb);
+        return;
+    }
     if (i < nb) {
         const long long src = 1 + (np == 0 ? i : (long long)((np & 1) ? sb.vals[1] : sb.vals[0])[off + i]);
+        if (src < 1 || src > sc->N_MAX_NEW) {
+            set_error(sc, CMCG_ERR_BOUNDS, src);
+            return;
+        }
         const long long gs = off + src, gd = off + 1 + i;
         f.r2[gd] = f.rnew[gs];
         f.m2[gd] = f.m[gs];
@@ -311,9 +323,6 @@ __global__ void __launch_bounds__(256) k_sort_gather(const Cluster *__restrict__
         f.ec_pre2[gd] = f.ec_pre[gs];
     }
     if (i == 0) {
-        // new N_MAX (cmc_sort.c:343-354 and cmc_utils.c:2246)
-        sc->N_MAX = nb;
-        sc->N_MAX_NEW = nb;
         // the second buffers become the live arrays: carry the sentinels over
         // (star_r[0] = ZERO, star_m[0] = 0; star_r[N+1] is reset by the potential)
         f.r2[off] = CMCG_ZERO;
@@ -323,6 +332,21 @@ __global__ void __launch_bounds__(256) k_sort_gather(const Cluster *__restrict__
         f.r2[off + nb + 1] = CMCG_SF_INFINITY;
         f.m2[off + nb + 1] = 0.0;
     }
+}
+
+// New N_MAX after the gather (cmc_sort.c:343-354, cmc_utils.c:2246); a kernel of
+// its own so no gather block ever sees the count change under it.
+__global__ void k_sort_commit(const Cluster *__restrict__ cls, int nclusters)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nclusters) return;
+    Scalars *sc = cls[c].sc;
+    if (sc->n_bound < 0 || sc->n_bound > sc->N_MAX_NEW) {
+        set_error(sc, CMCG_ERR_BOUNDS, sc->n_bound);
+        return;
+    }
+    sc->N_MAX = sc->n_bound;
+    sc->N_MAX_NEW = sc->n_bound;
 }
 
 }  // namespace cmcg

@@ -59,7 +59,9 @@ enum {
     CMCG_ERR_POT_INTERVAL = 11, /* cmc_nr.c:240   radius outside interval       */
     CMCG_ERR_ENCOUNTER = 12,    /* a strong-encounter draw hit (host physics)   */
     CMCG_ERR_SPIN = 20,         /* a bounded cross-block wait gave up           */
-    CMCG_ERR_TIDAL_ITER = 21    /* tidal stripping did not settle               */
+    CMCG_ERR_TIDAL_ITER = 21,   /* tidal stripping did not settle               */
+    CMCG_ERR_BOUNDS = 22        /* a star count or index outside the cluster's
+                                   capacity was refused (access skipped)        */
 };
 
 /* ------------------------------------------------------- parameters ----- */

@@ -38,6 +38,13 @@ UNIT = "star-updates/s"
 # traffic: reads + writes of the fields the phase consumes and produces)
 ALG_BYTES = {"sort": 116, "potential": 24, "relax": 72, "orbit": 80, "ec3": 72, "energy": 56,
              "timestep": 24, "tidal": 16, "begin": 0, "end": 0}
+# DRAM bytes per star of one launch, dram__bytes_read.sum + dram__bytes_write.sum
+# from one ncu capture (k_orbit: 391.9 MB over 1,913,957 stars, King W0=6 +
+# Kroupa, N=2e6; profiles/orbit_king6_kroupa_2e6.md), scaled by stars
+NCU_TRAFFIC_PER_STAR = {"orbit": 391.9e6 / 1913957}
+# share of active cycles the FP64 pipe was busy in the same capture: the
+# kernel's real bound on GB300 (1/64-rate FP64), reported beside the HBM roofline
+NCU_FP64_PIPE_ACTIVE = {"orbit": 0.861}
 
 
 def measured_peak():
@@ -283,7 +290,9 @@ def run_ours(a, rank, ws, dist):
                 "d2h_bytes_per_step": d2h // a.steps},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": (NCU_TRAFFIC_PER_STAR[top] * n_start if top in NCU_TRAFFIC_PER_STAR else None),
+                     "fp64_pipe_active": NCU_FP64_PIPE_ACTIVE.get(top),
                      "alg_bytes_per_star": ALG_BYTES[top], "ms_per_launch": ms_top / n_top},
         "kernels": per_family,
         "kernel_ms_per_step": step_ms,

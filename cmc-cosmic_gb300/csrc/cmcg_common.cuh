@@ -80,6 +80,7 @@ __device__ __forceinline__ bool arrive_last(unsigned int *ticket, int count)
 // block's partials; returns the same answer in all threads of the block.
 __device__ __forceinline__ bool block_arrive_last(unsigned int *ticket, int count, int *s_flag)
 {
+    __threadfence();  // every thread's writes before the ticket, not only thread 0's
     __syncthreads();
     if (threadIdx.x == 0) *s_flag = arrive_last(ticket, count) ? 1 : 0;
     __syncthreads();

@@ -50,6 +50,8 @@ struct cmcg_ctx {
     unsigned int *tickets = nullptr;
     SortBufs sb{};
     PotBufs pb{};
+    PhiBufs ph{};
+    long long rec_total = 0;
     Ec3Bufs eb{};
     double *d_query = nullptr;
     TileTable t128, t256, t1024, t2048, t5120;
@@ -166,8 +168,18 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->sb.kmin = cv.take<unsigned long long>(c->ncl);
     c->sb.kmax = cv.take<unsigned long long>(c->ncl);
     c->pb.q = cv.take<double>(tot);
-    c->pb.agg = cv.take<double>((size_t)c->t1024.ntiles * 4);
-    c->pb.carry = cv.take<double>((size_t)c->t1024.ntiles * 2);
+    c->pb.agg = cv.take<double>((size_t)c->t1024.ntiles * POT_AGG);
+    c->pb.carry = cv.take<double>((size_t)c->t1024.ntiles * POT_CARRY);
+    c->pb.sapx = cv.take<double>(tot);
+    c->pb.mapx = cv.take<double>(tot);
+    c->pb.papx = cv.take<double>(tot);
+    c->pb.t = cv.take<double>(tot);
+    for (int i = 0; i < 2; ++i) {
+        c->ph.agg[i] = cv.take<ChainAgg>(c->t1024.ntiles);
+        c->ph.carry[i] = cv.take<ChainCarry>(c->t1024.ntiles);
+        c->ph.rec[i] = cv.take<SPRec>((size_t)c->rec_total);
+    }
+    c->ph.ctl = cv.take<PhiCtl>(c->ncl);
     c->eb.a = cv.take<double>(tot);
     c->eb.list = cv.take<long long>((size_t)c->ncl * EXCESS_CAP);
     c->eb.nlist = cv.take<unsigned int>(c->ncl);
@@ -213,7 +225,13 @@ void cmcg_default_params(cmcg_params *p)
     p->n_try = 50000;
     p->seed = 0;
     p->relax_fp32 = 0;
+    p->phi_sequential = 0;
 }
+
+// Sequential points of the potential replay a cluster may record (per chain):
+// a few per binade crossed in practice; beyond this the cluster's potential
+// is computed by the one-thread loop.
+static long long phi_rec_cap(long long cap) { return 4096 + cap / 16; }
 
 int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_params *params)
 {
@@ -243,6 +261,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         tot += stride;
     }
     c->total = tot;
+    for (int k = 0; k < nclusters; ++k) c->rec_total += phi_rec_cap(capacity[k]);
     std::vector<int2> tabs[5];
     build_table(c->t128, c->cap, ORB_T, tabs[0]);
     build_table(c->t256, c->cap, RELAX_T, tabs[1]);
@@ -272,6 +291,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
     CK(cudaMemcpyAsync(c->sb.hist_off, hist_off.data(), nclusters * sizeof(long long), cudaMemcpyHostToDevice,
                        c->stream));
     c->h_cls.resize(nclusters);
+    long long rec_off = 0;
     for (int k = 0; k < nclusters; ++k) {
         Cluster &C = c->h_cls[k];
         const cmcg_params &p = params[k];
@@ -292,6 +312,10 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         C.apsides_convergence = p.apsides_convergence;
         C.seed = p.seed;
         C.relax_fp32 = p.relax_fp32;
+        C.phi_sequential = p.phi_sequential;
+        C.rec_off = rec_off;
+        C.rec_cap = phi_rec_cap(c->cap[k]);
+        rec_off += C.rec_cap;
     }
     CK(cudaMemcpyAsync(c->d_cls, c->h_cls.data(), nclusters * sizeof(Cluster), cudaMemcpyHostToDevice, c->stream));
     TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t5120};
@@ -434,11 +458,19 @@ long cmcg_get_stars(cmcg_ctx *c, int k, long cap, double *r, double *m, double *
 static int L_pot(cmcg_ctx *c)
 {
     fam_begin(c, F_POT);
-    k_pot_agg<<<c->t1024.ntiles, POT_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->f, c->pb);
-    k_pot_carry<<<c->ncl, POT_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->pb, c->ncl);
-    k_pot_apply<<<c->t1024.ntiles, POT_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->f, c->pb);
+    const Tiles tv = c->t1024.view();
+    const int nt = c->t1024.ntiles;
+    k_pot_agg<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb);
+    k_pot_carry<<<c->ncl, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->pb, c->ph, c->ncl);
+    k_pot_apply<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph);
+    k_phi_cls12<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
+    k_phi_rec12<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
+    k_phi_cls3<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
+    k_phi_rec3<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
+    k_phi_final<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph);
+    k_phi_seq<<<c->ncl, 32, 0, c->stream>>>(c->d_cls, c->f, c->ph, c->ncl);
     fam_end(c);
-    c->launches += 3;
+    c->launches += 9;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
@@ -818,7 +850,9 @@ int cmcg_get_scalar(cmcg_ctx *c, int k, const char *name, double *out)
                 {"Nrelbeta3", (double)s.Nrelbeta[3]}, {"n_excess", (double)s.n_excess},
                 {"tidal_iters", (double)s.tidal_iters}, {"err", (double)s.err},
                 {"qaverelbeta0", s.qaverelbeta[0]}, {"maverelbeta0", s.maverelbeta[0]},
-                {"raverelbeta0", s.raverelbeta[0]}};
+                {"raverelbeta0", s.raverelbeta[0]},
+                {"phi_nsp1", (double)s.phi_nsp[0]}, {"phi_nsp2", (double)s.phi_nsp[1]},
+                {"phi_nsp3", (double)s.phi_nsp[2]}, {"phi_fallback", (double)s.phi_fallback}};
     for (auto &t : ints)
         if (!strcmp(name, t.n)) {
             *out = t.v;

@@ -43,6 +43,10 @@ struct Scalars {
     long long n_bound;     // stars kept after the sort (r < SF_INFINITY)
     // set_velocities3 bookkeeping
     long long n_excess;    // stars whose predicted v^2 <= 0
+    // potential bookkeeping: sequential points of the three recurrences, and
+    // whether the last potential fell back to the one-thread loop
+    long long phi_nsp[3];
+    long long phi_fallback;
 };
 
 // Per-cluster constant description (built on the host, read-only on device).
@@ -58,7 +62,8 @@ struct Cluster {
     double apsides_precision, apsides_convergence;
     unsigned long long seed;
     int relax_fp32;
-    int pad1;
+    int phi_sequential;    // 1: potential by the plain sequential loop (one thread)
+    long long rec_off, rec_cap;  // this cluster's slice of the sequential-point records
 };
 
 // Device-resident fields (all concatenated over clusters).

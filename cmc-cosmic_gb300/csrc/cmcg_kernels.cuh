@@ -30,9 +30,53 @@ struct SortBufs {
 
 struct PotBufs {
     double *q;      // m_k / N_STAR per star
-    double *agg;    // per tile: q, Delta, C, sum m
-    double *carry;  // per tile: Q_after, D_after
+    double *agg;    // per tile: q, Delta, C, sum m, disorder flag (POT_AGG doubles)
+    double *carry;  // per tile: Q, D and forward mass entering the tile (POT_CARRY doubles)
+    // approximate running values of the three recurrences of potential_calculate
+    double *sapx;   // forward mass sum after star k
+    double *mapx;   // M_k, the enclosed mass the backward loop uses at star k
+    double *papx;   // Phi_k
+    double *t;      // exact M_k (1/r_k - 1/r_{k+1}) per star
 };
+constexpr int POT_AGG = 5, POT_CARRY = 3;
+
+// ---- exact replay of the sequential potential recurrences (cmcg_phi.cu)
+// A "sequential point" is a position whose rounding cannot be proven to stay
+// on one binade grid; the other positions add an integer number of grid units.
+struct ChainAgg {        // per tile, in the chain's order
+    long long P;         // grid units summed since the tile's last sequential point
+    int cnt;             // positions in that run
+    int nsp;             // sequential points in the tile
+};
+struct ChainCarry {      // per tile: the run entering it and its first record index
+    long long P;
+    int cnt;
+    int spoff;
+};
+struct SPRec {           // one sequential point
+    long long k;         // star index
+    double a;            // the term added at this position
+    long long Pprev;     // grid units of the run ending just before it
+    int keyprev;         // sign and exponent bits of that run's binade
+    int cntprev;         // length of that run (0: the previous position is a sequential point)
+    double sprev, snew;  // exact values before and after (filled by the replay)
+};
+struct PhiCtl {          // per cluster
+    double Sm, Qtot, Dtot, Mapx;   // approximate totals: sum m, sum q, sum d, Mtotal
+    double Mb, G;                  // bound on every |M_k|; scan error factor
+    double marg1, marg2;           // bounds on |approximate - sequential| of chains 1, 2
+    double c0, c1;                 // chain 3 bound: c0 + c1 / r_k
+    int fail;                      // 1: replay impossible or refused, recompute sequentially
+    int pad;
+    long long nsp[3];
+};
+struct PhiBufs {
+    ChainAgg *agg[2];
+    ChainCarry *carry[2];
+    SPRec *rec[2];
+    PhiCtl *ctl;
+};
+constexpr int PHI_WALK_BATCH = 512;
 
 struct Ec3Bufs {
     double *a;           // per star: excess added by an unphysical prediction (or -1)
@@ -57,8 +101,14 @@ __global__ void k_sort_scatter(const Cluster *cls, Tiles tm, Fields f, SortBufs 
 __global__ void k_sort_gather(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
 __global__ void k_sort_commit(const Cluster *cls, int nclusters);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);
-__global__ void k_pot_carry(const Cluster *cls, Tiles tm, PotBufs pb, int nclusters);
-__global__ void k_pot_apply(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);
+__global__ void k_pot_carry(const Cluster *cls, Tiles tm, PotBufs pb, PhiBufs ph, int nclusters);
+__global__ void k_pot_apply(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph);
+__global__ void k_phi_cls12(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);
+__global__ void k_phi_rec12(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);
+__global__ void k_phi_cls3(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);
+__global__ void k_phi_rec3(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);
+__global__ void k_phi_final(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph);
+__global__ void k_phi_seq(const Cluster *cls, Fields f, PhiBufs ph, int nclusters);
 __global__ void k_begin_step(const Cluster *cls, int nclusters);
 __global__ void k_end_step(const Cluster *cls, int nclusters);
 __global__ void k_ec3(const Cluster *cls, Tiles tm, Fields f, Ec3Bufs eb);

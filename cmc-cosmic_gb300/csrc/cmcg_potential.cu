@@ -1,4 +1,6 @@
-// cmcg_potential.cu -- potential_calculate (cmc_utils.c:675-736) as a scan.
+// cmcg_potential.cu -- potential_calculate (cmc_utils.c:675-736), first pass:
+// approximate values of its three running quantities, from a parallel scan.
+// cmcg_phi.cu turns them into the reference's exact FP64 results.
 //
 // The reference walks k = N..1 with
 //     Phi_k = Phi_{k+1} - M_k (1/r_k - 1/r_{k+1}),   M_{k-1} = M_k - m_k/N_STAR,
@@ -11,9 +13,12 @@
 // with the associative combine (outer A, inner B) ->
 //     (q_A + q_B, Delta_A + Delta_B, C_A + C_B + q_A Delta_B),
 // and the D entering a tile is Mtotal * Delta_before - C_before.
-//   k_pot_agg    per tile: q_j, 1/r_j (stored), the triple, and sum m_j
-//   k_pot_carry  per cluster: Mtotal, Rtidal, scan of the triples over tiles
-//   k_pot_apply  per tile: M_k, Phi_k, sentinels (Phi_0, Phi_{N+1}, r_{N+1})
+//   k_pot_agg    per tile: q_j, 1/r_j (stored), the triple, sum m_j, and a
+//                flag for input the exact replay does not take (radii out of
+//                order, non-finite or negative values)
+//   k_pot_carry  per cluster: approximate Mtotal, the bounds the replay
+//                classifies with, scan of the triples over tiles
+//   k_pot_apply  per tile: approximate forward mass sum, M_k and Phi_k
 #include "cmcg_kernels.cuh"
 
 namespace cmcg {
@@ -68,15 +73,20 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
     const double *r = f.r + off, *m = f.m + off;
     double q[POT_ITEMS], inv[POT_ITEMS], mm[POT_ITEMS];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    int bad = 0;
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) {
         const long long k = kstart - POT_ITEMS * t - i;
         if (k >= 1) {
             mm[i] = m[k];
+            const double rk = r[k];
             q[i] = mm[i] / NSTAR;
-            inv[i] = __drcp_rn(r[k]);
+            inv[i] = __drcp_rn(rk);
             pb.q[off + k] = q[i];
             f.inv_r[off + k] = inv[i];
+            if (!(mm[i] >= 0.0) || !(mm[i] < INFINITY) || !(rk > 0.0) || !(rk < CMCG_SF_INFINITY) ||
+                !(inv[i] < INFINITY))
+                bad = 1;
         } else {
             mm[i] = q[i] = inv[i] = 0.0;
         }
@@ -92,7 +102,9 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
         const long long k = kstart - POT_ITEMS * t - i;
         const double innext = (i == 0) ? up : inv[i - 1];
         d[i] = (k >= 1) ? inv[i] - innext : 0.0;
+        if (k >= 1 && !(d[i] >= 0.0)) bad = 1;  // radii out of order
     }
+    bad = __syncthreads_or(bad);
     // exclusive prefix of q in processing order -> C = sum Qexcl * d
     double tq = 0.0;
 #pragma unroll
@@ -111,20 +123,32 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
     const double Sc = block_sum<POT_THREADS>(tc, red);
     const double Sm = block_sum<POT_THREADS>(tm_, red);
     if (t == 0) {
-        double *a = pb.agg + (size_t)blockIdx.x * 4;
+        double *a = pb.agg + (size_t)blockIdx.x * POT_AGG;
         a[0] = Sq;
         a[1] = Sd;
         a[2] = Sc;
         a[3] = Sm;
+        a[4] = bad ? 1.0 : 0.0;
     }
 }
 
-// One block per cluster: Mtotal, Rtidal and the carries entering each tile.
+// One block per cluster: approximate Mtotal, the replay's error bounds and
+// the carries entering each tile.
+//
+// Bounds (u = 2^-53 the unit roundoff, n = N, G = (tiles + 4096) 2^-52, which
+// exceeds twice the error factor gamma of every summation depth these scans
+// use):
+//   chain 1, S_k = S_{k-1} + m_k: the sequential value drifts from the exact
+//     sum by at most (n+2) u Am (each step rounds by at most u |S| <= u Am,
+//     Am >= sum m); the scan's value S~_k errs by at most 2 G Am.
+//   Mtotal = S_N madhoc + cenma madhoc: |exact - approximate| <= dM0.
+//   chain 2, M_{k-1} = M_k - q_k, start Mtotal: drift (n+2) u Mb with
+//     Mb >= every |M_k|, start error dM0, scan error 2 G (Mb + sum q).
+// Each bound carries a factor 1.01 over the sum of its terms.
 __global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__restrict__ cls, Tiles tm, PotBufs pb,
-                                                            int nclusters)
+                                                            PhiBufs ph, int nclusters)
 {
-    __shared__ double s_a[POT_THREADS][3];
-    __shared__ double s_m[POT_THREADS];
+    __shared__ double s_a[POT_THREADS][4];
     const int c = blockIdx.x;
     if (c >= nclusters) return;
     const Cluster &C = cls[c];
@@ -137,54 +161,77 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__rest
     const int lo = t * per, hi = min(ntiles, lo + per);
     // chunk aggregate (outer tiles first) and mass sum
     double q = 0.0, D = 0.0, Cc = 0.0, sm = 0.0;
+    int bad = 0;
     for (int i = lo; i < hi; ++i) {
-        const double *a = pb.agg + (size_t)(b0 + i) * 4;
+        const double *a = pb.agg + (size_t)(b0 + i) * POT_AGG;
         Cc = Cc + a[2] + q * a[1];
         q += a[0];
         D += a[1];
         sm += a[3];
+        bad |= a[4] != 0.0;
     }
     s_a[t][0] = q;
     s_a[t][1] = D;
     s_a[t][2] = Cc;
-    s_m[t] = sm;
-    __syncthreads();
+    s_a[t][3] = sm;
+    bad = __syncthreads_or(bad);
+    PhiCtl &ctl = ph.ctl[c];
     if (t == 0) {
-        // mass: sum over tiles (N_MAX unchanged: every kept star has r < SF_INFINITY)
-        double msum = 0.0;
-        for (int i = 0; i < POT_THREADS; ++i) msum += s_m[i];
-        sc->cenma_m += 0.0;  // cenma.m_new is always zero on this path
-        sc->Mtotal = msum * sc->madhoc + sc->cenma_m * sc->madhoc;
-        sc->Rtidal = sc->orbit_r * pow(sc->Mtotal, 1.0 / 3.0);
-        // exclusive scan of the chunk triples
-        double eq = 0.0, eD = 0.0, eC = 0.0;
+        // exclusive scan of the chunk aggregates
+        double eq = 0.0, eD = 0.0, eC = 0.0, em = 0.0;
         for (int i = 0; i < POT_THREADS; ++i) {
-            const double aq = s_a[i][0], aD = s_a[i][1], aC = s_a[i][2];
+            const double aq = s_a[i][0], aD = s_a[i][1], aC = s_a[i][2], am = s_a[i][3];
             s_a[i][0] = eq;
             s_a[i][1] = eD;
             s_a[i][2] = eC;
+            s_a[i][3] = em;
             eC = eC + aC + eq * aD;
             eq += aq;
             eD += aD;
+            em += am;
         }
+        const double u = 0x1p-53, n = (double)N;
+        const double G = ((double)ntiles + 4096.0) * 0x1p-52;
+        const double madhoc = sc->madhoc, cm = __dmul_rn(sc->cenma_m, madhoc);
+        const double Mapx = __dadd_rn(__dmul_rn(em, madhoc), cm);
+        const double Am = em * (1.0 + 2.0 * G);
+        const double marg1 = 1.01 * ((n + 2.0) * u * Am + 2.0 * G * Am);
+        const double dM0 = 1.01 * marg1 * madhoc + 0x1p-50 * (fabs(Mapx) + fabs(cm));
+        const double Mb = (fabs(Mapx) + dM0) * (1.0 + 0x1p-40);
+        const double Qb = eq * (1.0 + 2.0 * G);
+        ctl.Sm = em;
+        ctl.Qtot = eq;
+        ctl.Dtot = eD;
+        ctl.Mapx = Mapx;
+        ctl.Mb = Mb;
+        ctl.G = G;
+        ctl.marg1 = marg1;
+        ctl.marg2 = 1.01 * ((n + 2.0) * u * Mb + dM0 + 2.0 * G * (Mb + Qb));
+        ctl.c0 = ctl.c1 = 0.0;
+        ctl.fail = (bad || C.phi_sequential) ? 1 : 0;
+        ctl.nsp[0] = ctl.nsp[1] = ctl.nsp[2] = 0;
     }
     __syncthreads();
-    const double Mtot = sc->Mtotal;
-    double eq = s_a[t][0], eD = s_a[t][1], eC = s_a[t][2];
+    const double Mtot = ctl.Mapx;
+    double eq = s_a[t][0], eD = s_a[t][1], eC = s_a[t][2], em = s_a[t][3];
     for (int i = lo; i < hi; ++i) {
-        const double *a = pb.agg + (size_t)(b0 + i) * 4;
-        double *cr = pb.carry + (size_t)(b0 + i) * 2;
+        const double *a = pb.agg + (size_t)(b0 + i) * POT_AGG;
+        double *cr = pb.carry + (size_t)(b0 + i) * POT_CARRY;
         cr[0] = eq;
         cr[1] = Mtot * eD - eC;
+        cr[2] = em;
         eC = eC + a[2] + eq * a[1];
         eq += a[0];
         eD += a[1];
+        em += a[3];
     }
-    (void)N;
 }
 
+// Approximate running values in the reference's indexing:
+//   sapx[k] = S_k (forward mass sum through star k), mapx[k] = M_k (the
+//   enclosed mass the backward loop multiplies at star k), papx[k] = Phi_k.
 __global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                            PotBufs pb)
+                                                            PotBufs pb, PhiBufs ph)
 {
     __shared__ double s_w[POT_THREADS / 32];
     __shared__ double s_lastinv[POT_THREADS / 32];
@@ -194,34 +241,45 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__rest
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX, off = C.off;
     const long long kstart = N - (long long)ct.y * POT_T;
-    double *r = f.r + off, *phi = f.phi + off, *inv_r = f.inv_r + off;
-    float2 *rphif = f.rphif + off;
-    const double Mtot = sc->Mtotal;
-    const double Qin = pb.carry[(size_t)blockIdx.x * 2], Din = pb.carry[(size_t)blockIdx.x * 2 + 1];
+    const double *r = f.r + off, *inv_r = f.inv_r + off, *m = f.m + off;
+    const PhiCtl &ctl = ph.ctl[ct.x];
+    const double Mtot = ctl.Mapx, Sm = ctl.Sm;
+    const double *cr = pb.carry + (size_t)blockIdx.x * POT_CARRY;
+    const double Qin = cr[0], Din = cr[1], SmIn = cr[2];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    double q[POT_ITEMS], inv[POT_ITEMS];
+    double q[POT_ITEMS], inv[POT_ITEMS], mm[POT_ITEMS];
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) {
         const long long k = kstart - POT_ITEMS * t - i;
         q[i] = (k >= 1) ? pb.q[off + k] : 0.0;
         inv[i] = (k >= 1) ? inv_r[k] : 0.0;
+        mm[i] = (k >= 1) ? m[k] : 0.0;
     }
     double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
     if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
     __syncthreads();
     if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : r_next_inv(r, kstart, N);
-    double tq = 0.0;
+    double tq = 0.0, tmm = 0.0;
 #pragma unroll
-    for (int i = 0; i < POT_ITEMS; ++i) tq += q[i];
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        tq += q[i];
+        tmm += mm[i];
+    }
     const double qex = block_excl_prefix<POT_THREADS>(tq, s_w);
-    double dk[POT_ITEMS], run = qex, td = 0.0;
+    const double mex = block_excl_prefix<POT_THREADS>(tmm, s_w);
+    double dk[POT_ITEMS], run = qex, runm = mex, td = 0.0;
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) {
         const long long k = kstart - POT_ITEMS * t - i;
         const double innext = (i == 0) ? up : inv[i - 1];
         const double Mk = (Mtot - Qin) - run;  // mprev when the reference reaches k
         dk[i] = (k >= 1) ? Mk * (inv[i] - innext) : 0.0;
+        if (k >= 1) {
+            pb.mapx[off + k] = Mk;
+            pb.sapx[off + k] = Sm - (SmIn + runm);
+        }
         run += q[i];
+        runm += mm[i];
         td += dk[i];
     }
     const double dex = block_excl_prefix<POT_THREADS>(td, s_w);
@@ -230,23 +288,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__rest
     for (int i = 0; i < POT_ITEMS; ++i) {
         const long long k = kstart - POT_ITEMS * t - i;
         acc += dk[i];
-        if (k >= 1) {
-            const double ph = -acc;
-            phi[k] = ph;
-            rphif[k] = make_float2((float)r[k], (float)ph);
-            if (k == 1) {
-                const double p0 = ph + sc->cenma_m * sc->madhoc / r[1];
-                phi[0] = p0;
-                rphif[0] = make_float2((float)r[0], (float)p0);
-            }
-        }
-    }
-    if (ct.y == 0 && t == 0) {
-        r[N + 1] = CMCG_SF_INFINITY;
-        phi[N + 1] = 0.0;
-        inv_r[N + 1] = __drcp_rn(CMCG_SF_INFINITY);
-        inv_r[0] = __drcp_rn(r[0]);
-        rphif[N + 1] = make_float2((float)CMCG_SF_INFINITY, 0.0f);
+        if (k >= 1) pb.papx[off + k] = -acc;
     }
 }
 

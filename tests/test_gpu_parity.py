@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import cmcgpu
-from parity_util import TOL_ORBIT, TOL_PHI, TOL_SIGMA, TOL_SUM, make_pair, max_rel, sync_state
+from parity_util import TOL_ORBIT, TOL_PHI, TOL_SIGMA, TOL_SUM, make_pair, max_rel, rel_err, sync_state
 
 pytestmark = pytest.mark.gpu
 
@@ -29,9 +29,11 @@ def _init(model, N, imf):
 @pytest.mark.parametrize("model,N,imf", CASES)
 def test_potential(gpulib, orc, model, N, imf):
     ic, o, g = _init(model, N, imf)
-    assert max_rel(g.get("star_phi"), o.get("star_phi")) <= TOL_PHI
-    for s in ("Mtotal", "Rtidal"):
-        assert max_rel(g.scalar(s), o.scalar(s)) <= TOL_PHI
+    # the replay of potential_calculate's three FP64 recurrences is exact
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
+    assert g.scalar("Mtotal") == o.scalar("Mtotal")
+    assert g.scalar("phi_fallback") == 0
+    assert max_rel(g.scalar("Rtidal"), o.scalar("Rtidal")) <= TOL_PHI  # pow() of libm vs CUDA
     assert max_rel(g.get("E"), o.get("E")) <= TOL_PHI
     assert max_rel(g.get("J"), o.get("J")) <= TOL_PHI
     for s in ("KE", "PE", "Etot"):
@@ -164,10 +166,10 @@ def test_tidal_sort_potential_ec3_energy(gpulib, orc, model, N, imf):
     assert np.array_equal(g.ids(), o.ids())
     for gn, on in (("r", "r"), ("m", "m"), ("vr", "vr"), ("vt", "vt"), ("rOld", "rOld")):
         assert np.array_equal(g.get(gn), o.get(on)), gn
-    # potential of the new order
+    # potential of the new order: bit-exact
     o.calc_potential()
     g.calc_potential()
-    assert max_rel(g.get("star_phi"), o.get("star_phi")) <= TOL_PHI
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
     # set_velocities3 from the same potential
     sync_state(o, g, fields=("star_phi",))
     o.energy_conservation3()
@@ -188,8 +190,17 @@ def test_tidal_sort_potential_ec3_energy(gpulib, orc, model, N, imf):
 
 @pytest.mark.parametrize("model,N,imf", CASES[:2])
 def test_free_running_steps(gpulib, orc, model, N, imf):
-    """Whole steps with no state injection: the trajectories stay together and
-    the per-step energy change matches the oracle's."""
+    """Whole steps with no state injection: the same stars in the same order,
+    positions that stay together, and the oracle's per-step energy change.
+
+    The trajectories are not bit-identical: the deflection angles go through
+    libm's sin/cos in the oracle and CUDA's sincos on the GPU, which differ by
+    an ulp for ~20% of pairs (step 0: |dv| <= 4.4e-16, r identical to 8e-15).
+    From step 1 on the time step sums see those differences, every pair
+    deflects with a slightly different dt, and apsides of near-circular orbits
+    amplify it.  Measured on the GB300 (r relative error, step 3 / plummer-eq,
+    king6): 99th percentile 3.1e-10 / 2.0e-11, maximum 9.2e-9 / 3.1e-10.  The
+    bounds hold the bulk to 1e-9 and every star to 1e-7."""
     ic, o, g = _init(model, N, imf)
     e0o, e0g = o.scalar("Etot"), g.scalar("Etot")
     for step in range(4):
@@ -198,7 +209,55 @@ def test_free_running_steps(gpulib, orc, model, N, imf):
         g.check_device(f"step {step}")
         assert g.nstars() == o.nstars()
         assert np.array_equal(g.ids(), o.ids())
-        assert max_rel(g.get("r"), o.get("r")) <= TOL_ORBIT
+        err = rel_err(g.get("r"), o.get("r"))
+        assert np.quantile(err, 0.99) <= 1e-9 and err.max() <= 1e-7, (step, np.quantile(err, 0.99), err.max())
         de_o = o.scalar("Etot") - e0o
         de_g = g.scalar("Etot") - e0g
         assert abs(de_g - de_o) <= 1e-9 * abs(e0o) + 1e-3 * abs(de_o)
+
+
+@pytest.mark.parametrize("model,N,imf", CASES)
+def test_potential_replay_matches_sequential_loop(gpulib, orc, model, N, imf):
+    """The parallel replay and the one-thread loop give the same bits."""
+    ic, o, g = _init(model, N, imf)
+    gs = gpulib.Context([N], gpulib.default_params(orbit_r=ic["rtid"], seed=12345, phi_sequential=1))
+    gs.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    gs.initialize()
+    assert gs.scalar("phi_fallback") == 1 and g.scalar("phi_fallback") == 0
+    assert np.array_equal(g.get("star_phi"), gs.get("star_phi"))
+    assert gs.scalar("Mtotal") == g.scalar("Mtotal")
+    # a handful of sequential points per binade crossed, far below the record capacity
+    for c in (1, 2, 3):
+        assert 2 <= g.scalar(f"phi_nsp{c}") <= 200
+    gs.close()
+
+
+def test_potential_out_of_order_radii_fall_back(gpulib, orc):
+    """Radii out of order (a host upload that skipped the sort) are outside
+    the replay's proof; the cluster falls back to the one-thread loop and
+    still returns the reference's bits."""
+    ic, o, g = _init(cmcgpu.KING, 6000, 1)
+    r = o.get("star_r").copy()
+    r[100], r[101] = r[101], r[100]
+    o.set("star_r", r)
+    g.set("star_r", r)
+    o.calc_potential()
+    g.calc_potential()
+    assert g.scalar("phi_fallback") == 1
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
+
+
+def test_potential_nan_mass_is_reported(gpulib, orc):
+    """A NaN mass stops the potential with the reference's error (cmc_utils.c:688)
+    at the same star."""
+    ic, o, g = _init(cmcgpu.PLUMMER, 4001, 1)
+    m = o.get("star_m").copy()
+    m[1234] = np.nan
+    o.set("star_m", m)
+    g.set("star_m", m)
+    with pytest.raises(orc.OracleError) as eo:
+        o.calc_potential()
+    g.calc_potential()
+    code, idx = g.last_error()
+    assert code == cmcgpu.CMCG_ERR_NAN_MASS == eo.value.code
+    assert idx == eo.value.index == 1234

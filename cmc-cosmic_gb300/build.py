@@ -29,10 +29,14 @@ CUDA_SOURCES = [
     "cmcg_orbit.cu",
     "cmcg_sort.cu",
     "cmcg_potential.cu",
+    "cmcg_phi.cu",
     "cmcg_energy.cu",
     "cmcg_noalloc.cu",
 ]
 C_SOURCES = ["cmcg_ic.c"]
+# the reference-named drop-in layer: a second library on the public C ABI
+DROPIN_SOURCE = "cmc_dropin.cpp"
+DROPIN_LIB = os.path.join(BUILD, "libcmc_dropin.so")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -88,6 +92,10 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
             list(ex.map(_run, jobs))
     if jobs or not os.path.exists(LIB):
         _run([nvcc(), GENCODE, "-shared", "-o", LIB, *objs, "-lm"])
+    src = os.path.join(CSRC, DROPIN_SOURCE)
+    if force or not _newer(DROPIN_LIB, [src, LIB] + headers):
+        _run(["g++", "-O2", "-fPIC", "-std=c++17", "-shared", *inc, "-o", DROPIN_LIB, src,
+              "-L" + BUILD, "-lcmcgpu", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -31,6 +31,9 @@ ERRORS = {
 }
 
 
+CMCG_ERR_NAN_MASS, CMCG_ERR_NAN_PHI = 1, 2
+
+
 class CmcError(RuntimeError):
     def __init__(self, code: int, where: str = "", index: int = -1):
         self.code = code
@@ -45,7 +48,7 @@ class Params(C.Structure):
         ("TIDAL_TREATMENT", C.c_int), ("orbit_r", C.c_double), ("cenma_m", C.c_double),
         ("apsides_max_iter", C.c_long), ("apsides_precision", C.c_double),
         ("apsides_convergence", C.c_double), ("n_try", C.c_long), ("seed", C.c_uint64),
-        ("relax_fp32", C.c_int),
+        ("relax_fp32", C.c_int), ("phi_sequential", C.c_int),
     ]
 
 
@@ -57,6 +60,52 @@ class ICSpec(C.Structure):
 class ICOut(C.Structure):
     _fields_ = [("r", C.POINTER(C.c_double)), ("m", C.POINTER(C.c_double)), ("vr", C.POINTER(C.c_double)),
                 ("vt", C.POINTER(C.c_double)), ("id", C.POINTER(C.c_int64)), ("rtid", C.c_double)]
+
+
+class DropinHost(C.Structure):
+    """cmcx_host of include/cmc_dropin.h."""
+    _fields_ = [
+        ("star", C.c_void_p), ("star_size", C.c_size_t),
+        *[(f"off_{n}", C.c_long) for n in ("r", "vr", "vt", "m", "E", "J", "id", "rnew", "vrnew", "vtnew",
+                                            "rOld", "X", "Y", "r_peri", "r_apo")],
+        ("id_bytes", C.c_int),
+        ("star_r", C.c_void_p), ("star_m", C.c_void_p), ("star_phi", C.c_void_p),
+        ("N_STAR_DIM", C.c_long), ("N_MAX", C.c_void_p), ("N_MAX_NEW", C.c_void_p),
+        *[(n, C.c_void_p) for n in ("Dt", "Mtotal", "Rtidal", "max_r", "Eescaped", "Jescaped", "TidalMassLoss",
+                                     "Etidal", "Etot", "KE", "PE", "tcount")],
+        ("sync_each", C.c_int),
+    ]
+
+
+ABORT_HANDLER = C.CFUNCTYPE(None, C.c_int, C.c_char_p)
+DROPIN_PATH = os.path.join(_HERE, "_build", "libcmc_dropin.so")
+DROPIN_FUNCS = {  # reference-named symbols: (restype, argtypes)
+    "calc_timestep": (None, [C.c_void_p]), "dynamics_apply": (None, [C.c_double, C.c_void_p]),
+    "energy_conservation1": (None, []), "energy_conservation2": (None, []),
+    "new_orbits_calculate": (None, []), "get_positions": (C.c_double, []),
+    "tidally_strip_stars": (None, []), "ComputeIntermediateEnergy": (None, []), "qsorts_new": (None, []),
+    "post_sort_comm": (None, []), "potential_calculate": (C.c_long, []), "calc_potential_new": (None, []),
+    "energy_conservation3": (None, []), "compute_energy_new": (None, []), "potential": (C.c_double, [C.c_double]),
+}
+_dropin = None
+
+
+def dropin_lib() -> C.CDLL:
+    """The reference-named drop-in library (include/cmc_dropin.h)."""
+    global _dropin
+    if _dropin is None:
+        lib()
+        if not os.path.exists(DROPIN_PATH):
+            raise RuntimeError(f"{DROPIN_PATH} is missing: run cmc-cosmic_gb300/build.py")
+        L = C.CDLL(DROPIN_PATH)
+        for name, (res, args) in DROPIN_FUNCS.items():
+            fn = getattr(L, name)
+            fn.restype, fn.argtypes = res, args
+        L.cmcx_default_host.argtypes = [C.POINTER(DropinHost)]
+        L.cmcx_bind.argtypes = [C.POINTER(DropinHost), C.POINTER(Params)]
+        L.cmcx_set_abort.argtypes = [ABORT_HANDLER]
+        _dropin = L
+    return _dropin
 
 
 PLUMMER, KING = 0, 1
@@ -201,6 +250,12 @@ class Context:
     def _check(self, rc, where):
         if rc:
             raise CmcError(rc, where)
+
+    def last_error(self):
+        """(code, star index) of the first device error since the last call; (0, 0) if none."""
+        c, idx = C.c_int(-1), C.c_long(0)
+        rc = lib().cmcg_last_error(self._h, C.byref(c), C.byref(idx))
+        return int(rc), int(idx.value)
 
     def check_device(self, where="device"):
         c, idx = C.c_int(-1), C.c_long(-1)

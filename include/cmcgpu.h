@@ -81,6 +81,9 @@ typedef struct {
     long n_try;                /* N_TRY (50000)                                   */
     uint64_t seed;             /* IDUM: keys the counter-based draws              */
     int relax_fp32;            /* 1 = FP32 relaxation kinematics, FP64 energies   */
+    int phi_sequential;        /* 1 = potential by the plain one-thread loop
+                                  instead of the parallel exact replay (both give
+                                  the reference's bits; for testing)              */
 } cmcg_params;
 
 void cmcg_default_params(cmcg_params *p);

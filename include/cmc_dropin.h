@@ -81,7 +81,11 @@ void cmcx_set_abort(void (*handler)(int code, const char *where));
 /* the device context, for callers that also use the cmcg_* API directly */
 cmcg_ctx *cmcx_context(void);
 
-/* ---- the reference's functions (prototypes as in include/cmc/cmc.h) ---- */
+/* ---- the reference's functions (prototypes as in include/cmc/cmc.h) ----
+ * A file that also includes the reference's cmc.h defines
+ * CMCX_NO_REFERENCE_PROTOTYPES first and takes these from there (cmc.h types
+ * the rng argument as gsl_rng *; it is passed through untouched). */
+#ifndef CMCX_NO_REFERENCE_PROTOTYPES
 /* cmc_utils.c:2132 calc_timestep.  On the device it first closes the
  * previous step (Prev_Dt = Dt, tcount; the host's tcount wins if bound),
  * then does the step's tallies of cmc.c:246-257; sets Dt */
@@ -116,6 +120,7 @@ void energy_conservation3(void);
 void compute_energy_new(void);
 /* cmc_utils.c:112 */
 double potential(double r);
+#endif /* CMCX_NO_REFERENCE_PROTOTYPES */
 
 #ifdef __cplusplus
 }

@@ -119,3 +119,72 @@ def test_ic_generator_is_seeded_and_sorted(gpulib):
     assert not np.array_equal(a["r"], c["r"])
     assert np.all(np.diff(a["r"]) >= 0)
     assert abs(a["m"].sum() - 1.0) < 1e-12
+
+
+GLUE = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include <stdlib.h>
+typedef struct gsl_rng gsl_rng;
+/* the reference's prototypes (include/cmc/cmc.h) as its host program sees them */
+void dynamics_apply(double dt, gsl_rng *rng);
+void calc_timestep(gsl_rng *rng);
+void qsorts_new(void);
+void post_sort_comm(void);
+long potential_calculate(void);
+void calc_potential_new(void);
+double get_positions(void);
+double potential(double r);
+#define CMCX_NO_REFERENCE_PROTOTYPES
+#include "cmc_dropin.h"
+
+typedef struct { double r, vr, vt, m, E, J; long id; double rnew, pad[9]; int se; } star_t;
+static star_t star[1002];
+static double star_r[1002], star_m[1002], star_phi[1002];
+static long N_MAX = 1000, N_MAX_NEW = 1000;
+static int seen;
+static void on_error(int code, const char *where) { (void)where; seen = code; }
+
+int main(void) {
+    cmcx_host h;
+    cmcx_default_host(&h);
+    for (long i = 1; i <= 1000; i++) { star[i].r = i * 1e-3; star[i].m = 1.0; star[i].vt = 0.5; star[i].id = i; }
+    h.star = star; h.star_size = sizeof(star_t);
+    h.off_r = offsetof(star_t, r); h.off_vr = offsetof(star_t, vr); h.off_vt = offsetof(star_t, vt);
+    h.off_m = offsetof(star_t, m); h.off_E = offsetof(star_t, E); h.off_J = offsetof(star_t, J);
+    h.off_id = offsetof(star_t, id); h.off_rnew = offsetof(star_t, rnew); h.id_bytes = sizeof(star[0].id);
+    h.star_r = star_r; h.star_m = star_m; h.star_phi = star_phi; h.N_STAR_DIM = 1002;
+    h.N_MAX = &N_MAX; h.N_MAX_NEW = &N_MAX_NEW;
+    cmcg_params p;
+    cmcg_default_params(&p);
+    p.N_STAR = 1000;
+    cmcx_set_abort(on_error);
+    int rc = cmcx_bind(&h, &p);
+    if (rc == 0) {              /* a GPU is present: one potential through the reference's name */
+        calc_potential_new();
+        rc = seen || !(star_phi[1] < 0.0) || potential(0.5) >= 0.0;
+        cmcx_unbind();
+        printf("bound %d\n", rc);
+        return rc;
+    }
+    printf("no device %d\n", rc);
+    return rc == CMCG_ERR_CUDA ? 0 : 1;
+}
+"""
+
+
+def test_c_host_with_reference_prototypes_links_and_runs(gpulib, tmp_path):
+    """A C program declaring the reference's prototypes (gsl_rng *) and its
+    own star_t compiles against cmc_dropin.h, links against the drop-in, and
+    runs: without a GPU the bind reports CMCG_ERR_CUDA, with one it computes
+    a potential through calc_potential_new()."""
+    import subprocess
+    gpulib.dropin_lib()
+    src = tmp_path / "glue.c"
+    src.write_text(GLUE)
+    exe = tmp_path / "glue"
+    build = os.path.join(ROOT, "cmc-cosmic_gb300", "_build")
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I" + INCLUDE, str(src), "-o", str(exe), "-L" + build,
+                    "-lcmc_dropin", "-lcmcgpu", "-Wl,-rpath," + build], check=True)
+    res = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stdout + res.stderr

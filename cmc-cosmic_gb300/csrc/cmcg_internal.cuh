@@ -293,6 +293,7 @@ __device__ __forceinline__ double function_q_dd(double r, double pot, double E, 
 struct QF32 {
     float E, J, mjN, pj;  // E, J, m_j/N_STAR, (m_j/r_j)/N_STAR as floats
     double rj;            // r_j: the self-potential branch is chosen in FP64
+    double Ed, Jd, mjNd, pjd;  // the same in FP64, for the second filter
 };
 
 __device__ __forceinline__ int fq_sign_f32(const QF32 &s, float2 rp, bool ge)
@@ -304,6 +305,26 @@ __device__ __forceinline__ int fq_sign_f32(const QF32 &s, float2 rp, bool ge)
     const float B = q * q;
     const float Q = 2.0f * A - B;
     const float bound = 1.5e-6f * (2.0f * (fabsf(s.E) + fabsf(rp.y) + fabsf(phis)) + B);
+    if (Q > bound) return 1;
+    if (Q < -bound) return -1;
+    return 0;
+}
+
+// Certified FP64 sign of function_q at table point k, from the stored
+// correctly rounded 1/r_k (no division).  With u = 2^-53: J*inv_r differs from
+// the reference's (double)(J/r) by at most 3.01u|J/r|, so the squares differ
+// by at most 8.2u (J/r)^2; the self-potential from mjN*inv_r by at most
+// 3.01u phis; the two subtractions and the final combination add at most
+// 2u(|E|+|Phi|+|phis|) + u(2|A| + (J/r)^2).  Twice the sum, 16u of each
+// magnitude, is the threshold.  Returns +1, -1, or 0 (undecided).
+__device__ __forceinline__ int fq_sign_f64(const QF32 &s, double inv_rk, double phik, bool ge)
+{
+    const double phis = ge ? __dmul_rn(s.mjNd, inv_rk) : s.pjd;
+    const double A = __dsub_rn(__dsub_rn(s.Ed, phik), phis);
+    const double q = __dmul_rn(s.Jd, inv_rk);
+    const double B = __dmul_rn(q, q);
+    const double Q = __dsub_rn(__dmul_rn(2.0, A), B);
+    const double bound = 0x1p-49 * (fabs(s.Ed) + fabs(phik) + fabs(phis) + fabs(A) + B);
     if (Q > bound) return 1;
     if (Q < -bound) return -1;
     return 0;

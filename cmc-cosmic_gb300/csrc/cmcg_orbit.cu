@@ -35,24 +35,30 @@ static __device__ __forceinline__ double fq(const OrbitCtx &o, long long k)
     return function_q_dd(__ldg(o.r + k), __ldg(o.phi + k), o.E, o.J, o.rj, o.mj, o.invN);
 }
 
-// Sign of function_q at table point k: certified FP32 first, double-double
-// only when the FP32 value lies within its error bound.
+// Sign of function_q at table point k: certified FP32 first, then certified
+// FP64 from the 1/r table, double-double only when both lie within their
+// error bounds (a table point within ~1e-15 of a root).
 static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
 {
-    const int s = fq_sign_f32(o.s, __ldg(o.rphif + k), k >= o.j);
+    const bool ge = k >= o.j;
+    int s = fq_sign_f32(o.s, __ldg(o.rphif + k), ge);
+    if (s) return s;
+    s = fq_sign_f64(o.s, __ldg(o.inv_r + k), __ldg(o.phi + k), ge);
     if (s) return s;
     const double q = fq(o, k);
     return (q > 0.0) - (q < 0.0);
 }
 
 // find_zero_Q, cmc_nr.c:316-383 (bounded; returns -1 if it does not terminate).
-// The end-point values decide the branch and are taken in double-double; the
-// bisection only needs signs.
+// The reference compares the end-point values to choose the direction; when
+// their signs differ the signs decide it, and only same-signed ends are
+// evaluated in double-double and compared.  The bisection only needs signs.
 static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long long kmax)
 {
-    const double qmin = fq(o, kmin), qmax = fq(o, kmax);
+    const int smin = fq_sign(o, kmin), smax = fq_sign(o, kmax);
+    const bool up = (smin != smax) ? (smin < smax) : (fq(o, kmin) < fq(o, kmax));
     int it = 0;
-    if (qmin < qmax) {
+    if (up) {
         do {
             const long long ktry = (kmin + kmax + 1) / 2;
             if (fq_sign(o, ktry) < 0)
@@ -207,8 +213,7 @@ static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, double 
     res.dQdrp = res.dQdra = 0.0;
     // get_positive_Q_index, cmc_orbit.c:30-59
     long long ktemp = j;
-    double Qtemp = fq(o, ktemp);
-    if (Qtemp <= 0.0) {
+    if (fq_sign(o, ktemp) <= 0) {
         ktemp = -1;
         int sgn;
         do {
@@ -277,10 +282,74 @@ static __device__ __forceinline__ void destroy_obj(const Fields &f, long long g)
     f.m[g] = CMCG_DBL_MIN;
 }
 
+// Stars of a block that still sample their position (get_positions_loop's
+// rejection loop, cmc_evolution_thr.c:855-926).  Each round packs the pending
+// stars onto the first threads, so warps are full or idle whatever the spread
+// of trial counts; a star's trials use draws keyed by (star id, trial), so the
+// order of rounds changes nothing.
+struct SampleSmem {
+    double rmin[ORB_T], rmax[ORB_T], F[ORB_T], E[ORB_T], J[ORB_T], rj[ORB_T], mj[ORB_T], vold2[ORB_T],
+        Uold[ORB_T];
+    long long id[ORB_T];
+    int tries[ORB_T];
+    int list[2][ORB_T];
+    int n[2];
+};
+
+// One trial of star slot s: returns true when it is accepted (outputs written).
+static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *sc, const Fields &f, SampleSmem &sm,
+                                                    int s, long long k, long long j0, double invN, double *max_rad,
+                                                    bool *bad)
+{
+    const long long off = C.off, N_MAX = sc->N_MAX;
+    const double rmin = sm.rmin[s], rmax = sm.rmax[s], E = sm.E[s], J = sm.J[s], rj = sm.rj[s], mj = sm.mj[s];
+    const long long idj = sm.id[s], j = j0 + s, g = off + j;
+    const long long tcount = sc->tcount;
+    const uint4 u = draw_block(C.seed, tcount, SITE_TRIAL, idj, (unsigned int)(k - 1));
+    const double X = u01(u.x);
+    const double s0 = 2.0 * X - 1.0;
+    const double g0 = sm.F[s] * u01(u.y);
+    const double r = 0.5 * (rmin + rmax) + 0.25 * (rmax - rmin) * (3.0 * s0 - s0 * s0 * s0);
+    int pok = 1;
+    const double pot =
+        potential_at(f.r + off, f.phi + off, f.inv_r + off, N_MAX, r, &pok) + phi_s(r, rj, mj, invN);
+    if (!pok) {
+        set_error(sc, CMCG_ERR_FINDZERO_R, j);
+        *bad = true;
+        return false;
+    }
+    const double drds = 0.25 * (rmax - rmin) * (3.0 - 3.0 * s0 * s0);
+    const double Q = 2.0 * E - 2.0 * pot - J * J / r / r;
+    double vr;
+    if (Q >= 0.0) {
+        vr = sqrt(Q);
+    } else {
+        if (isnan(Q)) {
+            set_error(sc, CMCG_ERR_Q_NAN, j);
+            *bad = true;
+            return false;
+        }
+        vr = 0;
+    }
+    if (!(g0 < 1.0 / vr * drds)) return false;
+    f.X[g] = X;
+    f.r_peri[g] = rmin;
+    f.r_apo[g] = rmax;
+    if (u01(draw_block(C.seed, tcount, SITE_SIGN, idj, 0u).x) < 0.5) vr = -vr;
+    f.rnew[g] = r;
+    f.vrnew[g] = vr;
+    f.vtnew[g] = J / r;
+    if (r > *max_rad) *max_rad = r;
+    // energy_conservation2: Uoldrnew = potential(rnew) + PHI_S(rnew)
+    f.ec_pre[g] = sm.vold2[s] + 2.0 * (1.0 - 0.5) * (sm.Uold[s] - pot);
+    return true;
+}
+
 __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                  double *partials, unsigned int *tickets)
 {
     __shared__ double red[ORB_T / 32];
+    __shared__ SampleSmem sm;
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
@@ -293,6 +362,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
     const long long g = off + j;
 
     double acc_E = 0.0, acc_J = 0.0, acc_M = 0.0, acc_Et = 0.0, max_rad = 0.0;
+    bool pend = false;
     if (j <= N_NEW) {
         const double Ej = f.E[g], Jj = f.J[g], rj = f.r[g], mj = f.m[g], phij = f.phi[g];
         const double vr0 = f.vr_rel[g], vt0 = f.vt_rel[g];
@@ -332,6 +402,10 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
             o.s.mjN = (float)(mj * invN);
             o.s.pj = (float)((mj / rj) * invN);
             o.s.rj = rj;
+            o.s.Ed = E;
+            o.s.Jd = J;
+            o.s.mjNd = mj * invN;
+            o.s.pjd = (mj / rj) * invN;
             int err = 0;
             const OrbitRs orb = calc_orbit_new(o, j, C.apsides_precision, C.apsides_max_iter, &err);
             if (err) {
@@ -357,57 +431,52 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
                 const double rmin = orb.rp, rmax = orb.ra;
                 const double g1 = sqrt(3.0 * (rmax - rmin) / orb.dQdrp);
                 const double g2 = sqrt(-3.0 * (rmax - rmin) / orb.dQdra);
-                const double F = 1.2 * (g1 >= g2 ? g1 : g2);
-                double r = 0.0, vr = 0.0, X = 0.0, pot = 0.0;
-                long long k;
-                const long long tcount = sc->tcount;
-                bool bad = false;
-                for (k = 1; k <= C.n_try; k++) {
-                    const uint4 u = draw_block(C.seed, tcount, SITE_TRIAL, idj, (unsigned int)(k - 1));
-                    X = u01(u.x);
-                    const double s0 = 2.0 * X - 1.0;
-                    const double g0 = F * u01(u.y);
-                    r = 0.5 * (rmin + rmax) + 0.25 * (rmax - rmin) * (3.0 * s0 - s0 * s0 * s0);
-                    int pok = 1;
-                    pot = potential_at(o.r, o.phi, o.inv_r, N_MAX, r, &pok) + phi_s(r, rj, mj, invN);
-                    if (!pok) {
-                        set_error(sc, CMCG_ERR_FINDZERO_R, j);
-                        bad = true;
-                        break;
-                    }
-                    const double drds = 0.25 * (rmax - rmin) * (3.0 - 3.0 * s0 * s0);
-                    const double Q = 2.0 * E - 2.0 * pot - J * J / r / r;
-                    if (Q >= 0.0) {
-                        vr = sqrt(Q);
-                    } else {
-                        if (isnan(Q)) {
-                            set_error(sc, CMCG_ERR_Q_NAN, j);
-                            bad = true;
-                            break;
-                        }
-                        vr = 0;
-                    }
-                    if (g0 < 1.0 / vr * drds) break;
-                }
-                if (!bad && k == C.n_try + 1) {
-                    set_error(sc, CMCG_ERR_NTRY, j);
-                    bad = true;
-                }
-                if (!bad) {
-                    f.X[g] = X;
-                    f.r_peri[g] = rmin;
-                    f.r_apo[g] = rmax;
-                    if (u01(draw_block(C.seed, tcount, SITE_SIGN, idj, 0u).x) < 0.5) vr = -vr;
-                    const double vt = J / r;
-                    f.rnew[g] = r;
-                    f.vrnew[g] = vr;
-                    f.vtnew[g] = vt;
-                    if (r > max_rad) max_rad = r;
-                    // energy_conservation2: Uoldrnew = potential(rnew) + PHI_S(rnew)
-                    f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - pot);
+                const int ts = threadIdx.x;
+                sm.rmin[ts] = rmin;
+                sm.rmax[ts] = rmax;
+                sm.F[ts] = 1.2 * (g1 >= g2 ? g1 : g2);
+                sm.E[ts] = E;
+                sm.J[ts] = J;
+                sm.rj[ts] = rj;
+                sm.mj[ts] = mj;
+                sm.vold2[ts] = vold2;
+                sm.Uold[ts] = Uoldrold;
+                sm.id[ts] = idj;
+                pend = C.n_try >= 1;
+                if (!pend) set_error(sc, CMCG_ERR_NTRY, j);  // no trial allowed (cmc_evolution_thr.c:888)
+            }
+        }
+    }
+    // rejection sampling in rounds over the block's pending stars
+    const int t = threadIdx.x;
+    if (t == 0) sm.n[0] = 0;
+    __syncthreads();
+    if (pend) {
+        const int p = atomicAdd(&sm.n[0], 1);
+        sm.list[0][p] = t;
+        sm.tries[t] = 0;
+    }
+    __syncthreads();
+    const long long j0 = 1 + (long long)ct.y * ORB_T;
+    for (int cur = 0;; cur ^= 1) {
+        const int n = sm.n[cur];
+        if (n == 0) break;
+        if (t == 0) sm.n[cur ^ 1] = 0;  // last read at the top of the previous round
+        __syncthreads();
+        if (t < n) {
+            const int slot = sm.list[cur][t];
+            const long long k = ++sm.tries[slot];
+            bool bad = false;
+            if (!sample_trial(C, sc, f, sm, slot, k, j0, invN, &max_rad, &bad) && !bad) {
+                if (k >= C.n_try) {
+                    set_error(sc, CMCG_ERR_NTRY, j0 + slot);
+                } else {
+                    const int p = atomicAdd(&sm.n[cur ^ 1], 1);
+                    sm.list[cur ^ 1][p] = slot;
                 }
             }
         }
+        __syncthreads();
     }
     const double tE = block_sum<ORB_T>(acc_E, red);
     const double tJ = block_sum<ORB_T>(acc_J, red);

@@ -4,6 +4,7 @@
 // Memory: one arena per context (a single cudaMalloc at creation), carved into
 // the structure-of-arrays fields, the sort/scan scratch and the per-tile
 // partial sums.  Nothing is allocated while stepping.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -48,6 +49,8 @@ struct cmcg_ctx {
     Fields f{};
     double *partials = nullptr;
     unsigned int *tickets = nullptr;
+    unsigned int *gbar = nullptr;  // grid barrier of the cooperative tidal kernel
+    int tidal_grid = 1;
     SortBufs sb{};
     PotBufs pb{};
     PhiBufs ph{};
@@ -191,6 +194,7 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     np = std::max(np, (size_t)c->t5120.ntiles * 1);
     c->partials = cv.take<double>(np);
     c->tickets = cv.take<unsigned int>(c->ncl);
+    c->gbar = cv.take<unsigned int>(2);
     c->d_sc = cv.take<Scalars>(c->ncl);
     c->d_cls = cv.take<Cluster>(c->ncl);
     c->d_query = cv.take<double>(2);
@@ -327,6 +331,12 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         CK(cudaMemcpyAsync(tts[i]->d_count, tts[i]->count.data(), nclusters * sizeof(int), cudaMemcpyHostToDevice,
                            c->stream));
     }
+    // grid of the cooperative tidal kernel: all co-resident blocks, at most one per tile
+    int dev = 0, nsm = 0, per_sm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tidal, TID_THREADS, 0));
+    c->tidal_grid = std::max(1, std::min(c->t2048.ntiles, nsm * std::max(per_sm, 1)));
     CK(cudaStreamSynchronize(c->stream));
     *out = c;
     return CMCG_OK;
@@ -533,15 +543,32 @@ static int L_orbit(cmcg_ctx *c)
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
+// One cooperative launch: every block of the grid is resident at once, as the
+// kernel's grid barrier requires (the launch fails rather than run otherwise).
 static int L_tidal(cmcg_ctx *c)
 {
     fam_begin(c, F_TIDAL);
-    for (int i = 0; i < TIDAL_PASSES; ++i)
-        k_tidal<<<c->t2048.ntiles, TID_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->partials,
-                                                                 c->tickets);
-    k_tidal_check<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
+    Tiles tv = c->t2048.view();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)c->tidal_grid);
+    cfg.blockDim = dim3(TID_THREADS);
+    cfg.stream = c->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    // arrivals start at zero even after a barrier that timed out; the
+    // generation word is left alone
+    CK(cudaMemsetAsync(c->gbar, 0, sizeof(unsigned int), c->stream));
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_tidal, (const Cluster *)c->d_cls, tv, c->f, c->partials,
+                                             c->gbar, c->ncl);
     fam_end(c);
-    c->launches += TIDAL_PASSES + 1;
+    c->launches += 1;
+    if (e != cudaSuccess) {
+        fprintf(stderr, "cmcgpu: tidal stripping launch failed: %s\n", cudaGetErrorString(e));
+        return CMCG_ERR_CUDA;
+    }
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 

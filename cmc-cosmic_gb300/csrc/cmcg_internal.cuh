@@ -35,6 +35,7 @@ struct Scalars {
     long long Nrel, Nrelbeta[4];
     double qaverelbeta[4], maverelbeta[4], raverelbeta[4];
     double phi_rtidal, gierszalpha;
+    double tid_Rt, tid_phirt;  // tidal radius and its potential for the coming stripping pass
     int tidal_done, tidal_iters;
     int err;
     int pad0;

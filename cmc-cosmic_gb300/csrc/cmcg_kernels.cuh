@@ -16,7 +16,7 @@ constexpr int EC3_T = 256, EN_T = 256;
 constexpr int EXCESS_CAP = 4096;      // listed unphysical predictions per cluster (else full replay)
 constexpr int EC3_FIX_THREADS = 512;
 constexpr int SORT_MAX_PASSES = 8;
-constexpr int TIDAL_PASSES = 32;  // passes after the cluster settles exit at once
+constexpr int TIDAL_PASSES = 32;  // bound on the stripping iteration (it settles in a few)
 
 struct SortBufs {
     unsigned long long *keys[2];
@@ -91,8 +91,7 @@ __global__ void k_relax64(const Cluster *cls, Tiles tm, Fields f, double *partia
 __global__ void k_relax32(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                           double dt_override);
 __global__ void k_orbit(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets);
-__global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets);
-__global__ void k_tidal_check(const Cluster *cls, int nclusters);
+__global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *bar, int nclusters);
 __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, double *partials,
                             unsigned int *tickets);
 __global__ void k_sort_hist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, int pass);

@@ -12,9 +12,9 @@
 //   ec_pre = vold^2 + 2(1-q)(Uoldrold - Uoldrnew),  q = 1/2,
 // is formed here, evaluated exactly as the reference's first partial sum.
 //
-// k_tidal restates one pass of the iteration in tidally_strip_stars
-// (cmc_evolution_thr.c:443-646); the host launches a bounded number of passes
-// and each exits at once after the cluster has settled.
+// k_tidal restates the iteration of tidally_strip_stars
+// (cmc_evolution_thr.c:443-646) in one cooperative launch, its passes
+// separated by a bounded grid barrier.
 #include "cmcg_kernels.cuh"
 #include "cmcgpu.h"
 
@@ -510,90 +510,155 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
     }
 }
 
-// One pass of tidally_strip_stars, cmc_evolution_thr.c:459-622.
-__global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                       double *partials, unsigned int *tickets)
+// Grid-wide barrier for a co-resident (cooperatively launched) grid:
+// bar[0] counts arrivals, bar[1] is the generation.  The wait is bounded; on
+// timeout the caller records CMCG_ERR_SPIN and the kernel stops iterating.
+static __device__ __forceinline__ bool grid_barrier(unsigned int *bar, unsigned int &gen, int *s_ok)
 {
-    __shared__ double red[TID_THREADS / 32];
-    __shared__ double s_phi_rt, s_Rtidal;
-    __shared__ int s_ok;
-    const int2 ct = tm.tiles[blockIdx.x];
-    const Cluster &C = cls[ct.x];
-    if (!counts_ok(C)) return;
-    Scalars *sc = C.sc;
-    if (sc->tidal_done) return;
-    const long long off = C.off;
-    const double NSTAR = (double)sc->N_STAR;
+    __threadfence();
+    __syncthreads();
     if (threadIdx.x == 0) {
-        const double Rt = sc->orbit_r * pow(sc->Mtotal - (sc->TidalMassLoss - sc->OldTidalMassLoss), 1.0 / 3.0);
-        int pok = 1;
-        s_phi_rt = potential_at(f.r + off, f.phi + off, f.inv_r + off, sc->N_MAX, Rt, &pok);
-        s_ok = pok;
-        s_Rtidal = Rt;
+        const unsigned int want = gen + 1u;
+        int ok = 1;
+        if (atomicAdd(&bar[0], 1u) + 1u == gridDim.x) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicExch(&bar[1], want);
+        } else {
+            long long spins = 0;
+            while (*(volatile unsigned int *)&bar[1] != want) {
+                if (++spins > CMCG_SPIN_LIMIT) {
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        gen = want;
+        *s_ok = ok;
     }
     __syncthreads();
-    const double phi_rtidal = s_phi_rt, Rtidal = s_Rtidal;
-    const double gierszalpha = 1.5 - 3.0 * pow(log(C.GAMMA * NSTAR) / NSTAR, 0.25);
-    double aE = 0.0, aJ = 0.0, aM = 0.0, aEt = 0.0;
-    const long long N_NEW = sc->N_MAX_NEW;
-    for (int it = 0; it < TID_T / TID_THREADS; ++it) {
-        const long long i = 1 + (long long)ct.y * TID_T + it * TID_THREADS + threadIdx.x;
-        if (i > N_NEW) break;
-        const long long g = off + i;
-        const double rn = f.rnew[g];
-        bool strip;
-        if (C.TIDAL_TREATMENT == 0)
-            strip = (f.r_apo[g] > Rtidal && rn < 1000000);
-        else
-            strip = (f.E[g] > gierszalpha * phi_rtidal && rn < 1000000);
-        if (strip) {
-            const double m = f.m[g], E = f.E[g], J = f.J[g];
-            aE += E * m / NSTAR;
-            aJ += J * m / NSTAR;
-            aM += m / NSTAR;
-            aEt += E * m / NSTAR;
-            destroy_obj(f, g);
-        }
-    }
-    const double tE = block_sum<TID_THREADS>(aE, red);
-    const double tJ = block_sum<TID_THREADS>(aJ, red);
-    const double tM = block_sum<TID_THREADS>(aM, red);
-    const double tEt = block_sum<TID_THREADS>(aEt, red);
-    __shared__ int s_last;
-    if (threadIdx.x == 0) {
-        double *slot = partials + (size_t)blockIdx.x * TID_NPART;
-        slot[0] = tE;
-        slot[1] = tJ;
-        slot[2] = tM;
-        slot[3] = tEt;
-    }
-    if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
-        double a[TID_NPART];
-        for (int q = 0; q < TID_NPART; ++q)
-            a[q] = reduce_partials_sum<TID_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], TID_NPART, q, red);
-        if (threadIdx.x == 0) {
-            if (!s_ok) set_error(sc, CMCG_ERR_FINDZERO_R, 0);
-            if (sc->tidal_iters == 0) sc->Etidal = 0.0;  // cmc_evolution_thr.c:452
-            sc->Rtidal = Rtidal;
-            sc->phi_rtidal = phi_rtidal;
-            sc->Eescaped += a[0];
-            sc->Jescaped += a[1];
-            sc->Etidal += a[3];
-            sc->DTidalMassLoss = a[2];
-            sc->TidalMassLoss += a[2];
-            sc->tidal_iters += 1;
-            if (!(a[2] > 0)) sc->tidal_done = 1;
-        }
-    }
+    return *s_ok != 0;
 }
 
-// After the bounded passes: a cluster still shedding stars is an error.
-__global__ void k_tidal_check(const Cluster *__restrict__ cls, int nclusters)
+// Tidal radius and its potential for the coming pass of cluster c
+// (cmc_evolution_thr.c:459-466).
+static __device__ __forceinline__ void tidal_radius(const Cluster &C, const Fields &f)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nclusters) return;
-    Scalars *sc = cls[c].sc;
-    if (!sc->tidal_done) set_error(sc, CMCG_ERR_TIDAL_ITER, sc->tidal_iters);
+    Scalars *sc = C.sc;
+    const double Rt = sc->orbit_r * pow(sc->Mtotal - (sc->TidalMassLoss - sc->OldTidalMassLoss), 1.0 / 3.0);
+    int pok = 1;
+    const double phi = potential_at(f.r + C.off, f.phi + C.off, f.inv_r + C.off, sc->N_MAX, Rt, &pok);
+    if (!pok) set_error(sc, CMCG_ERR_FINDZERO_R, 0);
+    sc->tid_Rt = Rt;
+    sc->tid_phirt = phi;
+}
+
+// tidally_strip_stars, cmc_evolution_thr.c:443-646: the iteration in one
+// cooperative launch.  Each pass scans every tile of every cluster not yet
+// settled (tiles strided over the co-resident grid, per-tile partials), then
+// one block per cluster sums its tiles in tile order, records the pass
+// (Rtidal, tallies) and either settles the cluster or prepares the next
+// radius.  At most TIDAL_PASSES passes; a cluster still shedding mass after
+// them is an error (CMCG_ERR_TIDAL_ITER).
+__global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                       double *partials, unsigned int *bar, int nclusters)
+{
+    __shared__ double red[TID_THREADS / 32];
+    __shared__ int s_ok;
+    unsigned int gen = 0;
+    if (threadIdx.x == 0) gen = *(volatile unsigned int *)&bar[1];
+    for (int c = blockIdx.x; c < nclusters; c += gridDim.x) {
+        const Cluster &C = cls[c];
+        if (threadIdx.x == 0 && counts_ok(C) && !C.sc->tidal_done) tidal_radius(C, f);
+    }
+    if (!grid_barrier(bar, gen, &s_ok)) {
+        if (threadIdx.x == 0) set_error(cls[0].sc, CMCG_ERR_SPIN, 0);
+        return;
+    }
+    for (int pass = 0; pass < TIDAL_PASSES; ++pass) {
+        for (int b = blockIdx.x; b < tm.ntiles; b += gridDim.x) {
+            const int2 ct = tm.tiles[b];
+            const Cluster &C = cls[ct.x];
+            Scalars *sc = C.sc;
+            if (*(volatile int *)&sc->tidal_done || !counts_ok(C)) continue;
+            const long long off = C.off;
+            const double NSTAR = (double)sc->N_STAR;
+            const double phi_rtidal = *(volatile double *)&sc->tid_phirt, Rtidal = *(volatile double *)&sc->tid_Rt;
+            const double gierszalpha = 1.5 - 3.0 * pow(log(C.GAMMA * NSTAR) / NSTAR, 0.25);
+            double aE = 0.0, aJ = 0.0, aM = 0.0, aEt = 0.0;
+            const long long N_NEW = sc->N_MAX_NEW;
+            for (int it = 0; it < TID_T / TID_THREADS; ++it) {
+                const long long i = 1 + (long long)ct.y * TID_T + it * TID_THREADS + threadIdx.x;
+                if (i > N_NEW) break;
+                const long long g = off + i;
+                const double rn = f.rnew[g];
+                bool strip;
+                if (C.TIDAL_TREATMENT == 0)
+                    strip = (f.r_apo[g] > Rtidal && rn < 1000000);
+                else
+                    strip = (f.E[g] > gierszalpha * phi_rtidal && rn < 1000000);
+                if (strip) {
+                    const double m = f.m[g], E = f.E[g], J = f.J[g];
+                    aE += E * m / NSTAR;
+                    aJ += J * m / NSTAR;
+                    aM += m / NSTAR;
+                    aEt += E * m / NSTAR;
+                    destroy_obj(f, g);
+                }
+            }
+            const double tE = block_sum<TID_THREADS>(aE, red);
+            const double tJ = block_sum<TID_THREADS>(aJ, red);
+            const double tM = block_sum<TID_THREADS>(aM, red);
+            const double tEt = block_sum<TID_THREADS>(aEt, red);
+            if (threadIdx.x == 0) {
+                double *slot = partials + (size_t)b * TID_NPART;
+                slot[0] = tE;
+                slot[1] = tJ;
+                slot[2] = tM;
+                slot[3] = tEt;
+            }
+        }
+        if (!grid_barrier(bar, gen, &s_ok)) {
+            if (threadIdx.x == 0) set_error(cls[0].sc, CMCG_ERR_SPIN, pass);
+            return;
+        }
+        // one block per cluster: the pass's sums in tile order
+        for (int c = blockIdx.x; c < nclusters; c += gridDim.x) {
+            const Cluster &C = cls[c];
+            Scalars *sc = C.sc;
+            if (*(volatile int *)&sc->tidal_done || !counts_ok(C)) continue;
+            double a[TID_NPART];
+            for (int q = 0; q < TID_NPART; ++q)
+                a[q] = reduce_partials_sum<TID_THREADS>(partials, tm.first[c], tm.count[c], TID_NPART, q, red);
+            if (threadIdx.x == 0) {
+                if (sc->tidal_iters == 0) sc->Etidal = 0.0;  // cmc_evolution_thr.c:452
+                sc->Rtidal = sc->tid_Rt;
+                sc->phi_rtidal = sc->tid_phirt;
+                sc->Eescaped += a[0];
+                sc->Jescaped += a[1];
+                sc->Etidal += a[3];
+                sc->DTidalMassLoss = a[2];
+                sc->TidalMassLoss += a[2];
+                sc->tidal_iters += 1;
+                if (!(a[2] > 0)) {
+                    sc->tidal_done = 1;
+                } else if (pass + 1 == TIDAL_PASSES) {
+                    set_error(sc, CMCG_ERR_TIDAL_ITER, sc->tidal_iters);
+                } else {
+                    tidal_radius(C, f);
+                }
+            }
+            __syncthreads();
+        }
+        if (!grid_barrier(bar, gen, &s_ok)) {
+            if (threadIdx.x == 0) set_error(cls[0].sc, CMCG_ERR_SPIN, pass);
+            return;
+        }
+        int open = 0;
+        for (int c = 0; c < nclusters && !open; ++c) open = !*(volatile int *)&cls[c].sc->tidal_done;
+        if (!open) break;
+    }
 }
 
 // potential(r) for one radius of cluster c (host queries, energy bookkeeping).

@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     const double invN = 1.0 / (double)sc->N_STAR;
     const double m = f.m[g], ri = f.r[g], rold = f.rOld[g];
     int pok = 1;
-    const double Unewrold = potential_at(f.r + off, f.phi + off, f.inv_r + off, sc->N_MAX, rold, &pok) +
+    const double Unewrold = potential_at(f.r + off, f.phi + off, f.inv_r + off, sc->N_MAX, rold, &pok, ridx_of(C, f)) +
                             phi_s(rold, ri, m, invN);
     if (!pok) set_error(sc, CMCG_ERR_FINDZERO_R, i);
     const double Unewrnew = f.phi[g] + phi_s(ri, ri, m, invN);

@@ -55,6 +55,8 @@ struct cmcg_ctx {
     PotBufs pb{};
     PhiBufs ph{};
     long long rec_total = 0;
+    long long ridx_total = 0;
+    int ridx_Bmax = 0;
     Ec3Bufs eb{};
     double *d_query = nullptr;
     TileTable t128, t256, t1024, t2048, t5120;
@@ -183,6 +185,7 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
         c->ph.rec[i] = cv.take<SPRec>((size_t)c->rec_total);
     }
     c->ph.ctl = cv.take<PhiCtl>(c->ncl);
+    f.ridx = cv.take<int>((size_t)c->ridx_total);
     c->eb.a = cv.take<double>(tot);
     c->eb.list = cv.take<long long>((size_t)c->ncl * EXCESS_CAP);
     c->eb.nlist = cv.take<unsigned int>(c->ncl);
@@ -237,6 +240,14 @@ void cmcg_default_params(cmcg_params *p)
 // is computed by the one-thread loop.
 static long long phi_rec_cap(long long cap) { return 4096 + cap / 16; }
 
+// Buckets of the radius index: about 16 stars each, 2^10 to 2^16.
+static int ridx_buckets(long long cap)
+{
+    int B = 1024;
+    while (B < 65536 && (long long)B * 16 < cap) B <<= 1;
+    return B;
+}
+
 int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_params *params)
 {
     if (!out || nclusters < 1 || !capacity || !params) return CMCG_ERR_ARG;
@@ -265,7 +276,11 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         tot += stride;
     }
     c->total = tot;
-    for (int k = 0; k < nclusters; ++k) c->rec_total += phi_rec_cap(capacity[k]);
+    for (int k = 0; k < nclusters; ++k) {
+        c->rec_total += phi_rec_cap(capacity[k]);
+        c->ridx_total += ridx_buckets(capacity[k]) + 1;
+        c->ridx_Bmax = std::max(c->ridx_Bmax, ridx_buckets(capacity[k]));
+    }
     std::vector<int2> tabs[5];
     build_table(c->t128, c->cap, ORB_T, tabs[0]);
     build_table(c->t256, c->cap, RELAX_T, tabs[1]);
@@ -295,7 +310,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
     CK(cudaMemcpyAsync(c->sb.hist_off, hist_off.data(), nclusters * sizeof(long long), cudaMemcpyHostToDevice,
                        c->stream));
     c->h_cls.resize(nclusters);
-    long long rec_off = 0;
+    long long rec_off = 0, ridx_off = 0;
     for (int k = 0; k < nclusters; ++k) {
         Cluster &C = c->h_cls[k];
         const cmcg_params &p = params[k];
@@ -320,6 +335,9 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         C.rec_off = rec_off;
         C.rec_cap = phi_rec_cap(c->cap[k]);
         rec_off += C.rec_cap;
+        C.ridx_off = ridx_off;
+        C.ridx_B = ridx_buckets(c->cap[k]);
+        ridx_off += C.ridx_B + 1;
     }
     CK(cudaMemcpyAsync(c->d_cls, c->h_cls.data(), nclusters * sizeof(Cluster), cudaMemcpyHostToDevice, c->stream));
     TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t5120};
@@ -405,6 +423,7 @@ __global__ void k_refresh_tables(const Cluster *cls, Fields f, int k, long long 
     const double r = f.r[g];
     f.inv_r[g] = __drcp_rn(r);
     f.rphif[g] = make_float2((float)r, (float)f.phi[g]);
+    if (i == 0) cls[k].sc->ridx_ok = 0;  // radii may have changed: search the whole table until rebuilt
 }
 
 // New star count after a host upload (the sentinel r[N+1] is copied separately).
@@ -413,6 +432,7 @@ __global__ void k_set_count(const Cluster *cls, int k, long long N)
     Scalars *sc = cls[k].sc;
     sc->N_MAX = N;
     sc->N_MAX_NEW = N;
+    sc->ridx_ok = 0;
 }
 
 int cmcg_put_stars(cmcg_ctx *c, int k, long N, const double *r, const double *m, const double *vr, const double *vt,
@@ -479,8 +499,10 @@ static int L_pot(cmcg_ctx *c)
     k_phi_rec3<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
     k_phi_final<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph);
     k_phi_seq<<<c->ncl, 32, 0, c->stream>>>(c->d_cls, c->f, c->ph, c->ncl);
+    k_ridx_build<<<dim3((unsigned)((c->ridx_Bmax + RIDX_THREADS) / RIDX_THREADS), (unsigned)c->ncl), RIDX_THREADS, 0,
+                   c->stream>>>(c->d_cls, c->f, c->ph, c->ncl);
     fam_end(c);
-    c->launches += 9;
+    c->launches += 10;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 

@@ -48,6 +48,9 @@ struct Scalars {
     // whether the last potential fell back to the one-thread loop
     long long phi_nsp[3];
     long long phi_fallback;
+    // radius index (RIdx) of the current star order
+    long long ridx_base;
+    int ridx_shift, ridx_ok;
 };
 
 // Per-cluster constant description (built on the host, read-only on device).
@@ -65,6 +68,8 @@ struct Cluster {
     int relax_fp32;
     int phi_sequential;    // 1: potential by the plain sequential loop (one thread)
     long long rec_off, rec_cap;  // this cluster's slice of the sequential-point records
+    long long ridx_off;    // this cluster's radius index table (ridx_B + 1 entries)
+    int ridx_B, pad2;
 };
 
 // Device-resident fields (all concatenated over clusters).
@@ -78,6 +83,7 @@ struct Fields {
     double *rOld;                      // star[].rOld after the sort
     double *sigma_r, *sigma;           // sigma_array.r, sigma_array.sigma
     float2 *rphif;                     // (float r_k, float Phi_k): table for certified FP32 sign tests
+    int *ridx;                         // radius index tables of all clusters (RIdx)
     long long *id;                     // star[].id
     // second buffers for the sort's gather (swapped on the host)
     double *r2, *m2, *ec_pre2;
@@ -224,12 +230,31 @@ __device__ __forceinline__ long long find_zero_r(const double *__restrict__ r, l
     return kmin;
 }
 
+// Bucketed index over the sorted radii: bucket(x) = (bits(x) - bits(r_1)) >> shift,
+// clamped to B-1, and T[b] = the first star k in 1..N+1 whose radius lies in
+// bucket b or above (T[B] = N+2).  Every star below T[b] has r_k < x and every
+// star from T[b+1] on has r_k > x for x in bucket b, so the reference's search
+// for x can start from [T[b]-1, T[b+1]-1] and gives the same index.
+struct RIdx {
+    const int *T;        // null: no index (radii not known to be in order)
+    long long base;
+    int shift, B;
+};
+
+__device__ __forceinline__ int ridx_bucket(const RIdx &ix, double x)
+{
+    const long long d = __double_as_longlong(x) - ix.base;
+    if (d < 0) return 0;
+    const long long b = d >> ix.shift;
+    return b >= ix.B - 1 ? ix.B - 1 : (int)b;
+}
+
 // potential(r), cmc_utils.c:112-164 with SEARCH_GRID = 0.  inv_r[k] holds the
 // correctly rounded 1.0/r[k], so the Henon interpolation performs exactly the
 // reference's divisions with two of the three precomputed.
 __device__ __forceinline__ double potential_at(const double *__restrict__ r, const double *__restrict__ phi,
                                                const double *__restrict__ inv_r, long long N_MAX, double x,
-                                               int *ok)
+                                               int *ok, const RIdx &ix = RIdx{nullptr, 0, 0, 0})
 {
     if (x == 0.0) return __ldg(phi);
     const double r1 = __ldg(r + 1);
@@ -237,7 +262,18 @@ __device__ __forceinline__ double potential_at(const double *__restrict__ r, con
         double p0 = __ldg(phi), p1 = __ldg(phi + 1);
         return __dsub_rn(p0, __ddiv_rn(__dmul_rn(__dsub_rn(p0, p1), r1), x));
     }
-    long long i = (N_MAX == 1) ? 1 : find_zero_r(r, 1, N_MAX + 1, x);
+    long long i;
+    if (N_MAX == 1) {
+        i = 1;
+    } else if (ix.T) {
+        const int b = ridx_bucket(ix, x);
+        long long lo = __ldg(ix.T + b) - 1, hi = __ldg(ix.T + b + 1) - 1;
+        if (lo < 1) lo = 1;
+        if (hi > N_MAX + 1) hi = N_MAX + 1;
+        i = (hi <= lo) ? lo : find_zero_r(r, lo, hi, x);
+    } else {
+        i = find_zero_r(r, 1, N_MAX + 1, x);
+    }
     if (i > N_MAX) {  // x beyond the r = SF_INFINITY sentinel: the reference's check fails too
         *ok = 0;
         return 0.0;
@@ -252,6 +288,14 @@ __device__ __forceinline__ double potential_at(const double *__restrict__ r, con
     const double ii = __ldg(inv_r + i), ii1 = __ldg(inv_r + i + 1);
     return __dadd_rn(pi, __ddiv_rn(__dmul_rn(__dsub_rn(pi1, pi), __dsub_rn(ii, __ddiv_rn(1.0, x))),
                                    __dsub_rn(ii, ii1)));
+}
+
+// The radius index of cluster C, or none while it is stale.
+__device__ __forceinline__ RIdx ridx_of(const Cluster &C, const Fields &f)
+{
+    const Scalars *sc = C.sc;
+    if (!sc->ridx_ok || !f.ridx) return RIdx{nullptr, 0, 0, 0};
+    return RIdx{f.ridx + C.ridx_off, sc->ridx_base, sc->ridx_shift, C.ridx_B};
 }
 
 // MPI_PHI_S(rad, j), cmc.h:2175

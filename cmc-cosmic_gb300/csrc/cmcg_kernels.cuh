@@ -67,7 +67,7 @@ struct PhiCtl {          // per cluster
     double marg1, marg2;           // bounds on |approximate - sequential| of chains 1, 2
     double c0, c1;                 // chain 3 bound: c0 + c1 / r_k
     int fail;                      // 1: replay impossible or refused, recompute sequentially
-    int pad;
+    int disorder;                  // radii out of order or non-finite input (no radius index)
     long long nsp[3];
 };
 struct PhiBufs {
@@ -108,6 +108,8 @@ __global__ void k_phi_cls3(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, P
 __global__ void k_phi_rec3(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);
 __global__ void k_phi_final(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph);
 __global__ void k_phi_seq(const Cluster *cls, Fields f, PhiBufs ph, int nclusters);
+__global__ void k_ridx_build(const Cluster *cls, Fields f, PhiBufs ph, int nclusters);
+constexpr int RIDX_THREADS = 256;
 __global__ void k_begin_step(const Cluster *cls, int nclusters);
 __global__ void k_end_step(const Cluster *cls, int nclusters);
 __global__ void k_ec3(const Cluster *cls, Tiles tm, Fields f, Ec3Bufs eb);

@@ -312,7 +312,7 @@ static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *s
     const double r = 0.5 * (rmin + rmax) + 0.25 * (rmax - rmin) * (3.0 * s0 - s0 * s0 * s0);
     int pok = 1;
     const double pot =
-        potential_at(f.r + off, f.phi + off, f.inv_r + off, N_MAX, r, &pok) + phi_s(r, rj, mj, invN);
+        potential_at(f.r + off, f.phi + off, f.inv_r + off, N_MAX, r, &pok, ridx_of(C, f)) + phi_s(r, rj, mj, invN);
     if (!pok) {
         set_error(sc, CMCG_ERR_FINDZERO_R, j);
         *bad = true;
@@ -417,7 +417,8 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
                 f.vtnew[g] = vt0;
                 bool ok = true;
                 int pok = 1;
-                const double Uoldrnew = potential_at(o.r, o.phi, o.inv_r, N_MAX, rj, &pok) + phi_s(rj, rj, mj, invN);
+                const double Uoldrnew =
+                    potential_at(o.r, o.phi, o.inv_r, N_MAX, rj, &pok, ridx_of(C, f)) + phi_s(rj, rj, mj, invN);
                 ok = pok;
                 if (!ok) set_error(sc, CMCG_ERR_FINDZERO_R, j);
                 f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - Uoldrnew);
@@ -548,7 +549,7 @@ static __device__ __forceinline__ void tidal_radius(const Cluster &C, const Fiel
     Scalars *sc = C.sc;
     const double Rt = sc->orbit_r * pow(sc->Mtotal - (sc->TidalMassLoss - sc->OldTidalMassLoss), 1.0 / 3.0);
     int pok = 1;
-    const double phi = potential_at(f.r + C.off, f.phi + C.off, f.inv_r + C.off, sc->N_MAX, Rt, &pok);
+    const double phi = potential_at(f.r + C.off, f.phi + C.off, f.inv_r + C.off, sc->N_MAX, Rt, &pok, ridx_of(C, f));
     if (!pok) set_error(sc, CMCG_ERR_FINDZERO_R, 0);
     sc->tid_Rt = Rt;
     sc->tid_phirt = phi;
@@ -671,7 +672,7 @@ __global__ void k_potential_query(const Cluster *__restrict__ cls, Fields f, int
         return;
     }
     int ok = 1;
-    out[0] = potential_at(f.r + C.off, f.phi + C.off, f.inv_r + C.off, C.sc->N_MAX, x, &ok);
+    out[0] = potential_at(f.r + C.off, f.phi + C.off, f.inv_r + C.off, C.sc->N_MAX, x, &ok, ridx_of(C, f));
     out[1] = ok ? 0.0 : 1.0;
 }
 

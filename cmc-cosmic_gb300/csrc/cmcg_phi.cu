@@ -794,4 +794,50 @@ __global__ void k_phi_seq(const Cluster *__restrict__ cls, Fields f, PhiBufs ph,
     sc->phi_fallback = 1;
 }
 
+// Radius index of the new star order (RIdx, cmcg_internal.cuh): one thread
+// per bucket finds its first star by a lower-bound search on the radii's bit
+// patterns.  Not built (queries then search the whole table) when the radii
+// are out of order or not finite.
+__global__ void __launch_bounds__(RIDX_THREADS) k_ridx_build(const Cluster *__restrict__ cls, Fields f, PhiBufs ph,
+                                                             int nclusters)
+{
+    const int c = blockIdx.y;
+    if (c >= nclusters) return;
+    const Cluster &C = cls[c];
+    if (!counts_ok(C)) return;
+    Scalars *sc = C.sc;
+    const long long N = sc->N_MAX;
+    const int B = C.ridx_B;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (*(volatile int *)&ph.ctl[c].disorder || N < 2 || B < 2) {
+        if (b == 0) sc->ridx_ok = 0;
+        return;
+    }
+    const double *r = f.r + C.off;
+    const long long base = __double_as_longlong(r[1]), dmax = __double_as_longlong(r[N]) - base;
+    int s = 0;
+    while (s < 62 && (dmax >> s) > (long long)(B - 2)) ++s;
+    if (b == 0) {
+        sc->ridx_base = base;
+        sc->ridx_shift = s;
+        sc->ridx_ok = 1;
+    }
+    if (b > B) return;
+    int *T = f.ridx + C.ridx_off;
+    if (b == B) {
+        T[B] = (int)(N + 2);
+        return;
+    }
+    const long long key = base + ((long long)b << s);
+    long long lo = 1, hi = N + 1;  // r[N+1] = SF_INFINITY is above every key of bucket B-1's range
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (__double_as_longlong(r[mid]) < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    T[b] = (int)lo;
+}
+
 }  // namespace cmcg

@@ -209,6 +209,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__rest
         ctl.marg2 = 1.01 * ((n + 2.0) * u * Mb + dM0 + 2.0 * G * (Mb + Qb));
         ctl.c0 = ctl.c1 = 0.0;
         ctl.fail = (bad || C.phi_sequential) ? 1 : 0;
+        ctl.disorder = bad ? 1 : 0;
         ctl.nsp[0] = ctl.nsp[1] = ctl.nsp[2] = 0;
     }
     __syncthreads();

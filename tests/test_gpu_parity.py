@@ -311,3 +311,21 @@ def test_tidal_stripping_iterates_to_a_fixed_point(gpulib, orc):
     assert np.array_equal(g.get("rnew") == 1e10, o.get("rnew") == 1e10)
     assert max_rel(g.scalar("Rtidal"), o.scalar("Rtidal")) <= TOL_PHI
     assert max_rel(g.scalar("TidalMassLoss"), o.scalar("TidalMassLoss")) <= 1e-10
+
+
+@pytest.mark.parametrize("model,N,imf", CASES[:2])
+def test_potential_queries_through_the_radius_index(gpulib, orc, model, N, imf):
+    """potential(r) through the bucketed radius index equals the oracle's
+    full binary search bit for bit: at table radii, their neighbours in the
+    last bit, midpoints, random radii, and both ends of the table."""
+    ic, o, g = _init(model, N, imf)
+    r = o.get("star_r")[1:N + 1]
+    rng = np.random.default_rng(11)
+    pick = rng.choice(N, 300, replace=False)
+    xs = list(r[pick]) + list(np.nextafter(r[pick], np.inf)) + list(np.nextafter(r[pick], 0.0))
+    inner = pick[pick < N - 1]
+    xs += list(0.5 * (r[inner] + r[inner + 1]))
+    xs += list(np.exp(rng.uniform(np.log(r[0]), np.log(r[-1]), 300)))
+    xs += [r[0], r[-1], np.nextafter(r[-1], np.inf), 0.5 * r[0], 2.0 * r[-1]]
+    for x in xs:
+        assert g.potential(float(x)) == o.potential(float(x)), x

@@ -153,22 +153,75 @@ def allreduce_sum(dist, x: float) -> float:
     return float(t.item())
 
 
-def make_model(N: int, seed: int):
+# The named synthetic configurations (seeded generators; no dataset exists for
+# them).  king1e6 is the headline; the others are measured on request.
+CONFIGS = {
+    "plummer1e5": dict(model="plummer", N=100_000, imf=0, bf=0.0, fp32=0,
+                       desc="Plummer, equal masses, N=1e5, plain FP64 Henon step"),
+    "king1e6": dict(model="king", w0=6.0, N=1_000_000, imf=1, bf=0.0, fp32=0,
+                    desc="King W0=6, Kroupa IMF, N=1e6, plain FP64 Henon step"),
+    "ensemble128": dict(model="ensemble", n=128, lo=10_000, hi=1_000_000, imf=1, bf=0.0, fp32=0,
+                        desc="128 clusters, N log-uniform in [1e4,1e6], alternating Plummer / King W0 in "
+                             "{3,5,7,9}, Kroupa IMF, one launch per kernel, whole step in a CUDA graph, FP64"),
+    "king4e6": dict(model="king", w0=7.0, N=4_000_000, imf=1, bf=0.0, fp32=0,
+                    desc="King W0=7, Kroupa IMF, N=4e6, plain FP64 Henon step (plain sampler)"),
+    "king1e7bin": dict(model="king", w0=7.0, N=10_000_000, imf=1, bf=0.1, fp32=1,
+                       desc="King W0=7, Kroupa IMF, N=1e7, 10% composite binaries, FP32 relaxation "
+                            "kinematics with FP64 energies, FP64 potential and root finds"),
+}
+
+
+def make_model(N: int, seed: int, cfg=None):
     import cmcgpu
 
-    return cmcgpu.generate(cmcgpu.KING, N, seed=seed, w0=6.0, imf=1)
+    cfg = cfg or CONFIGS["king1e6"]
+    if cfg["model"] == "plummer":
+        return cmcgpu.generate(cmcgpu.PLUMMER, N, seed=seed, imf=cfg["imf"], binary_fraction=cfg["bf"])
+    return cmcgpu.generate(cmcgpu.KING, N, seed=seed, w0=cfg.get("w0", 6.0), imf=cfg["imf"],
+                           binary_fraction=cfg["bf"])
+
+
+def make_clusters(cfg, N, rank):
+    """[(N_c, ic, seed)] for the configuration: one cluster, or the ensemble
+    (per-cluster seeds derived from one master seed)."""
+    import numpy as np
+
+    import cmcgpu
+
+    if cfg["model"] != "ensemble":
+        return [(N, make_model(N, 20240607 + rank, cfg), cmcgpu.derive_seed(777, rank))]
+    from concurrent.futures import ThreadPoolExecutor
+
+    master = 20240607 + rank
+    rng = np.random.default_rng(master)
+    Ns = np.exp(rng.uniform(np.log(cfg["lo"]), np.log(cfg["hi"]), cfg["n"])).astype(int)
+    w0s = rng.choice([3.0, 5.0, 7.0, 9.0], cfg["n"])
+
+    def one(i):
+        seed = cmcgpu.derive_seed(master, i)
+        if i % 2 == 0:
+            ic = cmcgpu.generate(cmcgpu.PLUMMER, int(Ns[i]), seed=seed, imf=cfg["imf"])
+        else:
+            ic = cmcgpu.generate(cmcgpu.KING, int(Ns[i]), seed=seed, w0=float(w0s[i]), imf=cfg["imf"])
+        return int(Ns[i]), ic, seed
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(one, range(cfg["n"])))
 
 
 # ------------------------------------------------------------- CPU legs ---
 def _ref_worker(args):
     """One host core: the oracle (reference algorithm, taus113 draws) stepping a
     bounded sample of the workload's model; returns (stars*steps, seconds)."""
-    n, steps, warmup, seed = args
+    n, steps, warmup, seed, cfg_name = args
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     sys.path.insert(0, os.path.join(ROOT, "cmc-cosmic_gb300"))
     import oracle
 
-    ic = make_model(n, seed)
+    cfg = CONFIGS[cfg_name]
+    if cfg["model"] == "ensemble":  # a sample cluster of the ensemble's kind
+        cfg = dict(CONFIGS["king1e6"], w0=5.0)
+    ic = make_model(n, seed, cfg)
     o = oracle.Oracle(ic, oracle.default_params(orbit_r=ic["rtid"], seed=seed, draw_mode=oracle.DRAW_TAUS113))
     o.initialize()
     for _ in range(warmup):
@@ -181,7 +234,7 @@ def _ref_worker(args):
     return done, time.perf_counter() - t0
 
 
-def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int):
+def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int, cfg_name: str = "king1e6"):
     import multiprocessing as mp
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -190,7 +243,7 @@ def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int):
     oracle.build()
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
-        res = pool.map(_ref_worker, [(n_sample, steps, warmup, 1000 + i) for i in range(procs)])
+        res = pool.map(_ref_worker, [(n_sample, steps, warmup, 1000 + i, cfg_name) for i in range(procs)])
     updates = sum(r[0] for r in res)
     secs = max(r[1] for r in res)
     return updates / secs, secs
@@ -199,77 +252,102 @@ def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int):
 # ------------------------------------------------------------ GPU leg ----
 def run_ours(a, rank, ws, dist):
     import numpy as np
+    import torch
 
     import cmcgpu
 
     cmcgpu.build()
-    N = a.N
-    ic = make_model(N, seed=20240607 + rank)
-    p = cmcgpu.default_params(orbit_r=ic["rtid"], seed=cmcgpu.derive_seed(777, rank))
-    ctx = cmcgpu.Context([N], p)
-    ctx.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    cfg = CONFIGS[a.config]
+    N = a.N or cfg.get("N", 0)
+    clusters = make_clusters(cfg, N, rank)
+    params = [cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed, relax_fp32=cfg["fp32"]) for _, ic, seed in clusters]
+    ctx = cmcgpu.Context([n for n, _, _ in clusters], params)
+    for c, (n, ic, _) in enumerate(clusters):
+        ctx.load(c, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
     ctx.initialize()
+    ncl = len(clusters)
+
+    def stars():
+        return sum(ctx.nstars(c) for c in range(ncl))
+
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+
+    def timed(k, graph):
+        """k steps between CUDA events recorded on the context's stream."""
+        ctx.use_graph(graph)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier(dist)
+        ctx.synchronize()
+        e0.record(stream)
+        ctx.step(k)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), ctx.launch_count()
+
+    # warm-up in the timed mode (the first step captures the graph)
+    ctx.use_graph(True)
     ctx.step(a.warmup)
     ctx.check_device("warmup")
-    n_start = ctx.nstars()
+    n_start = stars()
 
-    # ---- device-resident timed region
-    import torch
-
-    torch.cuda.synchronize()
+    # ---- headline: device-resident steps replayed from the CUDA graph
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     time.sleep(0.6)
-    ctx.profile(True)
-    ctx.kernel_time("reset")
-    barrier(dist)
-    ctx.synchronize()
-    t0 = time.perf_counter()
-    launches = 0
-    for _ in range(a.steps):
-        ctx.step(1)
-        launches += ctx.launch_count()
-    ctx.synchronize()
-    dt = time.perf_counter() - t0
-    barrier(dist)
+    ms, launches = timed(a.steps, True)
     clk = clocks.stop()
     ctx.check_device("timed steps")
-    fam = {}
-    for name in ALG_BYTES:
-        ms, n = ctx.kernel_time(name)
-        fam[name] = (ms, n)
+    ms_max = allreduce_max(dist, ms)
+    updates = allreduce_sum(dist, float(n_start * a.steps))
+    value = updates / (ms_max * 1e-3)
+
+    # ---- the same number of steps launched directly, with CUDA events per kernel family
+    n_prof = stars()
+    ctx.profile(True)
+    ctx.kernel_time("reset")
+    ms_prof, _ = timed(a.steps, False)
+    ctx.check_device("profiled steps")
+    fam = {name: ctx.kernel_time(name) for name in ALG_BYTES}
     ctx.profile(False)
     step_ms = sum(v[0] for v in fam.values()) / a.steps
-    dt_max = allreduce_max(dist, dt)
-    updates = allreduce_sum(dist, float(n_start * a.steps))
-    value = updates / dt_max
     top = max((k for k in fam if ALG_BYTES[k] > 0), key=lambda k: fam[k][0])
     ms_top, n_top = fam[top]
     peak, peak_kind = measured_peak()
-    achieved = ALG_BYTES[top] * n_start / (ms_top / n_top * 1e-3) / 1e9
+    achieved = ALG_BYTES[top] * n_prof / (ms_top / n_top * 1e-3) / 1e9
     per_family = {k: {"ms_per_step": round(v[0] / a.steps, 4), "launches": v[1]} for k, v in fam.items() if v[1]}
 
-    # ---- end to end: host buffers in pinned memory, copies inside the timed region
-    cap = N + 16
+    # ---- end to end through the public API: host star arrays in pinned memory,
+    # copied in before and out after every step
+    cap = max(n for n, _, _ in clusters) + 16
     bufs = {k: torch.empty(cap, dtype=torch.float64, pin_memory=True).numpy() for k in ("r", "m", "vr", "vt", "E", "J")}
     bufs["id"] = torch.empty(cap, dtype=torch.int64, pin_memory=True).numpy()
-    n_host = ctx.get_stars(0, bufs)
+    host = []
+    for c in range(ncl):
+        b = {k: v.copy() if ncl > 1 else v for k, v in bufs.items()}
+        host.append((b, ctx.get_stars(c, b)))
+    ctx.use_graph(False)
     h2d = d2h = 0
+    e2e_updates = 0
     barrier(dist)
     t1 = time.perf_counter()
-    e2e_updates = 0
     for _ in range(a.steps):
-        ctx.put_stars(0, n_host, bufs)
-        h2d += n_host * 7 * 8
-        e2e_updates += n_host
+        for c, (b, n) in enumerate(host):
+            ctx.put_stars(c, n, b)
+            h2d += n * 7 * 8
+            e2e_updates += n
         ctx.step(1)
-        n_host = ctx.get_stars(0, bufs)
-        d2h += n_host * 7 * 8
+        for c in range(ncl):
+            b = host[c][0]
+            n = ctx.get_stars(c, b)
+            host[c] = (b, n)
+            d2h += n * 7 * 8
     e2e_dt = time.perf_counter() - t1
     barrier(dist)
     ctx.check_device("e2e steps")
     e2e_value = allreduce_sum(dist, float(e2e_updates)) / allreduce_max(dist, e2e_dt)
 
+    model_txt = {"plummer": "Plummer model", "king": f"King W0={cfg.get('w0')} model",
+                 "ensemble": "Plummer and King models"}[cfg["model"]]
     out = {
         "metric": METRIC,
         "value": value,
@@ -277,25 +355,29 @@ def run_ours(a, rank, ws, dist):
         "n_gpus": ws,
         "steps": a.steps,
         "warmup": a.warmup,
-        "ms_per_step": dt_max / a.steps * 1e3,
+        "ms_per_step": ms_max / a.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
-        "data": "synthetic (seeded King W0=6 model, Kroupa 2001 IMF; no dataset)",
-        "config": {"workload": f"King W0=6, Kroupa IMF, N={N}, plain FP64 Henon step", "N": N,
+        "dtype": "f64" if not cfg["fp32"] else "f64 (f32 relaxation kinematics)",
+        "data": f"synthetic (seeded {model_txt}, {'Kroupa 2001 IMF' if cfg['imf'] else 'equal masses'}; no dataset)",
+        "config": {"workload": cfg["desc"], "name": a.config, "N": N if ncl == 1 else None, "clusters": ncl,
                    "stars_at_start": n_start, "parallelism": f"replicas x{ws}",
-                   "l2": "state ~250 B/star exceeds the 129 MB L2 at this N: no flush needed"},
+                   "timing": "CUDA events on the library's stream; whole step replayed from a CUDA graph",
+                   "l2": "state ~250 B/star exceeds the 129 MB L2 at this size: no flush needed"
+                         if n_start * 250 > 129e6 else "L2 holds the state: steps read warm data"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // a.steps,
                 "d2h_bytes_per_step": d2h // a.steps},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": (NCU_TRAFFIC_PER_STAR[top] * n_start if top in NCU_TRAFFIC_PER_STAR else None),
+                     "traffic": (NCU_TRAFFIC_PER_STAR[top] * n_prof if top in NCU_TRAFFIC_PER_STAR else None),
                      "fp64_pipe_active": NCU_FP64_PIPE_ACTIVE.get(top),
-                     "alg_bytes_per_star": ALG_BYTES[top], "ms_per_launch": ms_top / n_top},
+                     "alg_bytes_per_star": ALG_BYTES[top], "ms_per_launch": ms_top / n_top,
+                     "timed_in": "the profiled direct-launch pass"},
         "kernels": per_family,
         "kernel_ms_per_step": step_ms,
+        "profiled_ms_per_step": ms_prof / a.steps,
         "clocks": clk,
     }
     ctx.close()
@@ -308,8 +390,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--N", type=int, default=1_000_000)
-    ap.add_argument("--cpu-sample", type=int, default=100_000, help="stars per CPU-baseline process")
+    ap.add_argument("--config", default="king1e6", choices=sorted(CONFIGS))
+    ap.add_argument("--N", type=int, default=0, help="override the configuration's N (single-cluster configs)")
+    ap.add_argument("--cpu-sample", type=int, default=1_000_000, help="stars per CPU-baseline process")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="timed oracle steps of the 1-core CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--probe-rates", action="store_true",
                     help="build and run the FP64/FP32/INT64 pipe-rate probe, then exit")
@@ -329,15 +413,16 @@ def main():
         if rank != 0:
             return
         procs = min(os.cpu_count() or 1, 16)
-        val, secs = cpu_baseline(a.cpu_sample, a.steps, a.warmup, procs)
+        cfg = CONFIGS[a.config]
+        val, secs = cpu_baseline(a.cpu_sample, a.steps, a.warmup, procs, a.config)
         out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
                "ms_per_step": secs / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "impl": "reference",
-               "data": "synthetic (seeded King W0=6 model, Kroupa 2001 IMF)",
-               "config": {"workload": f"King W0=6, Kroupa IMF, N={a.N}, plain FP64 Henon step", "N": a.N},
+               "data": "synthetic (seeded cluster models of the configuration; no dataset)",
+               "config": {"workload": cfg["desc"], "name": a.config, "N": a.N or cfg.get("N")},
                "cpu_baseline": {"value": val, "unit": UNIT, "cores": procs, "kind": "port",
-                                "sample": f"{procs} processes x {a.cpu_sample}-star King W0=6 Kroupa clusters, "
-                                          f"{a.steps} timed steps each (reference algorithm, taus113 draws)"},
+                                "sample": f"{procs} processes x {a.cpu_sample}-star clusters of the configuration's "
+                                          f"model, {a.steps} timed steps each (reference algorithm, taus113 draws)"},
                "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         return
@@ -345,10 +430,11 @@ def main():
     out = run_ours(a, rank, ws, dist)
     if rank == 0:
         if not a.no_cpu_baseline and ws == 1:
-            val, secs = cpu_baseline(a.cpu_sample, 1, 0, 1)
+            val, secs = cpu_baseline(a.cpu_sample, a.cpu_steps, 0, 1, a.config)
             out["cpu_baseline"] = {"value": val, "unit": UNIT, "cores": 1, "kind": "port",
-                                   "sample": f"one {a.cpu_sample}-star King W0=6 Kroupa cluster, 1 step "
-                                             f"({secs:.1f} s; reference algorithm with taus113 draws, 1 core)"}
+                                   "sample": f"one {a.cpu_sample}-star cluster of the configuration's model, "
+                                             f"{a.cpu_steps} steps ({secs:.1f} s; reference algorithm with taus113 "
+                                             f"draws, 1 core)"}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

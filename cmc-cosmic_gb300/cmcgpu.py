@@ -156,6 +156,8 @@ def lib() -> C.CDLL:
         L.cmcg_last_error.argtypes = [vp, C.POINTER(i), C.POINTER(l)]
         L.cmcg_launch_count.argtypes = [vp]
         L.cmcg_launch_count.restype = l
+        L.cmcg_stream.argtypes = [vp]
+        L.cmcg_stream.restype = vp
         L.cmcg_ic_generate.argtypes = [C.POINTER(ICSpec), C.POINTER(ICOut)]
         L.cmcg_derive_seed.argtypes = [C.c_uint64, C.c_uint64]
         L.cmcg_derive_seed.restype = C.c_uint64
@@ -348,6 +350,10 @@ class Context:
 
     def synchronize(self):
         self._check(lib().cmcg_synchronize(self._h), "synchronize")
+
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t as an integer (torch.cuda.ExternalStream takes it)."""
+        return int(lib().cmcg_stream(self._h) or 0)
 
     def launch_count(self) -> int:
         return int(lib().cmcg_launch_count(self._h))

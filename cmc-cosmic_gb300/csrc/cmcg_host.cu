@@ -64,10 +64,13 @@ struct cmcg_ctx {
     size_t arena_bytes = 0;
     int relax_fp32 = 0;
     // graphs
-    bool use_graph = false, graph_ready = false;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    long launches = 0, launches_last = 0, graph_launches = 0;
+    // The sort swaps the field pointers every step, so a captured two-step
+    // graph is tied to the pointer parity it was captured at: one per parity.
+    bool use_graph = false, graph_ready[2] = {false, false};
+    int parity = 0;
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    long launches = 0, launches_last = 0, graph_launches[2] = {0, 0};
     // profiling
     bool profile = false;
     std::vector<ProfRec> prof;
@@ -364,8 +367,10 @@ int cmcg_destroy(cmcg_ctx *c)
 {
     if (!c) return CMCG_ERR_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->gexec) cudaGraphExecDestroy(c->gexec);
-    if (c->graph) cudaGraphDestroy(c->graph);
+    for (int p = 0; p < 2; ++p) {
+        if (c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);
+        if (c->graph[p]) cudaGraphDestroy(c->graph[p]);
+    }
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->arena) cudaFree(c->arena);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -600,6 +605,7 @@ static void swap_sorted(cmcg_ctx *c)
     std::swap(c->f.m, c->f.m2);
     std::swap(c->f.id, c->f.id2);
     std::swap(c->f.ec_pre, c->f.ec_pre2);
+    c->parity ^= 1;
 }
 
 static int L_sort(cmcg_ctx *c)
@@ -695,13 +701,14 @@ static int capture_pair(cmcg_ctx *c)
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->profile = prof;
-    c->graph_launches = c->launches - l0;  // kernel nodes in the two-step graph
+    const int p = c->parity;  // two swaps: back at the parity captured at
+    c->graph_launches[p] = c->launches - l0;  // kernel nodes in the two-step graph
     c->launches = l0;
     if (rc) return rc;
     if (e != cudaSuccess) return CMCG_ERR_CUDA;
-    c->graph = g;
-    CK(cudaGraphInstantiate(&c->gexec, g, 0));
-    c->graph_ready = true;
+    c->graph[p] = g;
+    CK(cudaGraphInstantiate(&c->gexec[p], g, 0));
+    c->graph_ready[p] = true;
     return CMCG_OK;
 }
 
@@ -713,11 +720,12 @@ int cmcg_run(cmcg_ctx *c, int nsteps)
     const long l0 = c->launches;
     int done = 0;
     if (c->use_graph && !c->profile && nsteps >= 2) {
-        if (!c->graph_ready) RUN(capture_pair(c));
-        // one graph holds two steps: the sort's buffer swap alternates the field pointers
+        const int p = c->parity;
+        if (!c->graph_ready[p]) RUN(capture_pair(c));
+        // one graph holds two steps, which bring the pointer parity back to p
         while (nsteps - done >= 2) {
-            CK(cudaGraphLaunch(c->gexec, c->stream));
-            c->launches += c->graph_launches;
+            CK(cudaGraphLaunch(c->gexec[p], c->stream));
+            c->launches += c->graph_launches[p];
             done += 2;
         }
     }
@@ -734,6 +742,8 @@ int cmcg_synchronize(cmcg_ctx *c)
 }
 
 long cmcg_launch_count(cmcg_ctx *c) { return c ? c->launches_last : -1; }
+
+void *cmcg_stream(cmcg_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 int cmcg_profile(cmcg_ctx *c, int enable)
 {

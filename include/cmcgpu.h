@@ -153,6 +153,9 @@ int cmcg_step(cmcg_ctx *ctx);
 int cmcg_run(cmcg_ctx *ctx, int nsteps);
 int cmcg_use_graph(cmcg_ctx *ctx, int enable);
 int cmcg_synchronize(cmcg_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or record events against the library's launches. */
+void *cmcg_stream(cmcg_ctx *ctx);
 
 /* ------------------------------------------------------------ queries --- */
 /* potential(r) of cmc_utils.c:112 for cluster c (synchronous). */

@@ -249,31 +249,27 @@ __device__ __forceinline__ int ridx_bucket(const RIdx &ix, double x)
     return b >= ix.B - 1 ? ix.B - 1 : (int)b;
 }
 
-// potential(r), cmc_utils.c:112-164 with SEARCH_GRID = 0.  inv_r[k] holds the
-// correctly rounded 1.0/r[k], so the Henon interpolation performs exactly the
-// reference's divisions with two of the three precomputed.
-__device__ __forceinline__ double potential_at(const double *__restrict__ r, const double *__restrict__ phi,
-                                               const double *__restrict__ inv_r, long long N_MAX, double x,
-                                               int *ok, const RIdx &ix = RIdx{nullptr, 0, 0, 0})
+// FindZero_r's answer for x >= r[1] (cmc_utils.c:140-146): the largest k in
+// [1, N_MAX+1] with r[k] < x, through the radius index when there is one.
+__device__ __forceinline__ long long potential_index(const double *__restrict__ r, long long N_MAX, double x,
+                                                     const RIdx &ix)
 {
-    if (x == 0.0) return __ldg(phi);
-    const double r1 = __ldg(r + 1);
-    if (x < r1) {
-        double p0 = __ldg(phi), p1 = __ldg(phi + 1);
-        return __dsub_rn(p0, __ddiv_rn(__dmul_rn(__dsub_rn(p0, p1), r1), x));
-    }
-    long long i;
-    if (N_MAX == 1) {
-        i = 1;
-    } else if (ix.T) {
+    if (N_MAX == 1) return 1;
+    if (ix.T) {
         const int b = ridx_bucket(ix, x);
         long long lo = __ldg(ix.T + b) - 1, hi = __ldg(ix.T + b + 1) - 1;
         if (lo < 1) lo = 1;
         if (hi > N_MAX + 1) hi = N_MAX + 1;
-        i = (hi <= lo) ? lo : find_zero_r(r, lo, hi, x);
-    } else {
-        i = find_zero_r(r, 1, N_MAX + 1, x);
+        return (hi <= lo) ? lo : find_zero_r(r, lo, hi, x);
     }
+    return find_zero_r(r, 1, N_MAX + 1, x);
+}
+
+// The Henon interpolation of potential(r) in interval i (cmc_utils.c:147-163).
+__device__ __forceinline__ double potential_in(const double *__restrict__ r, const double *__restrict__ phi,
+                                               const double *__restrict__ inv_r, long long N_MAX, double x,
+                                               long long i, int *ok)
+{
     if (i > N_MAX) {  // x beyond the r = SF_INFINITY sentinel: the reference's check fails too
         *ok = 0;
         return 0.0;
@@ -288,6 +284,22 @@ __device__ __forceinline__ double potential_at(const double *__restrict__ r, con
     const double ii = __ldg(inv_r + i), ii1 = __ldg(inv_r + i + 1);
     return __dadd_rn(pi, __ddiv_rn(__dmul_rn(__dsub_rn(pi1, pi), __dsub_rn(ii, __ddiv_rn(1.0, x))),
                                    __dsub_rn(ii, ii1)));
+}
+
+// potential(r), cmc_utils.c:112-164 with SEARCH_GRID = 0.  inv_r[k] holds the
+// correctly rounded 1.0/r[k], so the Henon interpolation performs exactly the
+// reference's divisions with two of the three precomputed.
+__device__ __forceinline__ double potential_at(const double *__restrict__ r, const double *__restrict__ phi,
+                                               const double *__restrict__ inv_r, long long N_MAX, double x,
+                                               int *ok, const RIdx &ix = RIdx{nullptr, 0, 0, 0})
+{
+    if (x == 0.0) return __ldg(phi);
+    const double r1 = __ldg(r + 1);
+    if (x < r1) {
+        double p0 = __ldg(phi), p1 = __ldg(phi + 1);
+        return __dsub_rn(p0, __ddiv_rn(__dmul_rn(__dsub_rn(p0, p1), r1), x));
+    }
+    return potential_in(r, phi, inv_r, N_MAX, x, potential_index(r, N_MAX, x, ix), ok);
 }
 
 // The radius index of cluster C, or none while it is stale.

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     const long long i = 1 + (long long)ct.y * EC3_T + threadIdx.x;
     const long long off = C.off, g = off + i;
     if (i > sc->N_MAX_NEW) return;
-    const double invN = 1.0 / (double)sc->N_STAR;
+    const double invN = sc->madhoc;  // 1.0 / N_STAR (cmc_utils.c:1183)
     const double m = f.m[g], ri = f.r[g], rold = f.rOld[g];
     int pok = 1;
     const double Unewrold = potential_at(f.r + off, f.phi + off, f.inv_r + off, sc->N_MAX, rold, &pok, ridx_of(C, f)) +
@@ -161,29 +161,36 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
     // on one rank the remainder is dropped (cmc_utils.c:313-348)
 }
 
-__global__ void __launch_bounds__(EN_T) k_energy(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                 double *partials, unsigned int *tickets)
+// Eight stars per thread: the per-star FP64 work is the reference's
+// expressions; the sums take one addition per star before the block tree.
+__global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                       double *partials, unsigned int *tickets)
 {
-    __shared__ double red[EN_T / 32];
+    __shared__ double red[EN_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long N = sc->N_MAX, off = C.off;
-    const long long i = 1 + (long long)ct.y * EN_T + threadIdx.x;
     const double madhoc = sc->madhoc;
+    // the central mass's share of PE, the same for every star (cmc_utils.c:633)
+    const double pc = f.phi[off] * sc->cenma_m * madhoc / (double)N;
     double K = 0.0, P = 0.0;
-    if (i <= N) {
+#pragma unroll 4
+    for (int it = 0; it < EN_T / EN_THREADS; ++it) {
+        const long long i = 1 + (long long)ct.y * EN_T + it * EN_THREADS + threadIdx.x;
+        if (i > N) break;
         const long long g = off + i;
         const double vr = f.vr[g], vt = f.vt[g], ph = f.phi[g], m = f.m[g];
-        f.E[g] = ph + 0.5 * (sqr(vr) + sqr(vt));
+        const double v2 = sqr(vr) + sqr(vt);
+        f.E[g] = ph + 0.5 * v2;
         f.J[g] = f.r[g] * vt;
-        K = 0.5 * (sqr(vr) + sqr(vt)) * m * madhoc;
-        P = ph * m * madhoc;
-        P += f.phi[off] * sc->cenma_m * madhoc / (double)N;
+        K += 0.5 * v2 * m * madhoc;
+        P += ph * m * madhoc;
+        P += pc;
     }
-    const double tK = block_sum<EN_T>(K, red);
-    const double tP = block_sum<EN_T>(P, red);
+    const double tK = block_sum<EN_THREADS>(K, red);
+    const double tP = block_sum<EN_THREADS>(P, red);
     __shared__ int s_last;
     if (threadIdx.x == 0) {
         double *slot = partials + (size_t)blockIdx.x * 2;
@@ -191,8 +198,8 @@ __global__ void __launch_bounds__(EN_T) k_energy(const Cluster *__restrict__ cls
         slot[1] = tP;
     }
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
-        const double sK = reduce_partials_sum<EN_T>(partials, tm.first[ct.x], tm.count[ct.x], 2, 0, red);
-        const double sP = reduce_partials_sum<EN_T>(partials, tm.first[ct.x], tm.count[ct.x], 2, 1, red);
+        const double sK = reduce_partials_sum<EN_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], 2, 0, red);
+        const double sP = reduce_partials_sum<EN_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], 2, 1, red);
         if (threadIdx.x == 0) {
             double aK = sK, aP = sP;
             // compute_energy_new, cmc_utils.c:2020-2025

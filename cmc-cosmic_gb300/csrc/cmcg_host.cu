@@ -162,7 +162,7 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     for (double **p : dfields) *p = cv.take<double>(tot);
     f.id = cv.take<long long>(tot);
     f.id2 = cv.take<long long>(tot);
-    f.rphif = cv.take<float2>(tot);
+    f.rphif = cv.take<float4>(tot);
     c->sb.keys[0] = cv.take<unsigned long long>(tot);
     c->sb.keys[1] = cv.take<unsigned long long>(tot);
     c->sb.vals[0] = cv.take<unsigned int>(tot);
@@ -427,7 +427,7 @@ __global__ void k_refresh_tables(const Cluster *cls, Fields f, int k, long long 
     const long long g = cls[k].off + i;
     const double r = f.r[g];
     f.inv_r[g] = __drcp_rn(r);
-    f.rphif[g] = make_float2((float)r, (float)f.phi[g]);
+    f.rphif[g] = rphi_entry(r, f.phi[g]);
     if (i == 0) cls[k].sc->ridx_ok = 0;  // radii may have changed: search the whole table until rebuilt
 }
 
@@ -514,7 +514,8 @@ static int L_pot(cmcg_ctx *c)
 static int L_energy(cmcg_ctx *c)
 {
     fam_begin(c, F_ENERGY);
-    k_energy<<<c->t256.ntiles, EN_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials, c->tickets);
+    k_energy<<<c->t2048.ntiles, EN_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->partials,
+                                                             c->tickets);
     fam_end(c);
     c->launches += 1;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;

@@ -82,7 +82,7 @@ struct Fields {
     double *ec_pre;                    // vold^2 + (Uoldrold - Uoldrnew), see set_velocities3
     double *rOld;                      // star[].rOld after the sort
     double *sigma_r, *sigma;           // sigma_array.r, sigma_array.sigma
-    float2 *rphif;                     // (float r_k, float Phi_k): table for certified FP32 sign tests
+    float4 *rphif;                     // (r_k, Phi_k hi, Phi_k lo, 0) as floats: certified FP32 sign tests
     int *ridx;                         // radius index tables of all clusters (RIdx)
     long long *id;                     // star[].id
     // second buffers for the sort's gather (swapped on the host)
@@ -310,6 +310,22 @@ __device__ __forceinline__ RIdx ridx_of(const Cluster &C, const Fields &f)
     return RIdx{f.ridx + C.ridx_off, sc->ridx_base, sc->ridx_shift, C.ridx_B};
 }
 
+// a / b rounded to nearest, given y = RN(1/b), in five FP64 operations instead
+// of a division.  Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34, 1990;
+// restated as the quotient-correction theorem in Muller et al., Handbook of
+// Floating-Point Arithmetic): if y is within half an ulp of 1/b and q within
+// one ulp of a/b, then r = a - b q is exact (one FMA) and RN(q + r y) = RN(a/b).
+// q0 = RN(a y) may lie up to 1.5 ulp from a/b; one correction brings it within
+// half an ulp plus 2^-52 ulp, and the second correction is the theorem's step.
+// Valid for normal operands whose quotient and remainders stay normal, which
+// holds for the radii, masses, potentials and angular momenta it is used on.
+__device__ __forceinline__ double div_rcp(double a, double b, double y)
+{
+    const double q0 = __dmul_rn(a, y);
+    const double q1 = __fma_rn(__fma_rn(-q0, b, a), y, q0);
+    return __fma_rn(__fma_rn(-q1, b, a), y, q1);
+}
+
 // MPI_PHI_S(rad, j), cmc.h:2175
 __device__ __forceinline__ double phi_s(double rad, double rj, double mj, double invN)
 {
@@ -348,20 +364,38 @@ __device__ __forceinline__ double function_q_dd(double r, double pot, double E, 
 // sign, hence also the sign of the reference's long double evaluation.
 // Returns +1, -1, or 0 when the caller must evaluate in double-double.
 struct QF32 {
-    float E, J, mjN, pj;  // E, J, m_j/N_STAR, (m_j/r_j)/N_STAR as floats
-    double rj;            // r_j: the self-potential branch is chosen in FP64
-    double Ed, Jd, mjNd, pjd;  // the same in FP64, for the second filter
+    float E, El, J, mjN, pj;  // E as a float pair (E ~ E + El), J, m_j/N_STAR, (m_j/r_j)/N_STAR as floats
+    double rj;                // r_j: the self-potential branch is chosen in FP64
+    double Ed, Jd, mjNd, pjd; // the same in FP64, for the second filter
 };
 
-__device__ __forceinline__ int fq_sign_f32(const QF32 &s, float2 rp, bool ge)
+// (float r, Phi as a float pair hi + lo with |Phi - hi - lo| <= 2^-48 |Phi|, 0)
+__device__ __forceinline__ float4 rphi_entry(double r, double phi)
+{
+    const float hi = (float)phi;
+    return make_float4((float)r, hi, (float)(phi - (double)hi), 0.0f);
+}
+
+// E - Phi is formed in float-float (exact difference of the high parts plus
+// the low parts), so its error is 2^-23 |E - Phi| + 2^-46 (|E| + |Phi|) rather
+// than 2^-24 of each term.  With the reciprocal of the float radius (2^-23)
+// the self-potential carries at most 2^-22, (J/r)^2 at most 2^-20.7, and the
+// final combinations 2^-24 of their magnitudes:
+//   |Q_f32 - Q| <= 2^-21 (|D| + phis + |A|) + 2^-20.5 (J/r)^2 + 2^-45 (|E| + |Phi|),
+// D = E - Phi, A = D - phis.  The threshold below is over twice that.
+__device__ __forceinline__ int fq_sign_f32(const QF32 &s, float4 rp, bool ge)
 {
     const float ir = __frcp_rn(rp.x);
     const float phis = ge ? s.mjN * ir : s.pj;
-    const float A = (s.E - rp.y) - phis;
+    const float d = s.E - rp.y;
+    const float bv = d - s.E;
+    const float err = (s.E - (d - bv)) + (-rp.y - bv);  // Eh - Phi_hi = d + err exactly
+    const float D = d + (err + (s.El - rp.z));
+    const float A = D - phis;
     const float q = s.J * ir;
     const float B = q * q;
     const float Q = 2.0f * A - B;
-    const float bound = 1.5e-6f * (2.0f * (fabsf(s.E) + fabsf(rp.y) + fabsf(phis)) + B);
+    const float bound = 0x1p-19f * (fabsf(D) + fabsf(phis) + fabsf(A) + B) + 0x1p-42f * (fabsf(s.E) + fabsf(rp.y));
     if (Q > bound) return 1;
     if (Q < -bound) return -1;
     return 0;

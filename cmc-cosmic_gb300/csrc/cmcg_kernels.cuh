@@ -12,7 +12,7 @@ constexpr int TID_T = 2048, TID_THREADS = 256, TID_NPART = 4;
 constexpr int SORT_THREADS = 256, SORT_ITEMS = 8, SORT_T = SORT_THREADS * SORT_ITEMS, RADIX = 256;
 constexpr int GATHER_T = 256;
 constexpr int POT_THREADS = 256, POT_ITEMS = 4, POT_T = POT_THREADS * POT_ITEMS;
-constexpr int EC3_T = 256, EN_T = 256;
+constexpr int EC3_T = 256, EN_T = 2048, EN_THREADS = 256;
 constexpr int EXCESS_CAP = 4096;      // listed unphysical predictions per cluster (else full replay)
 constexpr int EC3_FIX_THREADS = 512;
 constexpr int SORT_MAX_PASSES = 8;

@@ -24,7 +24,7 @@ constexpr int BISECT_LIMIT = 80;
 
 struct OrbitCtx {
     const double *__restrict__ r, *__restrict__ phi, *__restrict__ inv_r;
-    const float2 *__restrict__ rphif;
+    const float4 *__restrict__ rphif;
     long long N_MAX, j;
     double E, J, rj, mj, invN, cenma_m, madhoc;
     QF32 s;
@@ -87,12 +87,13 @@ static __device__ __forceinline__ void set_a_b(const OrbitCtx &o, long long k, d
         *a = -o.cenma_m * o.madhoc;
         *b = o.phi[1] + o.cenma_m * o.madhoc / o.r[1] + o.mj * o.madhoc / o.rj;
     } else {
-        const double rk = o.r[k], rk1 = o.r[k + 1];
-        const double Uk = o.phi[k] + phi_s(rk, o.rj, o.mj, o.invN);
-        const double Uk1 = o.phi[k + 1] + phi_s(rk1, o.rj, o.mj, o.invN);
-        const double den = o.inv_r[k + 1] - o.inv_r[k];
+        // the divisions by r_k and r_k+1 use the stored reciprocals (div_rcp)
+        const double rk = o.r[k], rk1 = o.r[k + 1], ik = o.inv_r[k], ik1 = o.inv_r[k + 1];
+        const double Uk = o.phi[k] + ((rk >= o.rj) ? __dmul_rn(div_rcp(o.mj, rk, ik), o.invN) : o.s.pjd);
+        const double Uk1 = o.phi[k + 1] + ((rk1 >= o.rj) ? __dmul_rn(div_rcp(o.mj, rk1, ik1), o.invN) : o.s.pjd);
+        const double den = ik1 - ik;
         *a = (Uk1 - Uk) / den;
-        *b = (Uk / rk1 - Uk1 / rk) / den;
+        *b = (div_rcp(Uk, rk1, ik1) - div_rcp(Uk1, rk, ik)) / den;
     }
 }
 
@@ -289,7 +290,7 @@ static __device__ __forceinline__ void destroy_obj(const Fields &f, long long g)
 // order of rounds changes nothing.
 struct SampleSmem {
     double rmin[ORB_T], rmax[ORB_T], F[ORB_T], E[ORB_T], J[ORB_T], rj[ORB_T], mj[ORB_T], vold2[ORB_T],
-        Uold[ORB_T];
+        Uold[ORB_T], ps[ORB_T];
     long long id[ORB_T];
     int tries[ORB_T];
     int list[2][ORB_T];
@@ -310,16 +311,31 @@ static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *s
     const double s0 = 2.0 * X - 1.0;
     const double g0 = sm.F[s] * u01(u.y);
     const double r = 0.5 * (rmin + rmax) + 0.25 * (rmax - rmin) * (3.0 * s0 - s0 * s0 * s0);
+    // one correctly rounded 1/r serves every division by r below (div_rcp)
+    const double ir = __drcp_rn(r);
     int pok = 1;
-    const double pot =
-        potential_at(f.r + off, f.phi + off, f.inv_r + off, N_MAX, r, &pok, ridx_of(C, f)) + phi_s(r, rj, mj, invN);
+    const double *rt = f.r + off, *pt = f.phi + off, *it = f.inv_r + off;
+    double pot;
+    if (r >= __ldg(rt + 1)) {
+        const long long i = potential_index(rt, N_MAX, r, ridx_of(C, f));
+        if (i > N_MAX || __ldg(rt + i) > r || __ldg(rt + i + 1) < r) {
+            pok = 0;
+            pot = 0.0;
+        } else {
+            const double pi = __ldg(pt + i), pi1 = __ldg(pt + i + 1), ii = __ldg(it + i), ii1 = __ldg(it + i + 1);
+            pot = __dadd_rn(pi, __ddiv_rn(__dmul_rn(__dsub_rn(pi1, pi), __dsub_rn(ii, ir)), __dsub_rn(ii, ii1)));
+        }
+    } else {
+        pot = potential_at(rt, pt, it, N_MAX, r, &pok);
+    }
+    pot += (r >= rj) ? __dmul_rn(div_rcp(mj, r, ir), invN) : sm.ps[s];
     if (!pok) {
         set_error(sc, CMCG_ERR_FINDZERO_R, j);
         *bad = true;
         return false;
     }
     const double drds = 0.25 * (rmax - rmin) * (3.0 - 3.0 * s0 * s0);
-    const double Q = 2.0 * E - 2.0 * pot - J * J / r / r;
+    const double Q = 2.0 * E - 2.0 * pot - div_rcp(div_rcp(J * J, r, ir), r, ir);
     double vr;
     if (Q >= 0.0) {
         vr = sqrt(Q);
@@ -338,7 +354,7 @@ static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *s
     if (u01(draw_block(C.seed, tcount, SITE_SIGN, idj, 0u).x) < 0.5) vr = -vr;
     f.rnew[g] = r;
     f.vrnew[g] = vr;
-    f.vtnew[g] = J / r;
+    f.vtnew[g] = div_rcp(J, r, ir);
     if (r > *max_rad) *max_rad = r;
     // energy_conservation2: Uoldrnew = potential(rnew) + PHI_S(rnew)
     f.ec_pre[g] = sm.vold2[s] + 2.0 * (1.0 - 0.5) * (sm.Uold[s] - pot);
@@ -356,7 +372,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
     Scalars *sc = C.sc;
     const long long off = C.off;
     const long long N_MAX = sc->N_MAX, N_NEW = sc->N_MAX_NEW;
-    const double invN = 1.0 / (double)sc->N_STAR;
+    const double invN = sc->madhoc;  // 1.0 / N_STAR, as the reference forms it (cmc_utils.c:1183)
     const double Rtidal = sc->Rtidal;
     const long long j = 1 + (long long)ct.y * ORB_T + threadIdx.x;
     const long long g = off + j;
@@ -367,7 +383,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
         const double Ej = f.E[g], Jj = f.J[g], rj = f.r[g], mj = f.m[g], phij = f.phi[g];
         const double vr0 = f.vr_rel[g], vt0 = f.vt_rel[g];
         const long long idj = f.id[g];
-        const double ps = phi_s(rj, rj, mj, invN);
+        const double ps = __dmul_rn(div_rcp(mj, rj, f.inv_r[g]), invN);  // PHI_S(r_j) (cmc.h:2175)
         const double E = Ej + ps;
         const double J = Jj;
         // energy_conservation1: vtold, vrold, Uoldrold
@@ -398,14 +414,15 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
             o.cenma_m = sc->cenma_m;
             o.madhoc = sc->madhoc;
             o.s.E = (float)E;
+            o.s.El = (float)(E - (double)o.s.E);
             o.s.J = (float)J;
             o.s.mjN = (float)(mj * invN);
-            o.s.pj = (float)((mj / rj) * invN);
+            o.s.pj = (float)ps;  // PHI_S(r_j) = (m_j / r_j) / N_STAR
             o.s.rj = rj;
             o.s.Ed = E;
             o.s.Jd = J;
             o.s.mjNd = mj * invN;
-            o.s.pjd = (mj / rj) * invN;
+            o.s.pjd = ps;
             int err = 0;
             const OrbitRs orb = calc_orbit_new(o, j, C.apsides_precision, C.apsides_max_iter, &err);
             if (err) {
@@ -418,7 +435,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
                 bool ok = true;
                 int pok = 1;
                 const double Uoldrnew =
-                    potential_at(o.r, o.phi, o.inv_r, N_MAX, rj, &pok, ridx_of(C, f)) + phi_s(rj, rj, mj, invN);
+                    potential_at(o.r, o.phi, o.inv_r, N_MAX, rj, &pok, ridx_of(C, f)) + ps;
                 ok = pok;
                 if (!ok) set_error(sc, CMCG_ERR_FINDZERO_R, j);
                 f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - Uoldrnew);
@@ -443,6 +460,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
                 sm.vold2[ts] = vold2;
                 sm.Uold[ts] = Uoldrold;
                 sm.id[ts] = idj;
+                sm.ps[ts] = ps;
                 pend = C.n_try >= 1;
                 if (!pend) set_error(sc, CMCG_ERR_NTRY, j);  // no trial allowed (cmc_evolution_thr.c:888)
             }

@@ -711,19 +711,19 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_final(const Cluster *__rest
         return;
     }
     double *r = f.r + off, *phi = f.phi + off;
-    float2 *rphif = f.rphif + off;
+    float4 *rphif = f.rphif + off;
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) {
         if (!it.valid[i]) continue;
         const long long k = it.k[i];
         const double ph_k = Pa[i];
         phi[k] = ph_k;
-        rphif[k] = make_float2((float)r[k], (float)ph_k);
+        rphif[k] = rphi_entry(r[k], ph_k);
         if (k == 1) {
             // cmc_utils.c:727
             const double p0 = __dadd_rn(ph_k, __ddiv_rn(__dmul_rn(sc->cenma_m, sc->madhoc), r[1]));
             phi[0] = p0;
-            rphif[0] = make_float2((float)r[0], (float)p0);
+            rphif[0] = rphi_entry(r[0], p0);
         }
     }
     if (ct.y == 0 && threadIdx.x == 0) {
@@ -731,7 +731,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_final(const Cluster *__rest
         phi[N + 1] = 0.0;
         f.inv_r[off + N + 1] = __drcp_rn(CMCG_SF_INFINITY);
         f.inv_r[off] = __drcp_rn(r[0]);
-        rphif[N + 1] = make_float2((float)CMCG_SF_INFINITY, 0.0f);
+        rphif[N + 1] = rphi_entry(CMCG_SF_INFINITY, 0.0);
         sc->phi_nsp[0] = ctl.nsp[0];
         sc->phi_nsp[1] = ctl.nsp[1];
         sc->phi_nsp[2] = ctl.nsp[2];
@@ -752,7 +752,7 @@ __global__ void k_phi_seq(const Cluster *__restrict__ cls, Fields f, PhiBufs ph,
     Scalars *sc = C.sc;
     const long long off = C.off;
     double *r = f.r + off, *m = f.m + off, *phi = f.phi + off, *inv_r = f.inv_r + off;
-    float2 *rphif = f.rphif + off;
+    float4 *rphif = f.rphif + off;
     long long k = 1;
     double mprev = 0.0;
     const long long NM = sc->N_MAX;
@@ -772,7 +772,7 @@ __global__ void k_phi_seq(const Cluster *__restrict__ cls, Fields f, PhiBufs ph,
     r[N + 1] = CMCG_SF_INFINITY;
     phi[N + 1] = 0.0;
     inv_r[N + 1] = __drcp_rn(CMCG_SF_INFINITY);
-    rphif[N + 1] = make_float2((float)CMCG_SF_INFINITY, 0.0f);
+    rphif[N + 1] = rphi_entry(CMCG_SF_INFINITY, 0.0);
     const double NSTAR = (double)sc->N_STAR;
     mprev = sc->Mtotal;
     for (k = N; k >= 1; --k) {
@@ -780,7 +780,7 @@ __global__ void k_phi_seq(const Cluster *__restrict__ cls, Fields f, PhiBufs ph,
         const double d = __dsub_rn(inv_r[k], inv_r[k + 1]);
         phi[k] = __dsub_rn(phi[k + 1], __dmul_rn(mprev, d));
         mprev = __dsub_rn(mprev, __ddiv_rn(m[k], NSTAR));
-        rphif[k] = make_float2((float)r[k], (float)phi[k]);
+        rphif[k] = rphi_entry(r[k], phi[k]);
         if (isnan(phi[k])) {
             set_error(sc, CMCG_ERR_NAN_PHI, k);
             return;
@@ -788,7 +788,7 @@ __global__ void k_phi_seq(const Cluster *__restrict__ cls, Fields f, PhiBufs ph,
     }
     phi[0] = __dadd_rn(phi[1], __ddiv_rn(__dmul_rn(sc->cenma_m, madhoc), r[1]));
     inv_r[0] = __drcp_rn(r[0]);
-    rphif[0] = make_float2((float)r[0], (float)phi[0]);
+    rphif[0] = rphi_entry(r[0], phi[0]);
     if (isnan(phi[0])) set_error(sc, CMCG_ERR_NAN_PHI, 0);
     sc->phi_nsp[0] = sc->phi_nsp[1] = sc->phi_nsp[2] = 0;
     sc->phi_fallback = 1;

@@ -57,10 +57,21 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     const double invN = sc->madhoc;  // 1.0 / N_STAR (cmc_utils.c:1183)
     const double m = f.m[g], ri = f.r[g], rold = f.rOld[g];
     int pok = 1;
-    const double Unewrold = potential_at(f.r + off, f.phi + off, f.inv_r + off, sc->N_MAX, rold, &pok, ridx_of(C, f)) +
-                            phi_s(rold, ri, m, invN);
+    // PHI_S (cmc.h:2175) by the stored 1/r_i, or by the 1/r_old the potential lookup forms anyway (div_rcp)
+    const double iri = f.inv_r[g];
+    const double phis_i = __dmul_rn(div_rcp(m, ri, iri), invN);
+    double Unewrold;
+    const double *rt = f.r + off, *pt = f.phi + off, *it = f.inv_r + off;
+    if (rold > 0.0 && rold >= rt[1]) {
+        const double iro = __drcp_rn(rold);
+        Unewrold = potential_in(rt, pt, it, sc->N_MAX, rold, potential_index(rt, sc->N_MAX, rold, ridx_of(C, f)), &pok,
+                                iro) +
+                   ((rold >= ri) ? __dmul_rn(div_rcp(m, rold, iro), invN) : phis_i);
+    } else {
+        Unewrold = potential_at(rt, pt, it, sc->N_MAX, rold, &pok, ridx_of(C, f)) + phi_s(rold, ri, m, invN);
+    }
     if (!pok) set_error(sc, CMCG_ERR_FINDZERO_R, i);
-    const double Unewrnew = f.phi[g] + phi_s(ri, ri, m, invN);
+    const double Unewrnew = f.phi[g] + phis_i;
     const double q = 0.5;
     const double vnew2 = f.ec_pre[g] + 2.0 * q * (Unewrold - Unewrnew);
     double vr = f.vr[g], vt = f.vt[g];

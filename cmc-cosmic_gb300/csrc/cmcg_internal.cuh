@@ -268,7 +268,7 @@ __device__ __forceinline__ long long potential_index(const double *__restrict__ 
 // The Henon interpolation of potential(r) in interval i (cmc_utils.c:147-163).
 __device__ __forceinline__ double potential_in(const double *__restrict__ r, const double *__restrict__ phi,
                                                const double *__restrict__ inv_r, long long N_MAX, double x,
-                                               long long i, int *ok)
+                                               long long i, int *ok, double ix = 0.0)
 {
     if (i > N_MAX) {  // x beyond the r = SF_INFINITY sentinel: the reference's check fails too
         *ok = 0;
@@ -282,8 +282,8 @@ __device__ __forceinline__ double potential_in(const double *__restrict__ r, con
     if (i == 0) return __ldg(phi + 1);
     const double pi = __ldg(phi + i), pi1 = __ldg(phi + i + 1);
     const double ii = __ldg(inv_r + i), ii1 = __ldg(inv_r + i + 1);
-    return __dadd_rn(pi, __ddiv_rn(__dmul_rn(__dsub_rn(pi1, pi), __dsub_rn(ii, __ddiv_rn(1.0, x))),
-                                   __dsub_rn(ii, ii1)));
+    if (ix == 0.0) ix = __drcp_rn(x);  // 1.0 / x, correctly rounded (or the caller's copy of it)
+    return __dadd_rn(pi, __ddiv_rn(__dmul_rn(__dsub_rn(pi1, pi), __dsub_rn(ii, ix)), __dsub_rn(ii, ii1)));
 }
 
 // potential(r), cmc_utils.c:112-164 with SEARCH_GRID = 0.  inv_r[k] holds the

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
         if (k >= 1) {
             mm[i] = m[k];
             const double rk = r[k];
-            q[i] = mm[i] / NSTAR;
+            q[i] = div_rcp(mm[i], NSTAR, sc->madhoc);  // m_k / N_STAR (madhoc = RN(1/N_STAR))
             inv[i] = __drcp_rn(rk);
             pb.q[off + k] = q[i];
             f.inv_r[off + k] = inv[i];

@@ -255,7 +255,9 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                 set_error(sc, CMCG_ERR_W_ZERO, k);
                 ok = false;
             }
-            const double rcm = (m[k] * r[k] + m[kp] * r[kp]) / (m[k] + m[kp]);
+            // the three quotients by m_k + m_kp share one correctly rounded reciprocal (div_rcp)
+            const double msum = mass_k + mass_kp, imsum = __drcp_rn(msum);
+            const double rcm = div_rcp(m[k] * r[k] + m[kp] * r[kp], msum, imsum);
             const double n_local = n_local_at(r, k, p, N);
             // S = 0: single-single with SS_COLLISION off, so P_enc = 0 and the
             // encounter draw (cmc_dynamics.c:406) can never succeed.
@@ -265,13 +267,16 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                 beta = (CMCG_PI / 2.0) * sqrt(dt / Trel12);
                 const double relbeta[4] = {CMCG_PI / 2.0, CMCG_PI / 4.0, CMCG_PI / 8.0, CMCG_PI / 16.0};
                 part[0] += 1.0;
+                if (beta > relbeta[3]) {  // the smallest threshold: the ratio is formed once per pair
+                    const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    if (beta > relbeta[i]) {
-                        part[1 + i] += 1.0;
-                        part[5 + i] += fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
-                        part[9 + i] += (mass_k + mass_kp) / 2.0;
-                        part[13 + i] += rcm;
+                    for (int i = 0; i < 4; ++i) {
+                        if (beta > relbeta[i]) {
+                            part[1 + i] += 1.0;
+                            part[5 + i] += qratio;
+                            part[9 + i] += (mass_k + mass_kp) / 2.0;
+                            part[13 + i] += rcm;
+                        }
                     }
                 }
                 if (beta > CMCG_PI / 2.0) beta = CMCG_PI / 2.0;
@@ -282,15 +287,16 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                         set_error(sc, CMCG_ERR_WP_ZERO, k);
                         ok = false;
                     } else {
-                        const double a1 = -w2 * W / wp, a2 = w1 * W / wp, a3 = 0.0;
-                        const double b1 = -w1 * w3 / wp, b2 = -w2 * w3 / wp, b3 = wp;
+                        const double iwp = __drcp_rn(wp);  // the four quotients by wp (div_rcp)
+                        const double a1 = div_rcp(-w2 * W, wp, iwp), a2 = div_rcp(w1 * W, wp, iwp), a3 = 0.0;
+                        const double b1 = div_rcp(-w1 * w3, wp, iwp), b2 = div_rcp(-w2 * w3, wp, iwp), b3 = wp;
                         double sb, cb, sp, cp;
                         sincos(beta, &sb, &cb);
                         sincos(psi, &sp, &cp);
                         const double wn1 = w1 * cb + a1 * sb * cp + b1 * sb * sp;
                         const double wn2 = w2 * cb + a2 * sb * cp + b2 * sb * sp;
                         const double wn3 = w3 * cb + a3 * sb * cp + b3 * sb * sp;
-                        const double fk = mass_kp / (mass_k + mass_kp), fkp = mass_k / (mass_k + mass_kp);
+                        const double fk = div_rcp(mass_kp, msum, imsum), fkp = div_rcp(mass_k, msum, imsum);
                         const double vn1 = v1 - fk * (wn1 - w1), vn2 = v2 - fk * (wn2 - w2), vn3 = v3 - fk * (wn3 - w3);
                         const double pn1 = vp1 + fkp * (wn1 - w1), pn2 = vp2 + fkp * (wn2 - w2), pn3 = vp3 + fkp * (wn3 - w3);
                         vr_k = vn3;

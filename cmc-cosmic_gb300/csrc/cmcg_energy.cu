@@ -92,11 +92,19 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
 // One block per cluster: the listed stars are put in radial order with a
 // shared-memory bitonic sort, then one thread replays the sequential
 // excess-energy pass from each of them; beyond the list's capacity the whole
-// sequential pass is replayed.
+// sequential pass is replayed.  The replay reads stars from windows of
+// FIX_WINDOW consecutive stars that the whole block stages in shared memory,
+// so it runs at shared-memory latency; the walk only moves forward and
+// changes each star once, so a staged star is never stale.
 __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__restrict__ cls, Fields f, Ec3Bufs eb,
                                                              int nclusters)
 {
-    __shared__ long long L[EXCESS_CAP];
+    __shared__ int L[EXCESS_CAP];  // star indices (below 2^31: counts_ok bounds them by the capacity)
+    __shared__ double wa[FIX_WINDOW], wm[FIX_WINDOW], wvr[FIX_WINDOW], wvt[FIX_WINDOW];
+    __shared__ long long s_i;
+    __shared__ unsigned int s_li;
+    __shared__ double s_exc;
+    __shared__ int s_done;
     const int c = blockIdx.x;
     if (c >= nclusters) return;
     const Cluster &C = cls[c];
@@ -115,7 +123,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
         unsigned int P = 1;
         while (P < n) P <<= 1;
         const long long *G = eb.list + (size_t)c * EXCESS_CAP;
-        for (unsigned int i = threadIdx.x; i < P; i += blockDim.x) L[i] = (i < n) ? G[i] : LLONG_MAX;
+        for (unsigned int i = threadIdx.x; i < P; i += blockDim.x) L[i] = (i < n) ? (int)G[i] : INT_MAX;
         __syncthreads();
         for (unsigned int k = 2; k <= P; k <<= 1) {
             for (unsigned int jj = k >> 1; jj > 0; jj >>= 1) {
@@ -123,7 +131,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
                     const unsigned int l = i ^ jj;
                     if (l > i) {
                         const bool up = (i & k) == 0;
-                        const long long a = L[i], b = L[l];
+                        const int a = L[i], b = L[l];
                         if ((a > b) == up) {
                             L[i] = b;
                             L[l] = a;
@@ -134,40 +142,79 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
             }
         }
     }
-    if (threadIdx.x != 0) return;
+    if (threadIdx.x == 0) {
+        s_exc = 0.0;
+        s_li = 0u;
+        s_i = overflow ? 1 : L[0];
+        s_done = 0;
+    }
+    __syncthreads();
     const double E_dump_factor = 0.8;
-    double Eexcess = 0.0;
-    unsigned int li = 0;
-    long long i = overflow ? 1 : L[0];
-    while (i <= N) {
-        const long long g = off + i;
-        const double ai = eb.a[g];
-        if (ai >= 0.0) {
-            Eexcess += ai;
-        } else if (Eexcess > 0) {
-            const double m = f.m[g];
-            double vr = f.vr[g], vt = f.vt[g];
-            const double v2 = sqr(vr) + sqr(vt);
-            const double E_dump_capacity = E_dump_factor * 0.5 * m * v2;
-            const double E_dump = (E_dump_capacity <= Eexcess) ? E_dump_capacity : Eexcess;
-            const double exc_ratio = sqrt((v2 - 2 * E_dump / m) / v2);
-            vr *= exc_ratio;
-            vt *= exc_ratio;
-            f.vr[g] = vr;
-            f.vt[g] = vt;
-            Eexcess -= E_dump;
+    // every window advances the walk by at least one star
+    for (long long guard = 0; guard <= N + 1; ++guard) {
+        const long long i0 = s_i;
+        if (s_done || i0 > N || i0 < 1) break;
+        for (int k = threadIdx.x; k < FIX_WINDOW; k += blockDim.x) {
+            const long long gi = i0 + k;
+            if (gi <= N) {
+                const long long g = off + gi;
+                wa[k] = eb.a[g];
+                wm[k] = f.m[g];
+                wvr[k] = f.vr[g];
+                wvt[k] = f.vt[g];
+            }
         }
-        if (overflow) {
-            ++i;
-            continue;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double Eexcess = s_exc;
+            unsigned int li = s_li;
+            long long i = i0;
+            int done = 0;
+            while (true) {
+                if (i > N) {
+                    done = 1;
+                    break;
+                }
+                if (i >= i0 + FIX_WINDOW) break;  // next window
+                const int k = (int)(i - i0);
+                const double ai = wa[k];
+                if (ai >= 0.0) {
+                    Eexcess += ai;
+                } else if (Eexcess > 0) {
+                    const double m = wm[k];
+                    double vr = wvr[k], vt = wvt[k];
+                    const double v2 = sqr(vr) + sqr(vt);
+                    const double E_dump_capacity = E_dump_factor * 0.5 * m * v2;
+                    const double E_dump = (E_dump_capacity <= Eexcess) ? E_dump_capacity : Eexcess;
+                    const double exc_ratio = sqrt((v2 - 2 * E_dump / m) / v2);
+                    vr *= exc_ratio;
+                    vt *= exc_ratio;
+                    f.vr[off + i] = vr;
+                    f.vt[off + i] = vt;
+                    Eexcess -= E_dump;
+                }
+                if (overflow) {
+                    ++i;
+                    continue;
+                }
+                if (ai >= 0.0) ++li;
+                if (Eexcess > 0) {
+                    ++i;
+                } else {
+                    if (li >= n) {
+                        done = 1;
+                        break;
+                    }
+                    i = L[li];  // the next listed star, further out (the list is sorted)
+                    if (i >= i0 + FIX_WINDOW) break;
+                }
+            }
+            s_exc = Eexcess;
+            s_li = li;
+            s_i = i;
+            s_done = done;
         }
-        if (ai >= 0.0) ++li;
-        if (Eexcess > 0) {
-            ++i;
-        } else {
-            if (li >= n) break;
-            i = L[li];
-        }
+        __syncthreads();
     }
     // on one rank the remainder is dropped (cmc_utils.c:313-348)
 }

@@ -261,7 +261,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         return CMCG_ERR_CUDA;
     }
     for (int k = 0; k < nclusters; ++k) {
-        if (capacity[k] < 1) return CMCG_ERR_ARG;
+        if (capacity[k] < 1 || capacity[k] > (1L << 31) - 64) return CMCG_ERR_ARG;  // 32-bit star indices
         if (params[k].AVEKERNEL < 1 || params[k].AVEKERNEL > PMAX) return CMCG_ERR_ARG;
         if (params[k].relax_fp32 != params[0].relax_fp32) return CMCG_ERR_ARG;
     }

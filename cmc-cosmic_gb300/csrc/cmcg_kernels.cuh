@@ -15,6 +15,7 @@ constexpr int POT_THREADS = 256, POT_ITEMS = 4, POT_T = POT_THREADS * POT_ITEMS;
 constexpr int EC3_T = 256, EN_T = 2048, EN_THREADS = 256;
 constexpr int EXCESS_CAP = 4096;      // listed unphysical predictions per cluster (else full replay)
 constexpr int EC3_FIX_THREADS = 512;
+constexpr int FIX_WINDOW = 512;       // stars staged per window of the excess-energy replay
 constexpr int SORT_MAX_PASSES = 8;
 constexpr int TIDAL_PASSES = 32;  // bound on the stripping iteration (it settles in a few)
 

@@ -51,6 +51,8 @@ struct cmcg_ctx {
     unsigned int *tickets = nullptr;
     unsigned int *gbar = nullptr;  // grid barrier of the cooperative tidal kernel
     int tidal_grid = 1;
+    PosQ pq{};
+    int posq_grid = 1;
     SortBufs sb{};
     PotBufs pb{};
     PhiBufs ph{};
@@ -201,6 +203,11 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->partials = cv.take<double>(np);
     c->tickets = cv.take<unsigned int>(c->ncl);
     c->gbar = cv.take<unsigned int>(2);
+    c->pq.slot = cv.take<int>(tot);
+    c->pq.count = cv.take<unsigned int>(1);
+    c->pq.cl = cv.take<int>(PQ_CAP);
+    c->pq.j = cv.take<long long>(PQ_CAP);
+    c->pq.res = cv.take<long long>(PQ_CAP);
     c->d_sc = cv.take<Scalars>(c->ncl);
     c->d_cls = cv.take<Cluster>(c->ncl);
     c->d_query = cv.take<double>(2);
@@ -358,6 +365,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tidal, TID_THREADS, 0));
     c->tidal_grid = std::max(1, std::min(c->t2048.ntiles, nsm * std::max(per_sm, 1)));
+    c->posq_grid = 2 * nsm;
     CK(cudaStreamSynchronize(c->stream));
     *out = c;
     return CMCG_OK;
@@ -565,9 +573,13 @@ static int L_relax(cmcg_ctx *c, double dt)
 static int L_orbit(cmcg_ctx *c)
 {
     fam_begin(c, F_ORBIT);
-    k_orbit<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials, c->tickets);
+    CK(cudaMemsetAsync(c->pq.count, 0, sizeof(unsigned int), c->stream));
+    k_orbit_pre<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->pq);
+    k_posq_scan<<<c->posq_grid, 256, 0, c->stream>>>(c->d_cls, c->f, c->pq);
+    k_orbit<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials, c->tickets,
+                                                     c->pq);
     fam_end(c);
-    c->launches += 1;
+    c->launches += 3;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 

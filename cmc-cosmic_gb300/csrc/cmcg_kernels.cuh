@@ -91,7 +91,17 @@ __global__ void k_relax64(const Cluster *cls, Tiles tm, Fields f, double *partia
                           double dt_override);
 __global__ void k_relax32(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                           double dt_override);
-__global__ void k_orbit(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets);
+// Stars whose Q(j) <= 0 and the first index with Q > 0 found for each (k_posq_scan)
+struct PosQ {
+    int *slot;            // per star: PQ_POSITIVE (Q(j) > 0), a list entry, or PQ_SCAN_HERE
+    unsigned int *count;  // list length this step
+    int *cl;              // list: cluster,
+    long long *j, *res;   //       star index, first index with Q > 0
+};
+constexpr int PQ_POSITIVE = -1, PQ_SCAN_HERE = -2, PQ_CAP = 1024;
+__global__ void k_orbit_pre(const Cluster *cls, Tiles tm, Fields f, PosQ pq);
+__global__ void k_posq_scan(const Cluster *cls, Fields f, PosQ pq);
+__global__ void k_orbit(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets, PosQ pq);
 __global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *bar, int nclusters);
 __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, double *partials,
                             unsigned int *tickets);

@@ -200,27 +200,66 @@ static __device__ double find_root_vr(const OrbitCtx &o, long long k, double pre
     return apsis;
 }
 
+// The per-star context of the orbit computation (E includes PHI_S(r_j)).
+static __device__ __forceinline__ OrbitCtx make_orbit_ctx(const Cluster &C, const Fields &f, long long j, double E,
+                                                          double J, double rj, double mj, double ps)
+{
+    const Scalars *sc = C.sc;
+    const long long off = C.off;
+    OrbitCtx o;
+    o.r = f.r + off;
+    o.phi = f.phi + off;
+    o.inv_r = f.inv_r + off;
+    o.rphif = f.rphif + off;
+    o.N_MAX = sc->N_MAX;
+    o.j = j;
+    o.E = E;
+    o.J = J;
+    o.rj = rj;
+    o.mj = mj;
+    o.invN = sc->madhoc;
+    o.cenma_m = sc->cenma_m;
+    o.madhoc = sc->madhoc;
+    o.s.E = (float)E;
+    o.s.El = (float)(E - (double)o.s.E);
+    o.s.J = (float)J;
+    o.s.mjN = (float)(mj * o.invN);
+    o.s.pj = (float)ps;  // PHI_S(r_j) = (m_j / r_j) / N_STAR
+    o.s.rj = rj;
+    o.s.Ed = E;
+    o.s.Jd = J;
+    o.s.mjNd = mj * o.invN;
+    o.s.pjd = ps;
+    return o;
+}
+
 struct OrbitRs {
     double rp, ra, dQdrp, dQdra;
     int circular;
 };
 
-// calc_orbit_new, cmc_orbit.c:413-540
-static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, double prec, long long maxit, int *err)
+// calc_orbit_new, cmc_orbit.c:413-540.  kpos is get_positive_Q_index's
+// answer (cmc_orbit.c:30-59) when already known: j when Q(j) > 0, or the
+// first index with Q > 0 found by k_posq_scan; -1 makes this thread scan.
+static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, long long kpos, double prec,
+                                         long long maxit, int *err)
 {
     OrbitRs res;
     res.circular = 1;
     res.rp = res.ra = o.rj;
     res.dQdrp = res.dQdra = 0.0;
-    // get_positive_Q_index, cmc_orbit.c:30-59
     long long ktemp = j;
-    if (fq_sign(o, ktemp) <= 0) {
-        ktemp = -1;
-        int sgn;
-        do {
-            ktemp++;
-            sgn = fq_sign(o, ktemp);
-        } while (sgn <= 0 && ktemp <= o.N_MAX);
+    if (kpos != j) {
+        if (kpos >= 0) {
+            ktemp = kpos;
+        } else {
+            ktemp = -1;
+            int sgn;
+            do {
+                ktemp++;
+                sgn = fq_sign(o, ktemp);
+            } while (sgn <= 0 && ktemp <= o.N_MAX);
+        }
         if (ktemp >= o.N_MAX) return res;
     }
     const long long kmin = find_zero_Q(o, 0, ktemp);
@@ -361,8 +400,63 @@ static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *s
     return true;
 }
 
+// Stars whose Q(j) <= 0 (a turning point: vr rounds to zero) need the first
+// table index with Q > 0, which get_positive_Q_index finds by a linear scan
+// from the centre.  k_orbit_pre marks them; k_posq_scan spreads each scan
+// over the whole grid (atomicMin of the indices with Q > 0; a thread skips
+// chunks above the minimum already found); k_orbit takes the answer.
+__global__ void __launch_bounds__(ORB_T) k_orbit_pre(const Cluster *__restrict__ cls, Tiles tm, Fields f, PosQ pq)
+{
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
+    const Scalars *sc = C.sc;
+    const long long off = C.off;
+    const long long j = 1 + (long long)ct.y * ORB_T + threadIdx.x;
+    if (j > sc->N_MAX_NEW) return;
+    const long long g = off + j;
+    const double Ej = f.E[g], rj = f.r[g], mj = f.m[g];
+    const double ps = __dmul_rn(div_rcp(mj, rj, f.inv_r[g]), sc->madhoc);
+    const double E = Ej + ps;
+    int slot = PQ_POSITIVE;
+    if (!(mj < CMCG_ZERO) && E < 0.0) {
+        const OrbitCtx o = make_orbit_ctx(C, f, j, E, f.J[g], rj, mj, ps);
+        if (fq_sign(o, j) <= 0) {
+            const unsigned int e = atomicAdd(pq.count, 1u);
+            if (e < PQ_CAP) {
+                pq.cl[e] = ct.x;
+                pq.j[e] = j;
+                pq.res[e] = sc->N_MAX + 1;  // none found: the reference's scan ends past N_MAX
+                slot = (int)e;
+            } else {
+                slot = PQ_SCAN_HERE;  // list full: k_orbit scans in the thread
+            }
+        }
+    }
+    pq.slot[g] = slot;
+}
+
+__global__ void __launch_bounds__(256) k_posq_scan(const Cluster *__restrict__ cls, Fields f, PosQ pq)
+{
+    const unsigned int n = min(*(volatile unsigned int *)pq.count, (unsigned int)PQ_CAP);
+    const long long T = (long long)gridDim.x * blockDim.x, gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (unsigned int e = 0; e < n; ++e) {
+        const Cluster &C = cls[pq.cl[e]];
+        const Scalars *sc = C.sc;
+        const long long j = pq.j[e], g = C.off + j, N_MAX = sc->N_MAX;
+        const double rj = f.r[g], mj = f.m[g];
+        const double ps = __dmul_rn(div_rcp(mj, rj, f.inv_r[g]), sc->madhoc);
+        const OrbitCtx o = make_orbit_ctx(C, f, j, f.E[g] + ps, f.J[g], rj, mj, ps);
+        for (long long base = 0; base <= N_MAX; base += T) {
+            if (*(volatile long long *)&pq.res[e] < base) break;
+            const long long k = base + gt;
+            if (k <= N_MAX && fq_sign(o, k) > 0) atomicMin(&pq.res[e], k);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                 double *partials, unsigned int *tickets)
+                                                 double *partials, unsigned int *tickets, PosQ pq)
 {
     __shared__ double red[ORB_T / 32];
     __shared__ SampleSmem sm;
@@ -399,32 +493,12 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
             acc_Et = Ej * mj / (double)sc->N_STAR;
             destroy_obj(f, g);
         } else {
-            OrbitCtx o;
-            o.r = f.r + off;
-            o.phi = f.phi + off;
-            o.inv_r = f.inv_r + off;
-            o.rphif = f.rphif + off;
-            o.N_MAX = N_MAX;
-            o.j = j;
-            o.E = E;
-            o.J = J;
-            o.rj = rj;
-            o.mj = mj;
-            o.invN = invN;
-            o.cenma_m = sc->cenma_m;
-            o.madhoc = sc->madhoc;
-            o.s.E = (float)E;
-            o.s.El = (float)(E - (double)o.s.E);
-            o.s.J = (float)J;
-            o.s.mjN = (float)(mj * invN);
-            o.s.pj = (float)ps;  // PHI_S(r_j) = (m_j / r_j) / N_STAR
-            o.s.rj = rj;
-            o.s.Ed = E;
-            o.s.Jd = J;
-            o.s.mjNd = mj * invN;
-            o.s.pjd = ps;
+            const OrbitCtx o = make_orbit_ctx(C, f, j, E, J, rj, mj, ps);
             int err = 0;
-            const OrbitRs orb = calc_orbit_new(o, j, C.apsides_precision, C.apsides_max_iter, &err);
+            // Q(j) > 0, or the index the grid-wide scan found (k_orbit_pre, k_posq_scan)
+            const int slot = pq.slot[g];
+            const long long kpos = (slot == PQ_POSITIVE) ? j : (slot >= 0 ? pq.res[slot] : -1);
+            const OrbitRs orb = calc_orbit_new(o, j, kpos, C.apsides_precision, C.apsides_max_iter, &err);
             if (err) {
                 set_error(sc, err, j);
             } else if (orb.circular) {

@@ -332,3 +332,35 @@ def test_potential_queries_through_the_radius_index(gpulib, orc, model, N, imf):
     xs += [r[0], r[-1], np.nextafter(r[-1], np.inf), 0.5 * r[0], 2.0 * r[-1]]
     for x in xs:
         assert g.potential(float(x)) == o.potential(float(x)), x
+
+
+@pytest.mark.parametrize("model,N,imf", CASES[:2])
+def test_new_orbits_when_q_is_negative_at_the_star(gpulib, orc, model, N, imf):
+    """Stars whose Q(r_j) <= 0 take get_positive_Q_index's scan from the centre
+    (cmc_orbit.c:30-59); on the GPU the scan is spread over the grid.  E is
+    lowered by vr^2 for a few stars so that Q(r_j) ~ -vr^2 < 0; the new orbits
+    must equal the oracle's."""
+    ic, o, g = _init(model, N, imf)
+    sync_state(o, g, star=[("E", "E"), ("J", "J")])
+    o.begin_step()
+    g.begin_step()
+    o.calc_timestep()
+    dt = o.scalar("Dt")
+    o.dynamics_apply(dt)
+    o.energy_conservation1()
+    vr = o.get("vr")
+    E = o.get("E").copy()
+    pick = np.argsort(-np.abs(vr))[:6]
+    E[pick] -= vr[pick] ** 2
+    o.set("E", E)
+    sync_state(o, g, star=[("vr", "vr_rel"), ("vt", "vt_rel"), ("E", "E"), ("J", "J")],
+               scalars=("Rtidal", "Mtotal"))
+    o.new_orbits_calculate()
+    g.new_orbits_calculate()
+    g.check_device("new_orbits_calculate")
+    rn_o, rn_g = o.get("rnew"), g.get("rnew")
+    assert np.array_equal(rn_o == 1e10, rn_g == 1e10)
+    keep = rn_o != 1e10
+    assert max_rel(rn_g[keep], rn_o[keep]) <= TOL_ORBIT
+    assert max_rel(g.get("r_peri")[pick], o.get("r_peri")[pick]) <= TOL_ORBIT
+    assert max_rel(g.get("r_apo")[pick], o.get("r_apo")[pick]) <= TOL_ORBIT

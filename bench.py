@@ -292,12 +292,15 @@ def run_ours(a, rank, ws, dist):
     n_start = stars()
 
     # ---- headline: device-resident steps replayed from the CUDA graph
+    e_start = [ctx.scalar("Etot", c) for c in range(ncl)]
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     time.sleep(0.6)
     ms, launches = timed(a.steps, True)
     clk = clocks.stop()
     ctx.check_device("timed steps")
+    # total energy (compute_energy_new's Etot, escaped energy included) per step
+    drift = [(ctx.scalar("Etot", c) - e0) / abs(e0) / a.steps for c, e0 in enumerate(e_start)]
     ms_max = allreduce_max(dist, ms)
     updates = allreduce_sum(dist, float(n_start * a.steps))
     value = updates / (ms_max * 1e-3)
@@ -376,6 +379,9 @@ def run_ours(a, rank, ws, dist):
                      "fp64_pipe_active": NCU_FP64_PIPE_ACTIVE.get(top),
                      "alg_bytes_per_star": ALG_BYTES[top], "ms_per_launch": ms_top / n_top,
                      "timed_in": "the profiled direct-launch pass"},
+        "energy": {"rel_drift_per_step": drift[0] if ncl == 1 else None,
+                   "max_abs_rel_drift_per_step": max(abs(d) for d in drift),
+                   "what": "(Etot after - Etot before) / |Etot before| / steps over the timed steps"},
         "kernels": per_family,
         "kernel_ms_per_step": step_ms,
         "profiled_ms_per_step": ms_prof / a.steps,

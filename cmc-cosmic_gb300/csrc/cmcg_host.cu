@@ -169,11 +169,10 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->sb.keys[1] = cv.take<unsigned long long>(tot);
     c->sb.vals[0] = cv.take<unsigned int>(tot);
     c->sb.vals[1] = cv.take<unsigned int>(tot);
-    size_t hist_total = 0;
-    for (int k = 0; k < c->ncl; ++k) hist_total += (size_t)RADIX * c->t2048.count[k];
-    c->sb.hist = cv.take<unsigned int>(hist_total);
-    c->sb.digit_total = cv.take<unsigned int>((size_t)c->ncl * RADIX);
-    c->sb.hist_off = cv.take<long long>(c->ncl);
+    c->sb.ghist = cv.take<unsigned long long>((size_t)c->ncl * SORT_MAX_PASSES * RADIX);
+    c->sb.status = cv.take<unsigned long long>((size_t)c->t2048.ntiles * RADIX);
+    c->sb.tile_next = cv.take<unsigned int>(SORT_MAX_PASSES);
+    c->sb.epoch = cv.take<unsigned int>(1);
     c->sb.npass = cv.take<int>(c->ncl);
     c->sb.kmin = cv.take<unsigned long long>(c->ncl);
     c->sb.kmax = cv.take<unsigned long long>(c->ncl);
@@ -311,14 +310,6 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
     carve_all(c, (char *)c->arena, tabs, &bytes);
     CK(cudaMemsetAsync(c->arena, 0, c->arena_bytes, c->stream));
     // cluster descriptors and tile tables
-    std::vector<long long> hist_off(nclusters);
-    long long ho = 0;
-    for (int k = 0; k < nclusters; ++k) {
-        hist_off[k] = ho;
-        ho += (long long)RADIX * c->t2048.count[k];
-    }
-    CK(cudaMemcpyAsync(c->sb.hist_off, hist_off.data(), nclusters * sizeof(long long), cudaMemcpyHostToDevice,
-                       c->stream));
     c->h_cls.resize(nclusters);
     long long rec_off = 0, ridx_off = 0;
     for (int k = 0; k < nclusters; ++k) {
@@ -624,17 +615,18 @@ static void swap_sorted(cmcg_ctx *c)
 static int L_sort(cmcg_ctx *c)
 {
     fam_begin(c, F_SORT);
+    CK(cudaMemsetAsync(c->sb.ghist, 0, (size_t)c->ncl * SORT_MAX_PASSES * RADIX * sizeof(unsigned long long),
+                       c->stream));
+    CK(cudaMemsetAsync(c->sb.tile_next, 0, SORT_MAX_PASSES * sizeof(unsigned int), c->stream));
     k_sort_prep<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb,
                                                                    c->partials, c->tickets);
-    for (int p = 0; p < SORT_MAX_PASSES; ++p) {
-        k_sort_hist<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
-        k_sort_scan<<<c->ncl * RADIX, 256, 0, c->stream>>>(c->t2048.view(), c->sb, p, c->ncl);
-        k_sort_scatter<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
-    }
+    k_sort_ghist<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb);
+    for (int p = 0; p < SORT_MAX_PASSES; ++p)
+        k_sort_onesweep<<<c->t2048.ntiles, OS_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
     k_sort_gather<<<c->t256.ntiles, GATHER_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->sb);
     k_sort_commit<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
     fam_end(c);
-    c->launches += 3 + 3 * SORT_MAX_PASSES;
+    c->launches += 4 + SORT_MAX_PASSES;
     swap_sorted(c);
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }

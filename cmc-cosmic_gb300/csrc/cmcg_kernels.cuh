@@ -10,6 +10,7 @@ constexpr int TS_T = 5120;
 constexpr int ORB_T = 128, ORB_NPART = 5;
 constexpr int TID_T = 2048, TID_THREADS = 256, TID_NPART = 4;
 constexpr int SORT_THREADS = 256, SORT_ITEMS = 8, SORT_T = SORT_THREADS * SORT_ITEMS, RADIX = 256;
+constexpr int OS_THREADS = 512;  // onesweep digit pass: 4 keys per thread, 32 warps per SM
 constexpr int GATHER_T = 256;
 constexpr int POT_THREADS = 256, POT_ITEMS = 4, POT_T = POT_THREADS * POT_ITEMS;
 constexpr int EC3_T = 256, EN_T = 2048, EN_THREADS = 256;
@@ -22,9 +23,10 @@ constexpr int TIDAL_PASSES = 32;  // bound on the stripping iteration (it settle
 struct SortBufs {
     unsigned long long *keys[2];
     unsigned int *vals[2];
-    unsigned int *hist;          // per cluster: [RADIX][ntiles_c] at hist_off[c]
-    unsigned int *digit_total;   // [nclusters][RADIX]
-    long long *hist_off;         // per cluster offset into hist
+    unsigned long long *ghist;   // per cluster: [SORT_MAX_PASSES][RADIX] digit totals
+    unsigned long long *status;  // per tile: [RADIX] look-back words (epoch | flag | count)
+    unsigned int *tile_next;     // [SORT_MAX_PASSES] tile counters, zeroed before each sort
+    unsigned int *epoch;         // sorts so far (advanced by k_sort_prep): tags the status words
     int *npass;                  // per cluster: passes needed
     unsigned long long *kmin, *kmax;
 };
@@ -105,9 +107,8 @@ __global__ void k_orbit(const Cluster *cls, Tiles tm, Fields f, double *partials
 __global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *bar, int nclusters);
 __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, double *partials,
                             unsigned int *tickets);
-__global__ void k_sort_hist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, int pass);
-__global__ void k_sort_scan(Tiles tm, SortBufs sb, int pass, int nclusters);
-__global__ void k_sort_scatter(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, int pass);
+__global__ void k_sort_ghist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
+__global__ void k_sort_onesweep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, int pass);
 __global__ void k_sort_gather(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
 __global__ void k_sort_commit(const Cluster *cls, int nclusters);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);

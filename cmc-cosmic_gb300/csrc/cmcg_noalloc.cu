@@ -34,10 +34,11 @@ constexpr size_t NA_K0 = na_align(NA_R + sizeof(double) * (NA_MAX + 2));
 constexpr size_t NA_K1 = na_align(NA_K0 + sizeof(unsigned long long) * NA_MAX);
 constexpr size_t NA_V0 = na_align(NA_K1 + sizeof(unsigned long long) * NA_MAX);
 constexpr size_t NA_V1 = na_align(NA_V0 + sizeof(unsigned int) * NA_MAX);
-constexpr size_t NA_HIST = na_align(NA_V1 + sizeof(unsigned int) * NA_MAX);
-constexpr size_t NA_DTOT = na_align(NA_HIST + sizeof(unsigned int) * RADIX * NA_TILES);
-constexpr size_t NA_MISC = na_align(NA_DTOT + sizeof(unsigned int) * RADIX);        // hist_off, npass, kmin, kmax
-constexpr size_t NA_PART = na_align(NA_MISC + 64);
+constexpr size_t NA_STATUS = na_align(NA_V1 + sizeof(unsigned int) * NA_MAX);      // look-back words
+constexpr size_t NA_GHIST = na_align(NA_STATUS + sizeof(unsigned long long) * RADIX * NA_TILES);
+constexpr size_t NA_MISC = na_align(NA_GHIST + sizeof(unsigned long long) * SORT_MAX_PASSES * RADIX);
+// NA_MISC: epoch (+0), npass (+8), kmin (+16), kmax (+24), tile counters (+32)
+constexpr size_t NA_PART = na_align(NA_MISC + 32 + sizeof(unsigned int) * SORT_MAX_PASSES);
 constexpr size_t NA_TICK = na_align(NA_PART + sizeof(double) * 3 * NA_TILES);
 constexpr size_t NA_SC = na_align(NA_TICK + sizeof(unsigned int));
 constexpr size_t NA_CL = na_align(NA_SC + sizeof(Scalars));
@@ -57,7 +58,6 @@ __global__ void k_na_setup(unsigned char *base, long long n, int ntiles)
         Scalars *sc = (Scalars *)(base + NA_SC);
         Cluster *cl = (Cluster *)(base + NA_CL);
         int *fc = (int *)(base + NA_FC);
-        long long *hist_off = (long long *)(base + NA_MISC);
         sc->N_MAX = n;
         sc->N_MAX_NEW = n;
         sc->err = 0;
@@ -67,7 +67,6 @@ __global__ void k_na_setup(unsigned char *base, long long n, int ntiles)
         cl->sc = sc;
         fc[0] = 0;
         fc[1] = ntiles;
-        hist_off[0] = 0;
         *(unsigned int *)(base + NA_TICK) = 0u;
     }
 }
@@ -126,22 +125,23 @@ extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_pe
     sb.keys[1] = (unsigned long long *)(base + NA_K1);
     sb.vals[0] = (unsigned int *)(base + NA_V0);
     sb.vals[1] = (unsigned int *)(base + NA_V1);
-    sb.hist = (unsigned int *)(base + NA_HIST);
-    sb.digit_total = (unsigned int *)(base + NA_DTOT);
-    sb.hist_off = (long long *)(base + NA_MISC);
+    sb.status = (unsigned long long *)(base + NA_STATUS);
+    sb.ghist = (unsigned long long *)(base + NA_GHIST);
+    sb.epoch = (unsigned int *)(base + NA_MISC);
     sb.npass = (int *)(base + NA_MISC + 8);
+    sb.tile_next = (unsigned int *)(base + NA_MISC + 32);
     sb.kmin = (unsigned long long *)(base + NA_MISC + 16);
     sb.kmax = (unsigned long long *)(base + NA_MISC + 24);
     const Cluster *cls = (const Cluster *)(base + NA_CL);
     Tiles tm{(const int2 *)(base + NA_TILE), (const int *)(base + NA_FC), (const int *)(base + NA_FC) + 1, ntiles};
     double *partials = (double *)(base + NA_PART);
     unsigned int *tickets = (unsigned int *)(base + NA_TICK);
+    if (cudaMemsetAsync(sb.ghist, 0, sizeof(unsigned long long) * SORT_MAX_PASSES * RADIX, s) != cudaSuccess ||
+        cudaMemsetAsync(sb.tile_next, 0, sizeof(unsigned int) * SORT_MAX_PASSES, s) != cudaSuccess)
+        return CMCG_ERR_CUDA;
     k_sort_prep<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, partials, tickets);
-    for (int p = 0; p < SORT_MAX_PASSES; ++p) {
-        k_sort_hist<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, p);
-        k_sort_scan<<<RADIX, 256, 0, s>>>(tm, sb, p, 1);
-        k_sort_scatter<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, p);
-    }
+    k_sort_ghist<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb);
+    for (int p = 0; p < SORT_MAX_PASSES; ++p) k_sort_onesweep<<<ntiles, OS_THREADS, 0, s>>>(cls, tm, f, sb, p);
     k_na_perm<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(base, n, d_perm);
     if (cudaGetLastError() != cudaSuccess) return CMCG_ERR_CUDA;
     if (n_bound) {

@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__rest
                                                             PhiBufs ph, int nclusters)
 {
     __shared__ double s_a[POT_THREADS][4];
+    __shared__ double s_tot[4];
     const int c = blockIdx.x;
     if (c >= nclusters) return;
     const Cluster &C = cls[c];
@@ -176,20 +177,57 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__rest
     s_a[t][3] = sm;
     bad = __syncthreads_or(bad);
     PhiCtl &ctl = ph.ctl[c];
-    if (t == 0) {
-        // exclusive scan of the chunk aggregates
-        double eq = 0.0, eD = 0.0, eC = 0.0, em = 0.0;
-        for (int i = 0; i < POT_THREADS; ++i) {
-            const double aq = s_a[i][0], aD = s_a[i][1], aC = s_a[i][2], am = s_a[i][3];
-            s_a[i][0] = eq;
-            s_a[i][1] = eD;
-            s_a[i][2] = eC;
-            s_a[i][3] = em;
-            eC = eC + aC + eq * aD;
-            eq += aq;
-            eD += aD;
-            em += am;
+    // exclusive scan of the chunk aggregates over threads: the triple combine
+    // (outer A, inner B) -> (q_A + q_B, D_A + D_B, C_A + C_B + q_A D_B) is
+    // associative, so a warp-shuffle scan and a pass over the warp totals do it
+    {
+        const int lane = t & 31, wid = t >> 5;
+        double xq = q, xD = D, xC = Cc, xm = sm;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double yq = __shfl_up_sync(0xffffffffu, xq, o), yD = __shfl_up_sync(0xffffffffu, xD, o);
+            const double yC = __shfl_up_sync(0xffffffffu, xC, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
+            if (lane >= o) {
+                xC = yC + xC + yq * xD;
+                xq = yq + xq;
+                xD = yD + xD;
+                xm = ym + xm;
+            }
         }
+        __shared__ double s_wt[POT_THREADS / 32][4];
+        if (lane == 31) {
+            s_wt[wid][0] = xq;
+            s_wt[wid][1] = xD;
+            s_wt[wid][2] = xC;
+            s_wt[wid][3] = xm;
+        }
+        __syncthreads();
+        double pq = 0.0, pD = 0.0, pC = 0.0, pm = 0.0;  // warps before this one
+        for (int u = 0; u < wid; ++u) {
+            pC = pC + s_wt[u][2] + pq * s_wt[u][1];
+            pq += s_wt[u][0];
+            pD += s_wt[u][1];
+            pm += s_wt[u][3];
+        }
+        // exclusive: the earlier warps, then the lanes before this one (previous lane's inclusive)
+        double eq_ = __shfl_up_sync(0xffffffffu, xq, 1), eD_ = __shfl_up_sync(0xffffffffu, xD, 1);
+        double eC_ = __shfl_up_sync(0xffffffffu, xC, 1), em_ = __shfl_up_sync(0xffffffffu, xm, 1);
+        if (lane == 0) eq_ = eD_ = eC_ = em_ = 0.0;
+        __syncthreads();
+        s_a[t][0] = pq + eq_;
+        s_a[t][1] = pD + eD_;
+        s_a[t][2] = pC + eC_ + pq * eD_;
+        s_a[t][3] = pm + em_;
+        if (t == POT_THREADS - 1) {
+            s_tot[0] = pq + xq;
+            s_tot[1] = pD + xD;
+            s_tot[2] = pC + xC + pq * xD;
+            s_tot[3] = pm + xm;
+        }
+    }
+    __syncthreads();
+    if (t == 0) {
+        const double eq = s_tot[0], eD = s_tot[1], em = s_tot[3];
         const double u = 0x1p-53, n = (double)N;
         const double G = ((double)ntiles + 4096.0) * 0x1p-52;
         const double madhoc = sc->madhoc, cm = __dmul_rn(sc->cenma_m, madhoc);

@@ -7,12 +7,12 @@
 // vt = vtnew, rOld = old r).
 //
 // Keys are the IEEE bit patterns of rnew (positive doubles order like their
-// bits), values the star's slot.  Each pass handles one 8-bit digit:
-//   k_sort_hist    per-tile digit counts, stored digit-major per cluster
-//   k_sort_scan    per (cluster, digit) exclusive scan over tiles
-//   k_sort_scatter stable in-tile ranking (warp match + per-warp counters),
-//                  staged through shared memory so runs of one digit leave
-//                  the block as contiguous stores
+// bits), values the star's slot.
+//   k_sort_ghist     every 8-bit digit's histogram in one read of the keys
+//   k_sort_onesweep  one kernel per digit pass: stable in-tile ranking (warp
+//                    match + per-warp counters), tile offsets by decoupled
+//                    look-back, staging through shared memory so runs of one
+//                    digit leave the block as contiguous stores
 // Tiles never straddle clusters, so one launch sorts every cluster of an
 // ensemble independently.  Passes whose digit is identical for every key of a
 // cluster (found from the key range) are skipped for that cluster.
@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
     const unsigned long long inf_bits = (unsigned long long)__double_as_longlong(CMCG_SF_INFINITY);
     unsigned long long kmn = ~0ull, kmx = 0ull;
     long long cnt = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(sb.epoch, 1u);  // this sort's look-back epoch
     const long long base = 1 + (long long)ct.y * SORT_T;
     for (int i = threadIdx.x; i < SORT_T; i += SORT_THREADS) {
         const long long k = base + i;
@@ -63,6 +64,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
         s_cnt[w] = cnt;
     }
     __syncthreads();
+    __shared__ int s_last;
     if (threadIdx.x == 0) {
         for (int q = 1; q < SORT_THREADS / 32; ++q) {
             kmn = min(kmn, s_min[q]);
@@ -73,15 +75,36 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
         slot[0] = __longlong_as_double((long long)kmn);
         slot[1] = __longlong_as_double((long long)kmx);
         slot[2] = (double)cnt;
-        if (arrive_last(tickets + ct.x, tm.count[ct.x])) {
-            unsigned long long a = ~0ull, b = 0ull;
-            long long n = 0;
-            const int b0 = tm.first[ct.x];
-            for (int q = 0; q < tm.count[ct.x]; ++q) {
-                const double *s = partials + (size_t)(b0 + q) * 3;
-                a = min(a, (unsigned long long)__double_as_longlong(s[0]));
-                b = max(b, (unsigned long long)__double_as_longlong(s[1]));
-                n += (long long)s[2];
+    }
+    if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
+        // every thread folds a strided share of the tiles (loads bypass L1), then the warps combine
+        unsigned long long a = ~0ull, b = 0ull;
+        long long n = 0;
+        const int b0 = tm.first[ct.x], nt = tm.count[ct.x];
+        for (int q = threadIdx.x; q < nt; q += SORT_THREADS) {
+            const double *sp = partials + (size_t)(b0 + q) * 3;
+            a = min(a, (unsigned long long)__double_as_longlong(__ldcg(sp)));
+            b = max(b, (unsigned long long)__double_as_longlong(__ldcg(sp + 1)));
+            n += (long long)__ldcg(sp + 2);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a = min(a, __shfl_down_sync(0xffffffffu, a, o));
+            b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+            n += __shfl_down_sync(0xffffffffu, n, o);
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) {
+            s_min[w] = a;
+            s_max[w] = b;
+            s_cnt[w] = n;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int q = 1; q < SORT_THREADS / 32; ++q) {
+                a = min(a, s_min[q]);
+                b = max(b, s_max[q]);
+                n += s_cnt[q];
             }
             sc->n_bound = n;
             // escapers sort after every bound star: the key range must include them
@@ -105,80 +128,74 @@ static __device__ __forceinline__ unsigned long long load_key(const Cluster &C, 
     return (cur ? sb.keys[1] : sb.keys[0])[C.off + pos];
 }
 
-__global__ void __launch_bounds__(SORT_THREADS) k_sort_hist(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                            SortBufs sb, int pass)
+// All digit histograms of the cluster's keys in one read (they do not depend
+// on the order the passes put the keys in): per-block shared counters, then
+// one global add per (pass, digit).
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_ghist(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                             SortBufs sb)
 {
-    __shared__ unsigned int h[SORT_THREADS / 32][RADIX];
+    __shared__ unsigned int h[SORT_MAX_PASSES][RADIX];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
-    if (pass >= sb.npass[ct.x]) return;
+    const int np = sb.npass[ct.x];
+    if (np == 0) return;
     const long long N = C.sc->N_MAX_NEW;
-    const int w = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < (SORT_THREADS / 32) * RADIX; i += SORT_THREADS) (&h[0][0])[i] = 0u;
+    for (int i = threadIdx.x; i < SORT_MAX_PASSES * RADIX; i += SORT_THREADS) (&h[0][0])[i] = 0u;
     __syncthreads();
-    const int cur = pass & 1;
     const long long base = (long long)ct.y * SORT_T;
-    const int shift = 8 * pass;
     for (int i = threadIdx.x; i < SORT_T; i += SORT_THREADS) {
         const long long pos = base + i;
         if (pos >= N) break;
-        const unsigned int d = (unsigned int)(load_key(C, f, sb, pass, cur, pos) >> shift) & (RADIX - 1);
-        atomicAdd(&h[w][d], 1u);
+        const unsigned long long k = (unsigned long long)__double_as_longlong(f.rnew[C.off + 1 + pos]);
+        for (int p = 0; p < np; ++p) atomicAdd(&h[p][(unsigned int)(k >> (8 * p)) & (RADIX - 1)], 1u);
     }
     __syncthreads();
-    const int ntiles = tm.count[ct.x];
-    for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) {
-        unsigned int s = 0;
-        for (int q = 0; q < SORT_THREADS / 32; ++q) s += h[q][d];
-        sb.hist[sb.hist_off[ct.x] + (long long)d * ntiles + ct.y] = s;
+    unsigned long long *g = sb.ghist + (size_t)ct.x * SORT_MAX_PASSES * RADIX;
+    for (int i = threadIdx.x; i < np * RADIX; i += SORT_THREADS) {
+        const unsigned int v = (&h[0][0])[i];
+        if (v) atomicAdd(g + i, (unsigned long long)v);
     }
 }
 
-// One block per (cluster, digit): exclusive scan over the cluster's tiles.
-__global__ void __launch_bounds__(256) k_sort_scan(Tiles tm, SortBufs sb, int pass, int nclusters)
+// Tile status word of the decoupled look-back: the pass's epoch (sort count x 8
+// + pass) in the top 30 bits, a flag (1 = this tile's count, 2 = inclusive
+// prefix through this tile) in the next two, the count below.  Words of
+// earlier passes and sorts carry another epoch and read as not ready, so the
+// words are never cleared (graph replays included).
+constexpr unsigned long long ST_AGG = 1ull << 32, ST_INC = 2ull << 32, ST_VAL = 0xffffffffull;
+__device__ __forceinline__ unsigned long long st_tag(unsigned int epoch, int pass)
 {
-    __shared__ unsigned int s_warp[8];
-    __shared__ unsigned int s_carry;
-    const int c = blockIdx.x / RADIX, d = blockIdx.x % RADIX;
-    if (c >= nclusters || pass >= sb.npass[c]) return;
-    const int ntiles = tm.count[c];
-    unsigned int *h = sb.hist + sb.hist_off[c] + (long long)d * ntiles;
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
-    for (int base = 0; base < ntiles; base += 256) {
-        const int t = base + threadIdx.x;
-        const unsigned int v = (t < ntiles) ? h[t] : 0u;
-        unsigned int x = v;
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) s_warp[wid] = x;
-        __syncthreads();
-        unsigned int wb = 0;
-        for (int q = 0; q < wid; ++q) wb += s_warp[q];
-        const unsigned int carry = s_carry;
-        if (t < ntiles) h[t] = carry + wb + x - v;  // exclusive
-        __syncthreads();
-        if (threadIdx.x == 255) s_carry = carry + wb + x;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) sb.digit_total[c * RADIX + d] = s_carry;
+    return ((unsigned long long)((epoch * SORT_MAX_PASSES + (unsigned)pass) & 0x3fffffffu)) << 34;
 }
 
-__global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                               SortBufs sb, int pass)
+// One digit pass (onesweep): tiles take their order from an atomic counter,
+// rank their keys stably in shared memory, publish per-digit counts and
+// obtain the counts of the tiles before them in the cluster by decoupled
+// look-back (Merrill & Garland's single-pass scan, as in Adinets & Merrill's
+// onesweep radix sort), then write their keys in runs of one digit.  A tile
+// only waits on tiles that took a smaller index, which have started; every
+// wait is bounded and records CMCG_ERR_SPIN if it gives up.
+__global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                              SortBufs sb, int pass)
 {
-    __shared__ unsigned int wcnt[SORT_THREADS / 32][RADIX];  // per-warp digit counters -> prefixes
-    __shared__ unsigned int dstart[RADIX];                     // in-tile digit start
-    __shared__ unsigned int gbase[RADIX];                      // global digit start for this tile
+    constexpr int NWARP = OS_THREADS / 32, ITEMS = SORT_T / OS_THREADS;
+    __shared__ unsigned int wcnt[NWARP][RADIX];  // per-warp digit counters -> prefixes
+    __shared__ unsigned int dcnt[RADIX];         // the tile's count per digit
+    __shared__ unsigned int dstart[RADIX];       // in-tile digit start
+    __shared__ unsigned long long gbase[RADIX];  // global digit start for this tile
     __shared__ unsigned long long sk[SORT_T];
     __shared__ unsigned int sv[SORT_T];
-    const int2 ct = tm.tiles[blockIdx.x];
+    __shared__ unsigned int s_w[RADIX / 32];
+    __shared__ unsigned long long s_t[RADIX / 32];
+    __shared__ int s_b;
+    if (threadIdx.x == 0) s_b = (int)atomicAdd(sb.tile_next + pass, 1u);
+    __syncthreads();
+    const int b = s_b;
+    if (b >= tm.ntiles) return;
+    const int2 ct = tm.tiles[b];
     const Cluster &C = cls[ct.x];
+    // every tile of a cluster takes the same early exit, so no tile waits on one that left
     if (!counts_ok(C)) return;
     if (pass >= sb.npass[ct.x]) return;
     const long long N = C.sc->N_MAX_NEW;
@@ -186,90 +203,111 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const Cluster *__
     const int cur = pass & 1, nxt = cur ^ 1;
     const int shift = 8 * pass;
     const long long base = (long long)ct.y * SORT_T;
-    for (int i = threadIdx.x; i < (SORT_THREADS / 32) * RADIX; i += SORT_THREADS) (&wcnt[0][0])[i] = 0u;
+    for (int i = threadIdx.x; i < NWARP * RADIX; i += OS_THREADS) (&wcnt[0][0])[i] = 0u;
     __syncthreads();
 
-    unsigned long long key[SORT_ITEMS];
-    unsigned int val[SORT_ITEMS], dig[SORT_ITEMS], rank[SORT_ITEMS];
-    bool valid[SORT_ITEMS];
+    unsigned long long key[ITEMS];
+    unsigned int val[ITEMS], dig[ITEMS], rank[ITEMS];
+    bool valid[ITEMS];
 #pragma unroll
-    for (int it = 0; it < SORT_ITEMS; ++it) {
-        // warp-striped: warp w owns [w*256, w*256+256), item it, lane l -> w*256 + it*32 + l
-        const long long pos = base + w * (SORT_ITEMS * 32) + it * 32 + lane;
+    for (int it = 0; it < ITEMS; ++it) {
+        // warp-striped: warp w owns [w*ITEMS*32, (w+1)*ITEMS*32), item it, lane l -> w*ITEMS*32 + it*32 + l
+        const long long pos = base + w * (ITEMS * 32) + it * 32 + lane;
         valid[it] = pos < N;
         key[it] = valid[it] ? load_key(C, f, sb, pass, cur, pos) : 0ull;
         val[it] = valid[it] ? (pass == 0 ? (unsigned int)pos : (cur ? sb.vals[1] : sb.vals[0])[C.off + pos]) : 0u;
         dig[it] = (unsigned int)(key[it] >> shift) & (RADIX - 1);
     }
 #pragma unroll
-    for (int it = 0; it < SORT_ITEMS; ++it) {
+    for (int it = 0; it < ITEMS; ++it) {
         const unsigned int tag = valid[it] ? dig[it] : (0x10000u + lane);
         const unsigned int peers = __match_any_sync(0xffffffffu, tag);
         const unsigned int below = peers & ((1u << lane) - 1u);
-        unsigned int b = 0;
-        if (valid[it]) b = wcnt[w][dig[it]];
+        unsigned int bb = 0;
+        if (valid[it]) bb = wcnt[w][dig[it]];
         __syncwarp();
-        if (valid[it] && below == 0u) wcnt[w][dig[it]] = b + __popc(peers);
+        if (valid[it] && below == 0u) wcnt[w][dig[it]] = bb + __popc(peers);
         __syncwarp();
-        rank[it] = b + __popc(below);
+        rank[it] = bb + __popc(below);
     }
     __syncthreads();
-    // per digit: exclusive prefix over warps, tile total
-    for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) {
-        unsigned int s = 0;
-        for (int q = 0; q < SORT_THREADS / 32; ++q) {
+    // threads 0..RADIX-1 own one digit each: prefix over warps, publish, look back
+    const int d = threadIdx.x;
+    unsigned long long prefix = 0, tot = 0;
+    unsigned int cnt = 0;
+    if (d < RADIX) {
+        for (int q = 0; q < NWARP; ++q) {
             const unsigned int t = wcnt[q][d];
-            wcnt[q][d] = s;
-            s += t;
+            wcnt[q][d] = cnt;
+            cnt += t;
         }
-        dstart[d] = s;  // tile count for now
+        dcnt[d] = cnt;
+        const unsigned long long tag = st_tag(*(volatile unsigned int *)sb.epoch, pass);
+        unsigned long long *st = sb.status + (size_t)b * RADIX;
+        atomicExch(st + d, tag | (ct.y == 0 ? ST_INC : ST_AGG) | cnt);
+        if (ct.y > 0) {
+            int j = b - 1;
+            long long spins = 0;
+            while (true) {
+                const unsigned long long v = *(volatile unsigned long long *)(sb.status + (size_t)j * RADIX + d);
+                if ((v & ~(ST_INC | ST_AGG | ST_VAL)) == tag) {
+                    if (v & ST_INC) {
+                        prefix += v & ST_VAL;
+                        break;
+                    }
+                    if (v & ST_AGG) {
+                        prefix += v & ST_VAL;
+                        --j;  // tile j is not the cluster's first (that one publishes inclusive)
+                        continue;
+                    }
+                }
+                if (++spins > CMCG_SPIN_LIMIT) {
+                    set_error(C.sc, CMCG_ERR_SPIN, j);
+                    break;
+                }
+            }
+            atomicExch(st + d, tag | ST_INC | (prefix + cnt));
+        }
+        tot = sb.ghist[((size_t)ct.x * SORT_MAX_PASSES + pass) * RADIX + d];
+    }
+    // exclusive scans over digits (warps 0..RADIX/32-1 are the digit owners):
+    // the tile's counts -> in-tile digit starts; the cluster's totals -> global starts
+    unsigned int x = cnt;
+    unsigned long long tx = tot;
+    if (d < RADIX) {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+            const unsigned long long ty = __shfl_up_sync(0xffffffffu, tx, o);
+            if (lane >= o) {
+                x += y;
+                tx += ty;
+            }
+        }
+        if (lane == 31) {
+            s_w[w] = x;
+            s_t[w] = tx;
+        }
     }
     __syncthreads();
-    // exclusive scan of the tile counts over digits (256 threads, one digit each)
-    {
-        const int d = threadIdx.x;
-        const unsigned int v = dstart[d];
-        unsigned int x = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        __shared__ unsigned int s_w[SORT_THREADS / 32];
-        if (lane == 31) s_w[w] = x;
-        // global base of digit d for this tile: digits below d in the cluster + tiles before
-        const int ntiles = tm.count[ct.x];
-        unsigned int dbelow = 0;
-        const unsigned int *tot = sb.digit_total + ct.x * RADIX;
-        // exclusive prefix of the cluster's digit totals
-        unsigned int tv = tot[d], tx = tv;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned int y = __shfl_up_sync(0xffffffffu, tx, o);
-            if (lane >= o) tx += y;
-        }
-        __shared__ unsigned int s_t[SORT_THREADS / 32];
-        if (lane == 31) s_t[w] = tx;
-        __syncthreads();
-        unsigned int wb = 0, tb = 0;
+    if (d < RADIX) {
+        unsigned int wb = 0;
+        unsigned long long tb = 0;
         for (int q = 0; q < w; ++q) {
             wb += s_w[q];
             tb += s_t[q];
         }
-        dbelow = tb + tx - tv;
-        const unsigned int excl = wb + x - v;
-        __syncthreads();
-        dstart[d] = excl;
-        gbase[d] = dbelow + sb.hist[sb.hist_off[ct.x] + (long long)d * ntiles + ct.y];
+        dstart[d] = wb + x - cnt;
+        gbase[d] = tb + tx - tot + prefix;
     }
     __syncthreads();
     // stage in shared memory in (digit, stable rank) order
 #pragma unroll
-    for (int it = 0; it < SORT_ITEMS; ++it) {
+    for (int it = 0; it < ITEMS; ++it) {
         if (valid[it]) {
-            const unsigned int p = dstart[dig[it]] + wcnt[w][dig[it]] + rank[it];
-            sk[p] = key[it];
-            sv[p] = val[it];
+            const unsigned int pidx = dstart[dig[it]] + wcnt[w][dig[it]] + rank[it];
+            sk[pidx] = key[it];
+            sv[pidx] = val[it];
         }
     }
     __syncthreads();
@@ -277,10 +315,10 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const Cluster *__
     if (nt > SORT_T) nt = SORT_T;
     unsigned long long *kout = nxt ? sb.keys[1] : sb.keys[0];
     unsigned int *vout = nxt ? sb.vals[1] : sb.vals[0];
-    for (int i = threadIdx.x; i < nt; i += SORT_THREADS) {
+    for (int i = threadIdx.x; i < nt; i += OS_THREADS) {
         const unsigned long long k = sk[i];
-        const unsigned int d = (unsigned int)(k >> shift) & (RADIX - 1);
-        const long long dst = (long long)gbase[d] + (i - (long long)dstart[d]);
+        const unsigned int dd = (unsigned int)(k >> shift) & (RADIX - 1);
+        const long long dst = (long long)gbase[dd] + (i - (long long)dstart[dd]);
         if (dst < 0 || dst >= N) {  // inconsistent counts: record, never write out of range
             set_error(C.sc, CMCG_ERR_SPIN, dst);
             continue;

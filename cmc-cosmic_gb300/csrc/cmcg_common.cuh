@@ -45,6 +45,50 @@ __device__ __forceinline__ double block_max(double v, double *smem)
     return s;
 }
 
+// K sums over the block in one pass, valid in thread 0's v[].  Each warp
+// reduces a column by shuffles only when one of its lanes holds a nonzero
+// value (a column that is zero over the warp contributes exactly 0), then
+// thread 0 adds the warps in a fixed order: the same tree as block_sum, with
+// two barriers for all K columns instead of two per column.
+template <int NT, int K>
+__device__ __forceinline__ void block_sums(double (&v)[K], double (*smem)[K] /* [NT/32][K], not shared with others */)
+{
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        double x = v[i];
+        if (__any_sync(0xffffffffu, x != 0.0)) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x = __dadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
+        }
+        if (l == 0) smem[w][i] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+            double s = 0.0;
+            for (int q = 0; q < NT / 32; ++q) s = __dadd_rn(s, smem[q][i]);
+            v[i] = s;
+        }
+    }
+}
+
+// Maximum of non-negative doubles (valid in thread 0), compared as their bit
+// patterns, which order like the values: integer instructions only.
+template <int NT>
+__device__ __forceinline__ double block_max_nonneg(double v, long long *smem /* >= NT/32, not shared */)
+{
+    long long b = __double_as_longlong(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+    if ((threadIdx.x & 31) == 0) smem[threadIdx.x >> 5] = b;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int i = 1; i < NT / 32; ++i) b = max(b, smem[i]);
+    return __longlong_as_double(b);
+}
+
 template <int NT>
 __device__ __forceinline__ long long block_sum_ll(long long v, long long *smem)
 {

@@ -323,29 +323,39 @@ static __device__ __forceinline__ void destroy_obj(const Fields &f, long long g)
 }
 
 // Stars of a block that still sample their position (get_positions_loop's
-// rejection loop, cmc_evolution_thr.c:855-926).  Each round packs the pending
-// stars onto the first threads, so warps are full or idle whatever the spread
-// of trial counts; a star's trials use draws keyed by (star id, trial), so the
-// order of rounds changes nothing.
+// rejection loop, cmc_evolution_thr.c:855-926).  A star's trial k uses draws
+// keyed by (star id, k), so its trials are independent of one another and of
+// the order they run in.  Each round gives every pending star m = ORB_T / n
+// threads (n pending stars), which evaluate its next m trials at once; the
+// first trial that decides (accepted, or an error the reference would stop
+// at) is the one the reference's sequential loop stops at, and only it
+// writes.  Rounds stay full of threads and their number falls from the
+// longest trial sequence of the block to about log of it.
 struct SampleSmem {
     double rmin[ORB_T], rmax[ORB_T], F[ORB_T], E[ORB_T], J[ORB_T], rj[ORB_T], mj[ORB_T], vold2[ORB_T],
         Uold[ORB_T], ps[ORB_T];
     long long id[ORB_T];
-    int tries[ORB_T];
+    int next[ORB_T];   // the star's next trial number (1-based)
+    int first[ORB_T];  // the first deciding trial of this round (INT_MAX: none)
     int list[2][ORB_T];
     int n[2];
 };
 
-// One trial of star slot s: returns true when it is accepted (outputs written).
-static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *sc, const Fields &f, SampleSmem &sm,
-                                                    int s, long long k, long long j0, double invN, double *max_rad,
-                                                    bool *bad)
+constexpr int TRIAL_REJECT = 0, TRIAL_ACCEPT = 1;  // anything else is a device status code
+
+struct Trial {
+    double X, r, ir, vr, pot;
+    int code;
+};
+
+// Trial k of star slot s, evaluated without writing anything.
+static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                   const SampleSmem &sm, int s, int k, double invN)
 {
+    Trial t;
     const long long off = C.off, N_MAX = sc->N_MAX;
     const double rmin = sm.rmin[s], rmax = sm.rmax[s], E = sm.E[s], J = sm.J[s], rj = sm.rj[s], mj = sm.mj[s];
-    const long long idj = sm.id[s], j = j0 + s, g = off + j;
-    const long long tcount = sc->tcount;
-    const uint4 u = draw_block(C.seed, tcount, SITE_TRIAL, idj, (unsigned int)(k - 1));
+    const uint4 u = draw_block(C.seed, sc->tcount, SITE_TRIAL, sm.id[s], (unsigned int)(k - 1));
     const double X = u01(u.x);
     const double s0 = 2.0 * X - 1.0;
     const double g0 = sm.F[s] * u01(u.y);
@@ -368,10 +378,14 @@ static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *s
         pot = potential_at(rt, pt, it, N_MAX, r, &pok);
     }
     pot += (r >= rj) ? __dmul_rn(div_rcp(mj, r, ir), invN) : sm.ps[s];
+    t.X = X;
+    t.r = r;
+    t.ir = ir;
+    t.pot = pot;
+    t.vr = 0.0;
     if (!pok) {
-        set_error(sc, CMCG_ERR_FINDZERO_R, j);
-        *bad = true;
-        return false;
+        t.code = CMCG_ERR_FINDZERO_R;
+        return t;
     }
     const double drds = 0.25 * (rmax - rmin) * (3.0 - 3.0 * s0 * s0);
     const double Q = 2.0 * E - 2.0 * pot - div_rcp(div_rcp(J * J, r, ir), r, ir);
@@ -380,24 +394,32 @@ static __device__ __forceinline__ bool sample_trial(const Cluster &C, Scalars *s
         vr = sqrt(Q);
     } else {
         if (isnan(Q)) {
-            set_error(sc, CMCG_ERR_Q_NAN, j);
-            *bad = true;
-            return false;
+            t.code = CMCG_ERR_Q_NAN;
+            return t;
         }
         vr = 0;
     }
-    if (!(g0 < 1.0 / vr * drds)) return false;
-    f.X[g] = X;
-    f.r_peri[g] = rmin;
-    f.r_apo[g] = rmax;
-    if (u01(draw_block(C.seed, tcount, SITE_SIGN, idj, 0u).x) < 0.5) vr = -vr;
-    f.rnew[g] = r;
+    t.vr = vr;
+    t.code = (g0 < 1.0 / vr * drds) ? TRIAL_ACCEPT : TRIAL_REJECT;
+    return t;
+}
+
+// The accepted trial's outputs (cmc_evolution_thr.c:918-935).
+static __device__ __forceinline__ void commit_trial(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                    const SampleSmem &sm, int s, long long g, const Trial &t,
+                                                    double *max_rad)
+{
+    f.X[g] = t.X;
+    f.r_peri[g] = sm.rmin[s];
+    f.r_apo[g] = sm.rmax[s];
+    double vr = t.vr;
+    if (u01(draw_block(C.seed, sc->tcount, SITE_SIGN, sm.id[s], 0u).x) < 0.5) vr = -vr;
+    f.rnew[g] = t.r;
     f.vrnew[g] = vr;
-    f.vtnew[g] = div_rcp(J, r, ir);
-    if (r > *max_rad) *max_rad = r;
+    f.vtnew[g] = div_rcp(sm.J[s], t.r, t.ir);
+    if (t.r > *max_rad) *max_rad = t.r;
     // energy_conservation2: Uoldrnew = potential(rnew) + PHI_S(rnew)
-    f.ec_pre[g] = sm.vold2[s] + 2.0 * (1.0 - 0.5) * (sm.Uold[s] - pot);
-    return true;
+    f.ec_pre[g] = sm.vold2[s] + 2.0 * (1.0 - 0.5) * (sm.Uold[s] - t.pot);
 }
 
 // Stars whose Q(j) <= 0 (a turning point: vr rounds to zero) need the first
@@ -455,7 +477,9 @@ __global__ void __launch_bounds__(256) k_posq_scan(const Cluster *__restrict__ c
     }
 }
 
-__global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+// Five blocks per SM (at most 102 registers a thread; a few bytes spill) keep
+// more warps on the FP64 pipe than the four that 116 registers allow.
+__global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                  double *partials, unsigned int *tickets, PosQ pq)
 {
     __shared__ double red[ORB_T / 32];
@@ -547,23 +571,42 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
     if (pend) {
         const int p = atomicAdd(&sm.n[0], 1);
         sm.list[0][p] = t;
-        sm.tries[t] = 0;
+        sm.next[t] = 1;
+        sm.first[t] = INT_MAX;
     }
     __syncthreads();
     const long long j0 = 1 + (long long)ct.y * ORB_T;
+    const long long n_try = C.n_try;
     for (int cur = 0;; cur ^= 1) {
         const int n = sm.n[cur];
         if (n == 0) break;
+        const int m = ORB_T / n;  // trials per pending star this round
         if (t == 0) sm.n[cur ^ 1] = 0;  // last read at the top of the previous round
+        int slot = -1, k = 0, kb = 0;
+        Trial tr;
+        tr.code = TRIAL_REJECT;
+        if (t < n * m) {
+            slot = sm.list[cur][t / m];
+            kb = sm.next[slot];
+            k = kb + t % m;
+            if (k <= n_try) {
+                tr = eval_trial(C, sc, f, sm, slot, k, invN);
+                if (tr.code != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
+            }
+        }
         __syncthreads();
-        if (t < n) {
-            const int slot = sm.list[cur][t];
-            const long long k = ++sm.tries[slot];
-            bool bad = false;
-            if (!sample_trial(C, sc, f, sm, slot, k, j0, invN, &max_rad, &bad) && !bad) {
-                if (k >= C.n_try) {
-                    set_error(sc, CMCG_ERR_NTRY, j0 + slot);
+        if (slot >= 0) {
+            const int fst = sm.first[slot];
+            if (k == fst) {
+                if (tr.code == TRIAL_ACCEPT)
+                    commit_trial(C, sc, f, sm, slot, off + j0 + slot, tr, &max_rad);
+                else
+                    set_error(sc, tr.code, j0 + slot);
+            } else if (t % m == 0 && fst == INT_MAX) {
+                if (kb + m - 1 >= n_try) {
+                    set_error(sc, CMCG_ERR_NTRY, j0 + slot);  // n_try trials, none accepted
                 } else {
+                    sm.next[slot] = kb + m;
                     const int p = atomicAdd(&sm.n[cur ^ 1], 1);
                     sm.list[cur ^ 1][p] = slot;
                 }
@@ -571,18 +614,19 @@ __global__ void __launch_bounds__(ORB_T) k_orbit(const Cluster *__restrict__ cls
         }
         __syncthreads();
     }
-    const double tE = block_sum<ORB_T>(acc_E, red);
-    const double tJ = block_sum<ORB_T>(acc_J, red);
-    const double tM = block_sum<ORB_T>(acc_M, red);
-    const double tEt = block_sum<ORB_T>(acc_Et, red);
-    const double tmax = block_max<ORB_T>(max_rad, red);
+    // escapers are rare: most warps skip the sums (block_sums)
+    __shared__ double s_acc[ORB_T / 32][4];
+    __shared__ long long s_max[ORB_T / 32];
+    double acc[4] = {acc_E, acc_J, acc_M, acc_Et};
+    block_sums<ORB_T>(acc, s_acc);
+    const double tmax = block_max_nonneg<ORB_T>(max_rad, s_max);
     __shared__ int s_last;
     if (threadIdx.x == 0) {
         double *slot = partials + (size_t)blockIdx.x * ORB_NPART;
-        slot[0] = tE;
-        slot[1] = tJ;
-        slot[2] = tM;
-        slot[3] = tEt;
+        slot[0] = acc[0];
+        slot[1] = acc[1];
+        slot[2] = acc[2];
+        slot[3] = acc[3];
         slot[4] = tmax;
     }
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {

@@ -352,12 +352,11 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
 
     // ---- statistics (cmc_dynamics.c:430-440), deterministic block order
     __shared__ int s_last;
-    double tot[RELAX_NPART];
-#pragma unroll
-    for (int i = 0; i < RELAX_NPART; ++i) tot[i] = block_sum<RELAX_THREADS>(part[i], red);
+    __shared__ double s_part[RELAX_THREADS / 32][RELAX_NPART];
+    block_sums<RELAX_THREADS>(part, s_part);  // most columns are zero over most warps
     if (tid == 0) {
         double *slot = partials + (size_t)blockIdx.x * RELAX_NPART;
-        for (int i = 0; i < RELAX_NPART; ++i) slot[i] = tot[i];
+        for (int i = 0; i < RELAX_NPART; ++i) slot[i] = part[i];
     }
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
         double acc[RELAX_NPART];

@@ -413,6 +413,9 @@ int cmcg_load(cmcg_ctx *c, int k, long N, const double *r, const double *m, cons
     s.orbit_r = p.orbit_r;
     s.madhoc = 1.0 / ((double)NSTAR);
     s.cenma_m = p.cenma_m;
+    // constant over the run; formed on the host with the C library's pow and
+    // log, as the reference forms it (cmc_evolution_thr.c:550)
+    s.tid_alpha = 1.5 - 3.0 * pow(log(p.GAMMA * ((double)NSTAR)) / ((double)NSTAR), 0.25);
     CK(cudaMemcpy(c->d_sc + k, &s, sizeof(Scalars), cudaMemcpyHostToDevice));
     return CMCG_OK;
 }

@@ -36,6 +36,7 @@ struct Scalars {
     double qaverelbeta[4], maverelbeta[4], raverelbeta[4];
     double phi_rtidal, gierszalpha;
     double tid_Rt, tid_phirt;  // tidal radius and its potential for the coming stripping pass
+    double tid_alpha;          // gierszalpha (cmc_evolution_thr.c:550), fixed by GAMMA and N_STAR
     int tidal_done, tidal_iters;
     int err;
     int pad0;

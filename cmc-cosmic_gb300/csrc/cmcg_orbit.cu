@@ -701,7 +701,7 @@ static __device__ __forceinline__ void tidal_radius(const Cluster &C, const Fiel
 __global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                        double *partials, unsigned int *bar, int nclusters)
 {
-    __shared__ double red[TID_THREADS / 32];
+    __shared__ double s_acc[TID_THREADS / 32][TID_NPART];
     __shared__ int s_ok;
     unsigned int gen = 0;
     if (threadIdx.x == 0) gen = *(volatile unsigned int *)&bar[1];
@@ -722,38 +722,41 @@ __global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict
             const long long off = C.off;
             const double NSTAR = (double)sc->N_STAR;
             const double phi_rtidal = *(volatile double *)&sc->tid_phirt, Rtidal = *(volatile double *)&sc->tid_Rt;
-            const double gierszalpha = 1.5 - 3.0 * pow(log(C.GAMMA * NSTAR) / NSTAR, 0.25);
-            double aE = 0.0, aJ = 0.0, aM = 0.0, aEt = 0.0;
+            const double gierszalpha = sc->tid_alpha;
+            double acc[TID_NPART] = {0.0, 0.0, 0.0, 0.0};  // E, J, M, Etidal
             const long long N_NEW = sc->N_MAX_NEW;
-            for (int it = 0; it < TID_T / TID_THREADS; ++it) {
-                const long long i = 1 + (long long)ct.y * TID_T + it * TID_THREADS + threadIdx.x;
-                if (i > N_NEW) break;
-                const long long g = off + i;
-                const double rn = f.rnew[g];
-                bool strip;
-                if (C.TIDAL_TREATMENT == 0)
-                    strip = (f.r_apo[g] > Rtidal && rn < 1000000);
-                else
-                    strip = (f.E[g] > gierszalpha * phi_rtidal && rn < 1000000);
-                if (strip) {
+            // the tile's (rnew, criterion) pairs are loaded before any test, so
+            // their latencies overlap; stars past N_MAX_NEW read as never stripped
+            constexpr int IT = TID_T / TID_THREADS;
+            const long long i0 = 1 + (long long)ct.y * TID_T + threadIdx.x;
+            const double *crit = (C.TIDAL_TREATMENT == 0) ? f.r_apo : f.E;
+            const double bound = (C.TIDAL_TREATMENT == 0) ? Rtidal : gierszalpha * phi_rtidal;
+            double rnv[IT], cv[IT];
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                const long long i = i0 + it * TID_THREADS;
+                const bool in = i <= N_NEW;
+                rnv[it] = in ? f.rnew[off + i] : CMCG_SF_INFINITY;
+                cv[it] = in ? crit[off + i] : 0.0;
+            }
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                const long long g = off + i0 + it * TID_THREADS;
+                // r_apo > Rtidal (treatment 0) or E > gierszalpha * phi_rtidal, and rnew < 1e6
+                if (cv[it] > bound && rnv[it] < 1000000) {
                     const double m = f.m[g], E = f.E[g], J = f.J[g];
-                    aE += E * m / NSTAR;
-                    aJ += J * m / NSTAR;
-                    aM += m / NSTAR;
-                    aEt += E * m / NSTAR;
+                    acc[0] += E * m / NSTAR;
+                    acc[1] += J * m / NSTAR;
+                    acc[2] += m / NSTAR;
+                    acc[3] += E * m / NSTAR;
                     destroy_obj(f, g);
                 }
             }
-            const double tE = block_sum<TID_THREADS>(aE, red);
-            const double tJ = block_sum<TID_THREADS>(aJ, red);
-            const double tM = block_sum<TID_THREADS>(aM, red);
-            const double tEt = block_sum<TID_THREADS>(aEt, red);
+            __syncthreads();  // s_acc is reused tile after tile
+            block_sums<TID_THREADS>(acc, s_acc);  // stripped stars are few: most warps skip
             if (threadIdx.x == 0) {
                 double *slot = partials + (size_t)b * TID_NPART;
-                slot[0] = tE;
-                slot[1] = tJ;
-                slot[2] = tM;
-                slot[3] = tEt;
+                for (int q = 0; q < TID_NPART; ++q) slot[q] = acc[q];
             }
         }
         if (!grid_barrier(bar, gen, &s_ok)) {
@@ -765,9 +768,14 @@ __global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict
             const Cluster &C = cls[c];
             Scalars *sc = C.sc;
             if (*(volatile int *)&sc->tidal_done || !counts_ok(C)) continue;
-            double a[TID_NPART];
-            for (int q = 0; q < TID_NPART; ++q)
-                a[q] = reduce_partials_sum<TID_THREADS>(partials, tm.first[c], tm.count[c], TID_NPART, q, red);
+            // the cluster's tiles in a fixed order: strided per thread, then block_sums
+            double a[TID_NPART] = {0.0, 0.0, 0.0, 0.0};
+            for (int t = threadIdx.x; t < tm.count[c]; t += TID_THREADS) {
+                const double *pt = partials + (size_t)(tm.first[c] + t) * TID_NPART;
+                for (int q = 0; q < TID_NPART; ++q) a[q] += __ldcg(pt + q);
+            }
+            __syncthreads();
+            block_sums<TID_THREADS>(a, s_acc);
             if (threadIdx.x == 0) {
                 if (sc->tidal_iters == 0) sc->Etidal = 0.0;  // cmc_evolution_thr.c:452
                 sc->Rtidal = sc->tid_Rt;

@@ -89,20 +89,51 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     }
 }
 
-// One block per cluster: the listed stars are put in radial order with a
-// shared-memory bitonic sort, then one thread replays the sequential
-// excess-energy pass from each of them; beyond the list's capacity the whole
-// sequential pass is replayed.  The replay reads stars from windows of
-// FIX_WINDOW consecutive stars that the whole block stages in shared memory,
-// so it runs at shared-memory latency; the walk only moves forward and
-// changes each star once, so a staged star is never stale.
+// One segment of set_velocities3's loop (cmc_utils.c:270-307): entering
+// listed star i0 with excess E (that star's own addition included), each
+// following star up to `end` (the next listed star, or N_MAX_NEW + 1) gives
+// up min(0.8 KE, excess) while the excess is positive.  Returns the excess
+// left on reaching `end`, 0 once it is used up.  WRITE applies the changes.
+template <bool WRITE>
+static __device__ double ec3_walk(const Fields &f, long long off, long long i0, long long end, double E)
+{
+    const double E_dump_factor = 0.8;
+    for (long long i = i0 + 1; i < end && E > 0; ++i) {
+        const long long g = off + i;
+        const double m = f.m[g], vr = f.vr[g], vt = f.vt[g];
+        const double v2 = sqr(vr) + sqr(vt);
+        const double E_dump_capacity = E_dump_factor * 0.5 * m * v2;
+        const double E_dump = (E_dump_capacity <= E) ? E_dump_capacity : E;
+        if (WRITE) {
+            const double exc_ratio = sqrt((v2 - 2 * E_dump / m) / v2);
+            f.vr[g] = vr * exc_ratio;
+            f.vt[g] = vt * exc_ratio;
+        }
+        E -= E_dump;
+    }
+    return E;
+}
+
+// One block per cluster.  The listed stars (unphysical predictions, which add
+// excess) are put in radial order with a shared-memory bitonic sort; they cut
+// the sequential loop into segments that start at a listed star and end
+// before the next one.  The only thing one segment passes to the next is the
+// excess still left at its end, which is almost always zero, so:
+//   1. every segment is walked in parallel as if nothing were carried into it,
+//      recording what it would carry out;
+//   2. one thread carries the excess through the segments in order, walking
+//      again only the segments that really receive some;
+//   3. every segment is walked in parallel with the excess it really receives,
+//      and writes.
+// Each segment performs the reference's operations in the reference's order,
+// so the result is the sequential loop's.  Beyond the list's capacity the
+// whole sequential loop is replayed by one thread, reading windows of
+// FIX_WINDOW consecutive stars that the block stages in shared memory.
 __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__restrict__ cls, Fields f, Ec3Bufs eb,
                                                              int nclusters)
 {
-    __shared__ int L[EXCESS_CAP];  // star indices (below 2^31: counts_ok bounds them by the capacity)
-    __shared__ double wa[FIX_WINDOW], wm[FIX_WINDOW], wvr[FIX_WINDOW], wvt[FIX_WINDOW];
+    __shared__ __align__(16) int L[EXCESS_CAP];  // star indices (below 2^31: counts_ok bounds them by the capacity)
     __shared__ long long s_i;
-    __shared__ unsigned int s_li;
     __shared__ double s_exc;
     __shared__ int s_done;
     const int c = blockIdx.x;
@@ -118,8 +149,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
         sc->n_excess = n;
     }
     if (n == 0) return;
-    const bool overflow = n > EXCESS_CAP;
-    if (!overflow) {
+    if (n <= EXCESS_CAP) {
         unsigned int P = 1;
         while (P < n) P <<= 1;
         const long long *G = eb.list + (size_t)c * EXCESS_CAP;
@@ -141,16 +171,43 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
                 __syncthreads();
             }
         }
+        double *carry = eb.carry + (size_t)c * EXCESS_CAP;
+        const int nn = (int)n;
+        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+            const long long i0 = L[t], end = (t + 1 < nn) ? L[t + 1] : N + 1;
+            carry[t] = ec3_walk<false>(f, off, i0, end, eb.a[off + i0]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double cin = 0.0;  // excess entering segment t
+            for (int t = 0; t < nn; ++t) {
+                double cout = carry[t];
+                if (cin > 0.0) {
+                    const long long i0 = L[t], end = (t + 1 < nn) ? L[t + 1] : N + 1;
+                    cout = ec3_walk<false>(f, off, i0, end, cin + eb.a[off + i0]);
+                }
+                carry[t] = cin;
+                cin = cout;
+            }
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+            const long long i0 = L[t], end = (t + 1 < nn) ? L[t + 1] : N + 1;
+            ec3_walk<true>(f, off, i0, end, carry[t] + eb.a[off + i0]);  // 0 + a = a when nothing is carried
+        }
+        return;
     }
+    // overflow: the whole loop, one thread, staged windows
+    double *wa = reinterpret_cast<double *>(L);  // 4 x FIX_WINDOW doubles fit in L's 16 KB
+    double *wm = wa + FIX_WINDOW, *wvr = wm + FIX_WINDOW, *wvt = wvr + FIX_WINDOW;
     if (threadIdx.x == 0) {
         s_exc = 0.0;
-        s_li = 0u;
-        s_i = overflow ? 1 : L[0];
+        s_i = 1;
         s_done = 0;
     }
     __syncthreads();
     const double E_dump_factor = 0.8;
-    // every window advances the walk by at least one star
+    // every window advances the walk by FIX_WINDOW stars
     for (long long guard = 0; guard <= N + 1; ++guard) {
         const long long i0 = s_i;
         if (s_done || i0 > N || i0 < 1) break;
@@ -167,15 +224,8 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
         __syncthreads();
         if (threadIdx.x == 0) {
             double Eexcess = s_exc;
-            unsigned int li = s_li;
             long long i = i0;
-            int done = 0;
-            while (true) {
-                if (i > N) {
-                    done = 1;
-                    break;
-                }
-                if (i >= i0 + FIX_WINDOW) break;  // next window
+            for (; i <= N && i < i0 + FIX_WINDOW; ++i) {
                 const int k = (int)(i - i0);
                 const double ai = wa[k];
                 if (ai >= 0.0) {
@@ -193,26 +243,10 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
                     f.vt[off + i] = vt;
                     Eexcess -= E_dump;
                 }
-                if (overflow) {
-                    ++i;
-                    continue;
-                }
-                if (ai >= 0.0) ++li;
-                if (Eexcess > 0) {
-                    ++i;
-                } else {
-                    if (li >= n) {
-                        done = 1;
-                        break;
-                    }
-                    i = L[li];  // the next listed star, further out (the list is sorted)
-                    if (i >= i0 + FIX_WINDOW) break;
-                }
             }
             s_exc = Eexcess;
-            s_li = li;
             s_i = i;
-            s_done = done;
+            s_done = i > N;
         }
         __syncthreads();
     }

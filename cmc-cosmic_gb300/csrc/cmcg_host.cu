@@ -193,6 +193,7 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->eb.a = cv.take<double>(tot);
     c->eb.list = cv.take<long long>((size_t)c->ncl * EXCESS_CAP);
     c->eb.nlist = cv.take<unsigned int>(c->ncl);
+    c->eb.carry = cv.take<double>((size_t)c->ncl * EXCESS_CAP);
     size_t np = 0;
     np = std::max(np, (size_t)c->t256.ntiles * RELAX_NPART);
     np = std::max(np, (size_t)c->t128.ntiles * ORB_NPART);

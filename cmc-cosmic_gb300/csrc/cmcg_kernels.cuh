@@ -85,6 +85,7 @@ struct Ec3Bufs {
     double *a;           // per star: excess added by an unphysical prediction (or -1)
     long long *list;     // per cluster: [EXCESS_CAP] indices
     unsigned int *nlist; // per cluster
+    double *carry;       // per cluster: [EXCESS_CAP] excess entering each listed star's segment
 };
 
 __global__ void k_timestep(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets);

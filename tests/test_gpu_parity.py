@@ -188,6 +188,65 @@ def test_tidal_sort_potential_ec3_energy(gpulib, orc, model, N, imf):
     assert max_rel(g.scalar("Etot"), o.scalar("Etot")) <= TOL_SUM
 
 
+def _ec3_planted(model, N, imf, picks, d):
+    """The tail of a step (stripping, sort, potential, set_velocities3) after
+    making the predictions of the stars at `picks` unphysical: with
+    Uoldrnew = Uoldrold + vold^2 + d, vnew^2 is about -d, and the star's excess
+    0.5 (v^2 - vnew^2) m is handed on to the stars after it (the larger d,
+    the further it reaches)."""
+    ic, o, g = _to_orbits(model, N, imf)
+    sync_state(o, g, star=[("rnew", "rnew"), ("vrnew", "vrnew"), ("vtnew", "vtnew"), ("E", "E"), ("J", "J"),
+                           ("r_apo", "r_apo")],
+               scalars=("TidalMassLoss", "OldTidalMassLoss", "Mtotal"))
+    vro, vto = o.get("vrold"), o.get("vtold")
+    vold2 = vto * vto + vro * vro
+    uo, un = o.get("Uoldrold"), o.get("Uoldrnew").copy()
+    un[picks] = uo[picks] + vold2[picks] + d
+    o.set("Uoldrnew", un)
+    g.set("ec_pre", vold2 + 1.0 * (uo - un))
+    o.tidally_strip_stars()
+    g.tidally_strip_stars()
+    o.compute_intermediate_energy()
+    o.qsorts_new()
+    g.qsorts_new()
+    o.calc_potential()
+    g.calc_potential()
+    sync_state(o, g, fields=("star_phi",))
+    o.energy_conservation3()
+    g.energy_conservation3()
+    g.check_device("energy_conservation3")
+    return o, g
+
+
+def test_excess_energy_carried_across_listed_stars(gpulib, orc):
+    """Listed stars close enough together that one's excess is still left when
+    the walk reaches the next: the segments' carries must chain exactly as
+    the sequential loop's running excess does."""
+    N = 6000
+    rng = np.random.default_rng(7)
+    scattered = rng.choice(np.arange(1, N + 1), 200, replace=False)
+    runs = np.concatenate([np.arange(s, s + 12) for s in (500, 2600, 4100)])  # adjacent listed stars
+    picks = np.unique(np.concatenate([scattered, runs]))
+    d = np.where(np.isin(picks, runs), 60.0, rng.uniform(0.5, 8.0, len(picks)))
+    o, g = _ec3_planted(cmcgpu.PLUMMER, N, 1, picks, d)
+    assert g.scalar("n_excess") >= 0.9 * len(picks)
+    assert max_rel(g.get("vr"), o.get("vr")) <= TOL_PHI
+    assert max_rel(g.get("vt"), o.get("vt")) <= TOL_PHI
+    assert np.array_equal(g.get("vr") == 0.0, o.get("vr") == 0.0)
+
+
+def test_excess_energy_beyond_the_list_capacity(gpulib, orc):
+    """More unphysical predictions than the per-cluster list holds (4096): the
+    whole sequential loop is replayed instead."""
+    N = 12000
+    rng = np.random.default_rng(11)
+    picks = rng.choice(np.arange(1, N + 1), 4700, replace=False)
+    o, g = _ec3_planted(cmcgpu.PLUMMER, N, 1, picks, rng.uniform(0.2, 3.0, len(picks)))
+    assert g.scalar("n_excess") > 4096
+    assert max_rel(g.get("vr"), o.get("vr")) <= TOL_PHI
+    assert max_rel(g.get("vt"), o.get("vt")) <= TOL_PHI
+
+
 @pytest.mark.parametrize("model,N,imf", CASES[:2])
 def test_free_running_steps(gpulib, orc, model, N, imf):
     """Whole steps with no state injection: the same stars in the same order,

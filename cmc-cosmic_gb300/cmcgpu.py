@@ -163,6 +163,7 @@ def lib() -> C.CDLL:
         L.cmcg_derive_seed.restype = C.c_uint64
         L.cmcg_draw.argtypes = [C.c_uint64, l, i, C.c_int64, C.c_uint32, i]
         L.cmcg_draw.restype = d
+        L.cmcg_sign_stages.argtypes = [vp, vp, vp, vp, d, vp, vp, l, vp]
         L.cmcg_sort_radii_noalloc.argtypes = [vp, l, vp, C.POINTER(l), vp]
         L.cmcg_put_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.cmcg_get_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
@@ -205,6 +206,20 @@ def derive_seed(master: int, index: int) -> int:
 
 def draw(seed: int, tcount: int, site: int, star_id: int, n: int, word: int) -> float:
     return float(lib().cmcg_draw(seed, tcount, site, star_id, n, word))
+
+
+def sign_stages(E, J, rj, mj, invN, rk, phik):
+    """[n, 4] signs of function_q from the FP32, float-float, FP64 and
+    double-double stages of the apsis sign test (0 = undecided)."""
+    import numpy as np
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (E, J, rj, mj, rk, phik)]
+    n = len(arrs[0])
+    out = np.zeros((n, 4), np.int32)
+    rc = lib().cmcg_sign_stages(*[a.ctypes.data for a in arrs[:4]], float(invN), arrs[4].ctypes.data,
+                                arrs[5].ctypes.data, n, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"cmcg_sign_stages failed: {rc}")
+    return out
 
 
 class Context:

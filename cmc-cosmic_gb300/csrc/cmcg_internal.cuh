@@ -366,15 +366,17 @@ __device__ __forceinline__ double function_q_dd(double r, double pot, double E, 
 // Returns +1, -1, or 0 when the caller must evaluate in double-double.
 struct QF32 {
     float E, El, J, mjN, pj;  // E as a float pair (E ~ E + El), J, m_j/N_STAR, (m_j/r_j)/N_STAR as floats
+    float Jl, mjNl, pjl;      // low parts of J, m_j/N_STAR, (m_j/r_j)/N_STAR (float-float stage)
     double rj;                // r_j: the self-potential branch is chosen in FP64
     double Ed, Jd, mjNd, pjd; // the same in FP64, for the second filter
 };
 
-// (float r, Phi as a float pair hi + lo with |Phi - hi - lo| <= 2^-48 |Phi|, 0)
+// (r hi, Phi hi, Phi lo, r lo): r and Phi as float pairs hi + lo, each within
+// 2^-48 of the double it stands for
 __device__ __forceinline__ float4 rphi_entry(double r, double phi)
 {
-    const float hi = (float)phi;
-    return make_float4((float)r, hi, (float)(phi - (double)hi), 0.0f);
+    const float hi = (float)phi, rh = (float)r;
+    return make_float4(rh, hi, (float)(phi - (double)hi), (float)(r - (double)rh));
 }
 
 // E - Phi is formed in float-float (exact difference of the high parts plus
@@ -395,8 +397,57 @@ __device__ __forceinline__ int fq_sign_f32(const QF32 &s, float4 rp, bool ge)
     const float A = D - phis;
     const float q = s.J * ir;
     const float B = q * q;
+    // (J/r)^2 beyond the float range (the r = 1e-20 sentinel at k = 0) against a
+    // finite 2(E - Phi - phis): Q is negative however either is rounded
+    if (B == INFINITY && fabsf(A) < 1e30f) return -1;
     const float Q = 2.0f * A - B;
     const float bound = 0x1p-19f * (fabsf(D) + fabsf(phis) + fabsf(A) + B) + 0x1p-42f * (fabsf(s.E) + fabsf(rp.y));
+    if (Q > bound) return 1;
+    if (Q < -bound) return -1;
+    return 0;
+}
+
+__device__ __forceinline__ float2 ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+
+// Certified float-float sign of function_q at a table point: every operand an
+// unevaluated float pair (within 2^-48 of its double), 1/r as y0 (1 + e) with
+// y0 the float reciprocal and e = 1 - r y0 from FMAs, J/r and m_j/(N r) as
+// compensated products, (J/r)^2 as a compensated square, the differences by
+// two-sum (Knuth).  With u = 2^-24, charging every rounding and neglected
+// term: 1/r to 9u^2, J/r to 17u^2, (J/r)^2 to 39u^2, the self-potential to
+// 17u^2, E - Phi to 4u^2 (|E| + |Phi|); the two differences add at most
+// 8u^2 (|E| + |Phi|) + 12u^2 phis + 6u^2 |A| + 4u^2 (J/r)^2.  In all
+//   |Q_ff - Q| <= 20u^2 (|E|+|Phi|) + 52u^2 phis + 6u^2 |A| + 43u^2 (J/r)^2
+// below 2^-42 of the magnitudes' sum; the reference's own roundings (J/r
+// rounded to double: 2^-52 (J/r)^2; long double) add under 2^-51 of it.  The
+// threshold is 2^-40 of the sum, plus 1e-30 against underflow.  Returns +1,
+// -1, or 0 (undecided: within about 2^-40 of a root).
+__device__ __forceinline__ int fq_sign_ff(const QF32 &s, float4 rp, bool ge)
+{
+    const float y0 = __frcp_rn(rp.x);
+    const float e = __fmaf_rn(-rp.w, y0, __fmaf_rn(-rp.x, y0, 1.0f));
+    const float il = __fmul_rn(y0, e);  // 1/r ~ y0 + il
+    const float q = __fmul_rn(s.J, y0);
+    const float ql = __fadd_rn(__fmaf_rn(s.J, y0, -q), __fadd_rn(__fmul_rn(s.J, il), __fmul_rn(s.Jl, y0)));
+    const float b = __fmul_rn(q, q);
+    const float bl = __fadd_rn(__fmaf_rn(q, q, -b), __fmul_rn(__fmul_rn(2.0f, q), ql));
+    float ph = s.pj, pl = s.pjl;
+    if (ge) {
+        ph = __fmul_rn(s.mjN, y0);
+        pl = __fadd_rn(__fmaf_rn(s.mjN, y0, -ph), __fadd_rn(__fmul_rn(s.mjN, il), __fmul_rn(s.mjNl, y0)));
+    }
+    const float2 d = ff_two_sum(s.E, -rp.y);
+    const float dl = __fadd_rn(d.y, __fsub_rn(s.El, rp.z));
+    const float2 a = ff_two_sum(d.x, -ph);
+    const float al = __fadd_rn(a.y, __fsub_rn(dl, pl));
+    const float2 qq = ff_two_sum(__fmul_rn(2.0f, a.x), -b);
+    const float Q = __fadd_rn(qq.x, __fadd_rn(qq.y, __fsub_rn(__fmul_rn(2.0f, al), bl)));
+    const float bound =
+        __fadd_rn(__fmul_rn(0x1p-40f, fabsf(s.E) + fabsf(rp.y) + fabsf(ph) + fabsf(a.x) + b), 1e-30f);
     if (Q > bound) return 1;
     if (Q < -bound) return -1;
     return 0;

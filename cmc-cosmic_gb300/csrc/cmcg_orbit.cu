@@ -36,12 +36,16 @@ static __device__ __forceinline__ double fq(const OrbitCtx &o, long long k)
 }
 
 // Sign of function_q at table point k: certified FP32 first, then certified
-// FP64 from the 1/r table, double-double only when both lie within their
-// error bounds (a table point within ~1e-15 of a root).
+// float-float (still on the FP32 pipe), then certified FP64 from the 1/r
+// table, double-double only when all lie within their error bounds (a table
+// point within ~1e-15 of a root).
 static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
 {
     const bool ge = k >= o.j;
-    int s = fq_sign_f32(o.s, __ldg(o.rphif + k), ge);
+    const float4 rp = __ldg(o.rphif + k);
+    int s = fq_sign_f32(o.s, rp, ge);
+    if (s) return s;
+    s = fq_sign_ff(o.s, rp, ge);
     if (s) return s;
     s = fq_sign_f64(o.s, __ldg(o.inv_r + k), __ldg(o.phi + k), ge);
     if (s) return s;
@@ -223,8 +227,12 @@ static __device__ __forceinline__ OrbitCtx make_orbit_ctx(const Cluster &C, cons
     o.s.E = (float)E;
     o.s.El = (float)(E - (double)o.s.E);
     o.s.J = (float)J;
-    o.s.mjN = (float)(mj * o.invN);
+    o.s.Jl = (float)(J - (double)o.s.J);
+    const double mjN = mj * o.invN;
+    o.s.mjN = (float)mjN;
+    o.s.mjNl = (float)(mjN - (double)o.s.mjN);
     o.s.pj = (float)ps;  // PHI_S(r_j) = (m_j / r_j) / N_STAR
+    o.s.pjl = (float)(ps - (double)o.s.pj);
     o.s.rj = rj;
     o.s.Ed = E;
     o.s.Jd = J;
@@ -820,4 +828,68 @@ __global__ void k_potential_query(const Cluster *__restrict__ cls, Fields f, int
     out[1] = ok ? 0.0 : 1.0;
 }
 
+// Every stage of the certified sign test at one point (cmcg_sign_stages).
+__global__ void k_sign_stages(const double *E, const double *J, const double *rj, const double *mj, double invN,
+                              const double *rk, const double *phik, long long n, int *out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double r = rk[i], ph = phik[i];
+    const double ps = __dmul_rn(__ddiv_rn(mj[i], rj[i]), invN);
+    OrbitCtx o;
+    o.invN = invN;
+    // the per-star constants exactly as make_orbit_ctx forms them
+    o.s.E = (float)E[i];
+    o.s.El = (float)(E[i] - (double)o.s.E);
+    o.s.J = (float)J[i];
+    o.s.Jl = (float)(J[i] - (double)o.s.J);
+    const double mjN = mj[i] * invN;
+    o.s.mjN = (float)mjN;
+    o.s.mjNl = (float)(mjN - (double)o.s.mjN);
+    o.s.pj = (float)ps;
+    o.s.pjl = (float)(ps - (double)o.s.pj);
+    o.s.rj = rj[i];
+    o.s.Ed = E[i];
+    o.s.Jd = J[i];
+    o.s.mjNd = mjN;
+    o.s.pjd = ps;
+    const bool ge = r >= rj[i];
+    const float4 rp = rphi_entry(r, ph);
+    out[4 * i + 0] = fq_sign_f32(o.s, rp, ge);
+    out[4 * i + 1] = fq_sign_ff(o.s, rp, ge);
+    out[4 * i + 2] = fq_sign_f64(o.s, __drcp_rn(r), ph, ge);
+    const double q = function_q_dd(r, ph, E[i], J[i], rj[i], mj[i], invN);
+    out[4 * i + 3] = (q > 0.0) - (q < 0.0);
+}
+
 }  // namespace cmcg
+
+extern "C" int cmcg_sign_stages(const double *E, const double *J, const double *rj, const double *mj, double invN,
+                                const double *rk, const double *phik, long n, int *out)
+{
+    using namespace cmcg;
+    if (n < 0 || (n > 0 && (!E || !J || !rj || !mj || !rk || !phik || !out))) return CMCG_ERR_ARG;
+    if (n == 0) return CMCG_OK;
+    const size_t nd = (size_t)n * sizeof(double);
+    double *d = nullptr;
+    int *dout = nullptr;
+    if (cudaMalloc(&d, 6 * nd) != cudaSuccess) return CMCG_ERR_NOMEM;
+    if (cudaMalloc(&dout, 4 * (size_t)n * sizeof(int)) != cudaSuccess) {
+        cudaFree(d);
+        return CMCG_ERR_NOMEM;
+    }
+    const double *src[6] = {E, J, rj, mj, rk, phik};
+    int rc = CMCG_OK;
+    for (int a = 0; a < 6 && rc == CMCG_OK; ++a)
+        if (cudaMemcpy(d + (size_t)a * n, src[a], nd, cudaMemcpyHostToDevice) != cudaSuccess) rc = CMCG_ERR_CUDA;
+    if (rc == CMCG_OK) {
+        k_sign_stages<<<(unsigned)((n + 255) / 256), 256>>>(d, d + n, d + 2 * n, d + 3 * n, invN, d + 4 * n, d + 5 * n,
+                                                           n, dout);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(out, dout, 4 * (size_t)n * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = CMCG_ERR_CUDA;
+    }
+    cudaFree(d);
+    cudaFree(dout);
+    return rc;
+}

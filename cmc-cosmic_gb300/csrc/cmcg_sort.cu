@@ -181,7 +181,6 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
 {
     constexpr int NWARP = OS_THREADS / 32, ITEMS = SORT_T / OS_THREADS;
     __shared__ unsigned int wcnt[NWARP][RADIX];  // per-warp digit counters -> prefixes
-    __shared__ unsigned int dcnt[RADIX];         // the tile's count per digit
     __shared__ unsigned int dstart[RADIX];       // in-tile digit start
     __shared__ unsigned long long gbase[RADIX];  // global digit start for this tile
     __shared__ unsigned long long sk[SORT_T];
@@ -241,7 +240,6 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
             wcnt[q][d] = cnt;
             cnt += t;
         }
-        dcnt[d] = cnt;
         const unsigned long long tag = st_tag(*(volatile unsigned int *)sb.epoch, pass);
         unsigned long long *st = sb.status + (size_t)b * RADIX;
         atomicExch(st + d, tag | (ct.y == 0 ? ST_INC : ST_AGG) | cnt);

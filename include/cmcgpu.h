@@ -179,6 +179,14 @@ int cmcg_profile(cmcg_ctx *ctx, int enable);
 int cmcg_kernel_time(cmcg_ctx *ctx, const char *family, double *ms_total, long *launches);
 /* Counter-based uniform draw the kernels use (site, star id, n, word). */
 double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, int word);
+/* Diagnostic: the sign of function_q (cmc_utils.c:1654) at n points
+ * (r_k, Phi_k) for stars (E, J, r_j, m_j), E including PHI_S(r_j), from each
+ * stage of the certified test the apsis bisections use: out[4i + s] for
+ * s = 0 FP32, 1 float-float, 2 FP64 (+1 / -1, or 0 = undecided) and s = 3 the
+ * double-double evaluation (always decided).  Host arrays; runs on the
+ * current device and waits for it. */
+int cmcg_sign_stages(const double *E, const double *J, const double *rj, const double *mj, double invN,
+                     const double *rk, const double *phik, long n, int *out);
 
 /* --------------------------------------------- allocation-free variant ---
  * No counterpart in the reference.  For callers that cannot allocate device

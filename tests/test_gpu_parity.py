@@ -423,3 +423,36 @@ def test_new_orbits_when_q_is_negative_at_the_star(gpulib, orc, model, N, imf):
     assert max_rel(rn_g[keep], rn_o[keep]) <= TOL_ORBIT
     assert max_rel(g.get("r_peri")[pick], o.get("r_peri")[pick]) <= TOL_ORBIT
     assert max_rel(g.get("r_apo")[pick], o.get("r_apo")[pick]) <= TOL_ORBIT
+
+
+def test_sign_stages_agree_near_roots(gpulib):
+    """Every stage of the apsis sign test that decides agrees with the
+    double-double evaluation, on points placed at relative distances 1e-18 to
+    1e-2 from a root of function_q; the float-float stage decides every point
+    farther than 2^-36 of the magnitudes involved."""
+    rng = np.random.default_rng(5)
+    n = 400000
+    invN = 1.0 / 1e6
+    E = -rng.uniform(0.01, 3.0, n)
+    J = 10 ** rng.uniform(-4, 0.5, n)
+    rj = 10 ** rng.uniform(-3, 1.7, n)
+    mj = 10 ** rng.uniform(-1, 1.7, n)
+    rk = 10 ** rng.uniform(-3, 1.7, n)
+    phis = np.where(rk >= rj, mj * invN / rk, (mj / rj) * invN)
+    B = (J / rk) ** 2
+    phi0 = E - phis - 0.5 * B                 # function_q = 2 (E - Phi - phis) - (J/r)^2 = 0
+    scale = np.abs(E) + np.abs(phi0) + phis + 0.5 * B
+    delta = rng.choice([-1.0, 1.0], n) * 10 ** rng.uniform(-18, -2, n)
+    out = cmcgpu.sign_stages(E, J, rj, mj, invN, rk, phi0 + delta * scale)
+    dd = out[:, 3]
+    assert (dd != 0).mean() > 0.99
+    for s in range(3):
+        decided = out[:, s] != 0
+        wrong = decided & (out[:, s] != dd)
+        assert not wrong.any(), (s, np.flatnonzero(wrong)[:5])
+    far = np.abs(delta) > 2.0 ** -36
+    assert (out[far, 1] != 0).all()
+    # the r = 1e-20 sentinel: (J/r)^2 overflows the float stages
+    m = 2000
+    out0 = cmcgpu.sign_stages(E[:m], J[:m], rj[:m], mj[:m], invN, np.full(m, 1e-20), phi0[:m])
+    assert (out0[:, 3] == -1).all() and (out0[:, 0] == -1).all()

@@ -48,7 +48,7 @@ class Params(C.Structure):
         ("TIDAL_TREATMENT", C.c_int), ("orbit_r", C.c_double), ("cenma_m", C.c_double),
         ("apsides_max_iter", C.c_long), ("apsides_precision", C.c_double),
         ("apsides_convergence", C.c_double), ("n_try", C.c_long), ("seed", C.c_uint64),
-        ("relax_fp32", C.c_int), ("phi_sequential", C.c_int),
+        ("relax_fp32", C.c_int), ("phi_sequential", C.c_int), ("check_filters", C.c_int),
     ]
 
 

@@ -243,6 +243,7 @@ void cmcg_default_params(cmcg_params *p)
     p->seed = 0;
     p->relax_fp32 = 0;
     p->phi_sequential = 0;
+    p->check_filters = 0;
 }
 
 // Sequential points of the potential replay a cluster may record (per chain):
@@ -334,6 +335,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         C.seed = p.seed;
         C.relax_fp32 = p.relax_fp32;
         C.phi_sequential = p.phi_sequential;
+        C.check_filters = p.check_filters;
         C.rec_off = rec_off;
         C.rec_cap = phi_rec_cap(c->cap[k]);
         rec_off += C.rec_cap;

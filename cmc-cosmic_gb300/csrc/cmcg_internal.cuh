@@ -70,7 +70,8 @@ struct Cluster {
     int phi_sequential;    // 1: potential by the plain sequential loop (one thread)
     long long rec_off, rec_cap;  // this cluster's slice of the sequential-point records
     long long ridx_off;    // this cluster's radius index table (ridx_B + 1 entries)
-    int ridx_B, pad2;
+    int ridx_B;
+    int check_filters;     // verify every certified FP32 trial decision exactly (CMCG_ERR_FILTER)
 };
 
 // Device-resident fields (all concatenated over clusters).

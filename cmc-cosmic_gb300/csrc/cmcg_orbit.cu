@@ -334,40 +334,50 @@ static __device__ __forceinline__ void destroy_obj(const Fields &f, long long g)
 // rejection loop, cmc_evolution_thr.c:855-926).  A star's trial k uses draws
 // keyed by (star id, k), so its trials are independent of one another and of
 // the order they run in.  Each round gives every pending star m = ORB_T / n
-// threads (n pending stars), which evaluate its next m trials at once; the
-// first trial that decides (accepted, or an error the reference would stop
-// at) is the one the reference's sequential loop stops at, and only it
-// writes.  Rounds stay full of threads and their number falls from the
-// longest trial sequence of the block to about log of it.
+// threads (n pending stars), which test its next m trials at once with a
+// certified FP32 filter (filter_trial); the first trial the filter does not
+// reject is the only candidate for the star's outcome in the reference's
+// sequential loop, and those candidates, one per star, are then evaluated
+// exactly in FP64 by threads packed into full warps.  A candidate the exact
+// evaluation rejects (the filter was unsure) puts the star back with its
+// next trial.  Rounds stay full of threads, their number falls to about the
+// log of the longest trial sequence, and the FP64 evaluation runs about
+// once per star instead of once per trial.
 struct SampleSmem {
     double rmin[ORB_T], rmax[ORB_T], F[ORB_T], E[ORB_T], J[ORB_T], rj[ORB_T], mj[ORB_T], vold2[ORB_T],
         Uold[ORB_T], ps[ORB_T];
+    double c0[ORB_T], c1[ORB_T];  // 0.5 (rmin + rmax), 0.25 (rmax - rmin): the reference's factors
     long long id[ORB_T];
+    long long rjb[ORB_T];         // bits of r_j (r >= r_j compared on bit patterns)
+    float fE[ORB_T], fEl[ORB_T], fJ[ORB_T], fmjN[ORB_T], fpj[ORB_T], fF[ORB_T], fc1[ORB_T];
     int next[ORB_T];   // the star's next trial number (1-based)
-    int first[ORB_T];  // the first deciding trial of this round (INT_MAX: none)
+    int first[ORB_T];  // the first trial of this round the filter did not reject (INT_MAX: none)
     int list[2][ORB_T];
-    int n[2];
+    int wl[ORB_T];     // this round's candidates, one slot per star
+    int n[2], nw;
 };
 
 constexpr int TRIAL_REJECT = 0, TRIAL_ACCEPT = 1;  // anything else is a device status code
+constexpr int TRIAL_UNSURE = -1;                  // filter only: left to the exact evaluation
 
 struct Trial {
     double X, r, ir, vr, pot;
     int code;
 };
 
-// Trial k of star slot s, evaluated without writing anything.
+// Trial k of star slot s, evaluated exactly as the reference does, without
+// writing anything.
 static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scalars *sc, const Fields &f,
                                                    const SampleSmem &sm, int s, int k, double invN)
 {
     Trial t;
     const long long off = C.off, N_MAX = sc->N_MAX;
-    const double rmin = sm.rmin[s], rmax = sm.rmax[s], E = sm.E[s], J = sm.J[s], rj = sm.rj[s], mj = sm.mj[s];
+    const double E = sm.E[s], J = sm.J[s], rj = sm.rj[s], mj = sm.mj[s], c1 = sm.c1[s];
     const uint4 u = draw_block(C.seed, sc->tcount, SITE_TRIAL, sm.id[s], (unsigned int)(k - 1));
     const double X = u01(u.x);
     const double s0 = 2.0 * X - 1.0;
     const double g0 = sm.F[s] * u01(u.y);
-    const double r = 0.5 * (rmin + rmax) + 0.25 * (rmax - rmin) * (3.0 * s0 - s0 * s0 * s0);
+    const double r = sm.c0[s] + c1 * (3.0 * s0 - s0 * s0 * s0);
     // one correctly rounded 1/r serves every division by r below (div_rcp)
     const double ir = __drcp_rn(r);
     int pok = 1;
@@ -395,7 +405,7 @@ static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scala
         t.code = CMCG_ERR_FINDZERO_R;
         return t;
     }
-    const double drds = 0.25 * (rmax - rmin) * (3.0 - 3.0 * s0 * s0);
+    const double drds = c1 * (3.0 - 3.0 * s0 * s0);  // 0.25 (rmax - rmin) (3 - 3 s0^2)
     const double Q = 2.0 * E - 2.0 * pot - div_rcp(div_rcp(J * J, r, ir), r, ir);
     double vr;
     if (Q >= 0.0) {
@@ -410,6 +420,71 @@ static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scala
     t.vr = vr;
     t.code = (g0 < 1.0 / vr * drds) ? TRIAL_ACCEPT : TRIAL_REJECT;
     return t;
+}
+
+// Certified FP32 decision of trial k: TRIAL_ACCEPT or TRIAL_REJECT where the
+// exact evaluation must agree, TRIAL_UNSURE otherwise.  Only r is formed in
+// FP64 (as the reference forms it, so the radius search is the reference's);
+// the rest works on floats.
+//  * The interpolated potential lies between the two table values around r:
+//    the reference's weight RN(1/r_i - 1/r) / RN(1/r_i - 1/r_i+1) is in [0, 1]
+//    because RN is monotone, so Q is bracketed by its values at those two
+//    potentials.  Each end, formed from the float pairs of E and the table's
+//    float Phi, is within 2^-20.7 M of the reference's (M = |E| + |Phi| +
+//    phis + |A| + (J/r)^2, A = E - Phi - phis); the bracket is widened by
+//    2^-18 M.
+//  * Accepted when g0^2 Qmax < drds^2 (1 - eta), rejected when g0^2 Qmin >
+//    drds^2 (1 + eta): g0, drds and the products carry at most 2^-19.5 of
+//    their value in float; the reference's 3 - 3 s0^2 loses up to
+//    2^-51 / (1 - s0^2) to cancellation, and 1 - s0^2 = 4 X (1 - X) is formed
+//    from the integer draw without it.  eta = 2^-17 + 2^-48 / (1 - s0^2).
+//  * Q < 0 for certain: vr = 0 and 1/vr * drds is +inf (drds > 0 unless the
+//    draw is 0), so the trial is accepted.
+// Radii at or below r_1, a failed search, neighbours within 4 ulps (whose
+// reciprocals may round equal) and non-finite values are unsure.
+static __device__ __forceinline__ int filter_trial(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                   const SampleSmem &sm, int s, int k)
+{
+    const uint4 u = draw_block(C.seed, sc->tcount, SITE_TRIAL, sm.id[s], (unsigned int)(k - 1));
+    const float fc1 = sm.fc1[s];
+    if (u.x == 0u || !(fc1 > 0.0f)) return TRIAL_UNSURE;
+    const double X = u01(u.x);
+    const double s0 = 2.0 * X - 1.0;
+    const double r = sm.c0[s] + sm.c1[s] * (3.0 * s0 - s0 * s0 * s0);
+    const long long off = C.off, N_MAX = sc->N_MAX;
+    const double *rt = f.r + off;
+    const long long rb = dbits(r);
+    if (rb <= dbits(__ldg(rt + 1))) return TRIAL_UNSURE;
+    const long long i = potential_index(rt, N_MAX, r, ridx_of(C, f));
+    if (i < 1 || i > N_MAX) return TRIAL_UNSURE;
+    const long long bi = dbits(__ldg(rt + i)), bi1 = dbits(__ldg(rt + i + 1));
+    if (bi >= rb || bi1 < rb || bi1 - bi <= 4) return TRIAL_UNSURE;
+    const float4 ta = __ldg(f.rphif + off + i), tb = __ldg(f.rphif + off + i + 1);
+    const float plo = fminf(ta.y, tb.y), phi = fmaxf(ta.y, tb.y);
+    const float irf = __frcp_rn((float)r);
+    const float phis = (rb >= sm.rjb[s]) ? __fmul_rn(sm.fmjN[s], irf) : sm.fpj[s];
+    const float q = __fmul_rn(sm.fJ[s], irf);
+    const float B = __fmul_rn(q, q);
+    const float2 dlo = ff_two_sum(sm.fE[s], -phi), dhi = ff_two_sum(sm.fE[s], -plo);
+    const float Alo = __fsub_rn(__fadd_rn(dlo.x, __fadd_rn(dlo.y, sm.fEl[s])), phis);
+    const float Ahi = __fsub_rn(__fadd_rn(dhi.x, __fadd_rn(dhi.y, sm.fEl[s])), phis);
+    const float M = fabsf(sm.fE[s]) + fmaxf(fabsf(plo), fabsf(phi)) + phis + B + fmaxf(fabsf(Alo), fabsf(Ahi));
+    const float eQ = __fmul_rn(0x1p-18f, M);
+    const float Qlo = __fsub_rn(__fsub_rn(__fmul_rn(2.0f, Alo), B), eQ);
+    const float Qhi = __fadd_rn(__fsub_rn(__fmul_rn(2.0f, Ahi), B), eQ);
+    if (!(fabsf(Qlo) <= 1e30f) || !(fabsf(Qhi) <= 1e30f)) return TRIAL_UNSURE;
+    if (Qhi < 0.0f) return TRIAL_ACCEPT;
+    if (!(Qlo > 0.0f)) return TRIAL_UNSURE;
+    // 1 - s0^2 = 4 X (1 - X) = u (2^32 - u) 2^-62
+    const float w = __fmul_rn(__fmul_rn((float)u.x, (float)(0u - u.x)), 0x1p-62f);
+    const float drds = __fmul_rn(__fmul_rn(3.0f, fc1), w);
+    const float g0 = __fmul_rn(sm.fF[s], __fmul_rn((float)u.y, 0x1p-32f));
+    const float eta = __fadd_rn(0x1p-17f, __fmul_rn(0x1p-48f, __frcp_rn(w)));
+    const float g2 = __fmul_rn(g0, g0), d2 = __fmul_rn(drds, drds);
+    if (!(g2 <= 1e30f) || !(d2 <= 1e30f) || !(d2 > 1e-30f)) return TRIAL_UNSURE;
+    if (__fmul_rn(g2, Qhi) < __fmul_rn(d2, __fsub_rn(1.0f, eta))) return TRIAL_ACCEPT;
+    if (__fmul_rn(g2, Qlo) > __fmul_rn(d2, __fadd_rn(1.0f, eta))) return TRIAL_REJECT;
+    return TRIAL_UNSURE;
 }
 
 // The accepted trial's outputs (cmc_evolution_thr.c:918-935).
@@ -556,9 +631,10 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
                 const double g1 = sqrt(3.0 * (rmax - rmin) / orb.dQdrp);
                 const double g2 = sqrt(-3.0 * (rmax - rmin) / orb.dQdra);
                 const int ts = threadIdx.x;
+                const double F = 1.2 * (g1 >= g2 ? g1 : g2);
                 sm.rmin[ts] = rmin;
                 sm.rmax[ts] = rmax;
-                sm.F[ts] = 1.2 * (g1 >= g2 ? g1 : g2);
+                sm.F[ts] = F;
                 sm.E[ts] = E;
                 sm.J[ts] = J;
                 sm.rj[ts] = rj;
@@ -567,6 +643,17 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
                 sm.Uold[ts] = Uoldrold;
                 sm.id[ts] = idj;
                 sm.ps[ts] = ps;
+                sm.c0[ts] = 0.5 * (rmin + rmax);
+                sm.c1[ts] = 0.25 * (rmax - rmin);
+                sm.rjb[ts] = dbits(rj);
+                // the filter's floats: E as a float pair, the rest rounded once
+                sm.fE[ts] = o.s.E;
+                sm.fEl[ts] = o.s.El;
+                sm.fJ[ts] = o.s.J;
+                sm.fmjN[ts] = o.s.mjN;
+                sm.fpj[ts] = o.s.pj;
+                sm.fF[ts] = (float)F;
+                sm.fc1[ts] = (float)sm.c1[ts];
                 pend = C.n_try >= 1;
                 if (!pend) set_error(sc, CMCG_ERR_NTRY, j);  // no trial allowed (cmc_evolution_thr.c:888)
             }
@@ -585,39 +672,60 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
     __syncthreads();
     const long long j0 = 1 + (long long)ct.y * ORB_T;
     const long long n_try = C.n_try;
+    const bool check = C.check_filters != 0;
     for (int cur = 0;; cur ^= 1) {
         const int n = sm.n[cur];
         if (n == 0) break;
         const int m = ORB_T / n;  // trials per pending star this round
-        if (t == 0) sm.n[cur ^ 1] = 0;  // last read at the top of the previous round
+        if (t == 0) {
+            sm.n[cur ^ 1] = 0;  // last read at the top of the previous round
+            sm.nw = 0;
+        }
+        // 1. the filter on each star's next m trials
         int slot = -1, k = 0, kb = 0;
-        Trial tr;
-        tr.code = TRIAL_REJECT;
         if (t < n * m) {
             slot = sm.list[cur][t / m];
             kb = sm.next[slot];
             k = kb + t % m;
             if (k <= n_try) {
-                tr = eval_trial(C, sc, f, sm, slot, k, invN);
-                if (tr.code != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
+                const int dec = filter_trial(C, sc, f, sm, slot, k);
+                if (dec != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
+                if (check && dec != TRIAL_UNSURE && eval_trial(C, sc, f, sm, slot, k, invN).code != dec)
+                    set_error(sc, CMCG_ERR_FILTER, j0 + slot);
             }
         }
         __syncthreads();
+        // 2. candidates listed; stars whose m trials were all rejected go on
         if (slot >= 0) {
             const int fst = sm.first[slot];
             if (k == fst) {
-                if (tr.code == TRIAL_ACCEPT)
-                    commit_trial(C, sc, f, sm, slot, off + j0 + slot, tr, &max_rad);
-                else
-                    set_error(sc, tr.code, j0 + slot);
+                sm.wl[atomicAdd(&sm.nw, 1)] = slot;
             } else if (t % m == 0 && fst == INT_MAX) {
                 if (kb + m - 1 >= n_try) {
                     set_error(sc, CMCG_ERR_NTRY, j0 + slot);  // n_try trials, none accepted
                 } else {
                     sm.next[slot] = kb + m;
-                    const int p = atomicAdd(&sm.n[cur ^ 1], 1);
-                    sm.list[cur ^ 1][p] = slot;
+                    sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = slot;
                 }
+            }
+        }
+        __syncthreads();
+        // 3. the candidates evaluated exactly, one star per thread
+        if (t < sm.nw) {
+            const int s = sm.wl[t];
+            const int kk = sm.first[s];
+            const Trial tr = eval_trial(C, sc, f, sm, s, kk, invN);
+            if (tr.code == TRIAL_ACCEPT) {
+                commit_trial(C, sc, f, sm, s, off + j0 + s, tr, &max_rad);
+            } else if (tr.code != TRIAL_REJECT) {
+                set_error(sc, tr.code, j0 + s);
+            } else if (kk >= n_try) {
+                set_error(sc, CMCG_ERR_NTRY, j0 + s);
+            } else {
+                // the filter was unsure and the trial is rejected: go on from the next one
+                sm.first[s] = INT_MAX;
+                sm.next[s] = kk + 1;
+                sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = s;
             }
         }
         __syncthreads();

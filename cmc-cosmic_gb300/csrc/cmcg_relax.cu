@@ -374,7 +374,7 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
     }
 }
 
-__global__ void __launch_bounds__(RELAX_THREADS) k_relax64(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+__global__ void __launch_bounds__(RELAX_THREADS, 5) k_relax64(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                            double *partials, unsigned int *tickets, double dt)
 {
     relax_body<false>(cls, tm, f, partials, tickets, dt);

@@ -60,8 +60,10 @@ enum {
     CMCG_ERR_ENCOUNTER = 12,    /* a strong-encounter draw hit (host physics)   */
     CMCG_ERR_SPIN = 20,         /* a bounded cross-block wait gave up           */
     CMCG_ERR_TIDAL_ITER = 21,   /* tidal stripping did not settle               */
-    CMCG_ERR_BOUNDS = 22        /* a star count or index outside the cluster's
+    CMCG_ERR_BOUNDS = 22,       /* a star count or index outside the cluster's
                                    capacity was refused (access skipped)        */
+    CMCG_ERR_FILTER = 23        /* check_filters: a certified FP32 decision
+                                   disagreed with the exact evaluation         */
 };
 
 /* ------------------------------------------------------- parameters ----- */
@@ -84,6 +86,9 @@ typedef struct {
     int phi_sequential;        /* 1 = potential by the plain one-thread loop
                                   instead of the parallel exact replay (both give
                                   the reference's bits; for testing)              */
+    int check_filters;         /* 1 = every certified FP32 accept/reject of an
+                                  orbit trial is also evaluated exactly; a
+                                  disagreement is CMCG_ERR_FILTER (for testing)   */
 } cmcg_params;
 
 void cmcg_default_params(cmcg_params *p);

@@ -456,3 +456,23 @@ def test_sign_stages_agree_near_roots(gpulib):
     m = 2000
     out0 = cmcgpu.sign_stages(E[:m], J[:m], rj[:m], mj[:m], invN, np.full(m, 1e-20), phi0[:m])
     assert (out0[:, 3] == -1).all() and (out0[:, 0] == -1).all()
+
+
+@pytest.mark.parametrize("model,N", [(cmcgpu.KING, 200000), (cmcgpu.PLUMMER, 100000)])
+def test_trial_filter_decisions_match_exact(gpulib, model, N):
+    """With check_filters every certified FP32 accept/reject of an orbit trial
+    is also evaluated exactly: whole steps run without a disagreement, and
+    the state is the same as without the check."""
+    ic = cmcgpu.generate(model, N, seed=3, imf=1)
+    states = []
+    for check in (1, 0):
+        p = cmcgpu.default_params(orbit_r=ic["rtid"], seed=99, check_filters=check)
+        g = cmcgpu.Context([N], [p])
+        g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+        g.initialize()
+        g.step(3)
+        g.check_device("three steps")
+        states.append([g.get(name) for name in ("r", "vr", "vt", "m")] + [g.ids()])
+        g.close()
+    for a, b in zip(*states):
+        assert np.array_equal(a, b)

@@ -39,10 +39,9 @@ static __device__ __forceinline__ double fq(const OrbitCtx &o, long long k)
 // float-float (still on the FP32 pipe), then certified FP64 from the 1/r
 // table, double-double only when all lie within their error bounds (a table
 // point within ~1e-15 of a root).
-static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
+static __device__ __forceinline__ int fq_sign_at(const OrbitCtx &o, long long k, float4 rp)
 {
     const bool ge = k >= o.j;
-    const float4 rp = __ldg(o.rphif + k);
     int s = fq_sign_f32(o.s, rp, ge);
     if (s) return s;
     s = fq_sign_ff(o.s, rp, ge);
@@ -53,10 +52,17 @@ static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
     return (q > 0.0) - (q < 0.0);
 }
 
+static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
+{
+    return fq_sign_at(o, k, __ldg(o.rphif + k));
+}
+
 // find_zero_Q, cmc_nr.c:316-383 (bounded; returns -1 if it does not terminate).
 // The reference compares the end-point values to choose the direction; when
 // their signs differ the signs decide it, and only same-signed ends are
 // evaluated in double-double and compared.  The bisection only needs signs.
+// (Fetching several levels of probes at once measured slower: the extra
+// live entries cost occupancy and spills that outweigh the shorter chain.)
 static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long long kmax)
 {
     const int smin = fq_sign(o, kmin), smax = fq_sign(o, kmax);

@@ -7,15 +7,16 @@
 // vt = vtnew, rOld = old r).
 //
 // Keys are the IEEE bit patterns of rnew (positive doubles order like their
-// bits), values the star's slot.
+// bits) less the cluster's smallest, with every escaper (rnew = SF_INFINITY)
+// one past the largest bound key; values the star's slot.
 //   k_sort_ghist     every 8-bit digit's histogram in one read of the keys
 //   k_sort_onesweep  one kernel per digit pass: stable in-tile ranking (warp
 //                    match + per-warp counters), tile offsets by decoupled
 //                    look-back, staging through shared memory so runs of one
 //                    digit leave the block as contiguous stores
 // Tiles never straddle clusters, so one launch sorts every cluster of an
-// ensemble independently.  Passes whose digit is identical for every key of a
-// cluster (found from the key range) are skipped for that cluster.
+// ensemble independently.  Only the digits that span a cluster's key range
+// are sorted (7 for radii spanning up to 2^4 binades).
 // k_sort_gather then moves the payload (rnew, m, vrnew, vtnew, id, r, ec_pre)
 // into radial order with 128-bit-aligned SoA loads and drops the escapers
 // (r == SF_INFINITY), which sort last.
@@ -107,24 +108,35 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
                 n += s_cnt[q];
             }
             sc->n_bound = n;
-            // escapers sort after every bound star: the key range must include them
-            const bool esc = (n < N);
-            if (esc) b = inf_bits;
-            if (n == 0) a = b = inf_bits;
-            sb.kmin[ct.x] = 0ull;
-            sb.kmax[ct.x] = b;
-            // digits where every key agrees need no pass: highest differing bit
-            const unsigned long long diff = a ^ b;
-            int bits = diff ? 64 - __clzll((long long)diff) : 0;
+            // sort keys: a bound star's bit pattern minus the smallest one, an
+            // escaper one past the largest (escapers sort after every bound
+            // star, in input order); only the digits that span the range pass
+            unsigned long long top = 0ull;
+            if (n == 0) {
+                a = inf_bits;  // every key the same: nothing to sort
+            } else {
+                top = (b - a) + (n < N ? 1ull : 0ull);
+            }
+            sb.kmin[ct.x] = a;
+            sb.kmax[ct.x] = top;
+            const int bits = top ? 64 - __clzll((long long)top) : 0;
             sb.npass[ct.x] = (bits + 7) / 8;
         }
     }
 }
 
-static __device__ __forceinline__ unsigned long long load_key(const Cluster &C, const Fields &f, const SortBufs &sb,
-                                                              int pass, int cur, long long pos /*0-based*/)
+// The sort key of a radius (k_sort_prep): bits - kmin, escapers kmax.
+static __device__ __forceinline__ unsigned long long radius_key(double r, unsigned long long kmin,
+                                                                unsigned long long kesc)
 {
-    if (pass == 0) return (unsigned long long)__double_as_longlong(f.rnew[C.off + 1 + pos]);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(r);
+    return b == (unsigned long long)__double_as_longlong(CMCG_SF_INFINITY) ? kesc : b - kmin;
+}
+
+static __device__ __forceinline__ unsigned long long load_key(const Cluster &C, const Fields &f, const SortBufs &sb,
+                                                              int pass, int cur, long long pos /*0-based*/, int c)
+{
+    if (pass == 0) return radius_key(f.rnew[C.off + 1 + pos], sb.kmin[c], sb.kmax[c]);
     return (cur ? sb.keys[1] : sb.keys[0])[C.off + pos];
 }
 
@@ -141,13 +153,14 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_ghist(const Cluster *__re
     const int np = sb.npass[ct.x];
     if (np == 0) return;
     const long long N = C.sc->N_MAX_NEW;
+    const unsigned long long kmin = sb.kmin[ct.x], kesc = sb.kmax[ct.x];
     for (int i = threadIdx.x; i < SORT_MAX_PASSES * RADIX; i += SORT_THREADS) (&h[0][0])[i] = 0u;
     __syncthreads();
     const long long base = (long long)ct.y * SORT_T;
     for (int i = threadIdx.x; i < SORT_T; i += SORT_THREADS) {
         const long long pos = base + i;
         if (pos >= N) break;
-        const unsigned long long k = (unsigned long long)__double_as_longlong(f.rnew[C.off + 1 + pos]);
+        const unsigned long long k = radius_key(f.rnew[C.off + 1 + pos], kmin, kesc);
         for (int p = 0; p < np; ++p) atomicAdd(&h[p][(unsigned int)(k >> (8 * p)) & (RADIX - 1)], 1u);
     }
     __syncthreads();
@@ -213,7 +226,7 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
         // warp-striped: warp w owns [w*ITEMS*32, (w+1)*ITEMS*32), item it, lane l -> w*ITEMS*32 + it*32 + l
         const long long pos = base + w * (ITEMS * 32) + it * 32 + lane;
         valid[it] = pos < N;
-        key[it] = valid[it] ? load_key(C, f, sb, pass, cur, pos) : 0ull;
+        key[it] = valid[it] ? load_key(C, f, sb, pass, cur, pos, ct.x) : 0ull;
         val[it] = valid[it] ? (pass == 0 ? (unsigned int)pos : (cur ? sb.vals[1] : sb.vals[0])[C.off + pos]) : 0u;
         dig[it] = (unsigned int)(key[it] >> shift) & (RADIX - 1);
     }

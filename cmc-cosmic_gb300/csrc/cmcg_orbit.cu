@@ -99,8 +99,9 @@ static __device__ __forceinline__ void set_a_b(const OrbitCtx &o, long long k, d
     } else {
         // the divisions by r_k and r_k+1 use the stored reciprocals (div_rcp)
         const double rk = o.r[k], rk1 = o.r[k + 1], ik = o.inv_r[k], ik1 = o.inv_r[k + 1];
-        const double Uk = o.phi[k] + ((rk >= o.rj) ? __dmul_rn(div_rcp(o.mj, rk, ik), o.invN) : o.s.pjd);
-        const double Uk1 = o.phi[k + 1] + ((rk1 >= o.rj) ? __dmul_rn(div_rcp(o.mj, rk1, ik1), o.invN) : o.s.pjd);
+        const long long rjb = dbits(o.rj);  // positive radii compare as their bit patterns
+        const double Uk = o.phi[k] + ((dbits(rk) >= rjb) ? __dmul_rn(div_rcp(o.mj, rk, ik), o.invN) : o.s.pjd);
+        const double Uk1 = o.phi[k + 1] + ((dbits(rk1) >= rjb) ? __dmul_rn(div_rcp(o.mj, rk1, ik1), o.invN) : o.s.pjd);
         const double den = ik1 - ik;
         *a = (Uk1 - Uk) / den;
         *b = (div_rcp(Uk, rk1, ik1) - div_rcp(Uk1, rk, ik)) / den;
@@ -360,6 +361,9 @@ struct SampleSmem {
     int first[ORB_T];  // the first trial of this round the filter did not reject (INT_MAX: none)
     int list[2][ORB_T];
     int wl[ORB_T];     // this round's candidates, one slot per star
+    double wX[ORB_T], wr[ORB_T];  // a candidate's X and r, as its filter pass formed them
+    long long wi[ORB_T];          // and its radius-table interval (-1: not searched)
+    unsigned int wuy[ORB_T];      // and its second draw word
     int n[2], nw;
 };
 
@@ -371,27 +375,49 @@ struct Trial {
     int code;
 };
 
-// Trial k of star slot s, evaluated exactly as the reference does, without
-// writing anything.
+// A trial's draws and radius (cmc_evolution_thr.c:860-870), and the table
+// interval holding r once a search has found it (i = -1 before).
+struct TrialIn {
+    double X, r;
+    long long i;
+    unsigned int ux, uy;
+};
+
+static __device__ __forceinline__ TrialIn trial_input(const Cluster &C, const Scalars *sc, const SampleSmem &sm,
+                                                      int s, int k)
+{
+    const uint4 u = draw_block(C.seed, sc->tcount, SITE_TRIAL, sm.id[s], (unsigned int)(k - 1));
+    TrialIn in;
+    in.X = u01(u.x);
+    const double s0 = 2.0 * in.X - 1.0;
+    in.r = sm.c0[s] + sm.c1[s] * (3.0 * s0 - s0 * s0 * s0);  // 0.5 (rmin + rmax) + 0.25 (rmax - rmin) (...)
+    in.i = -1;
+    in.ux = u.x;
+    in.uy = u.y;
+    return in;
+}
+
+// A trial of star slot s, evaluated exactly as the reference does, without
+// writing anything.  Radii are positive, so they are compared on their bit
+// patterns (integer instructions, as the FP64 comparisons would decide).
 static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scalars *sc, const Fields &f,
-                                                   const SampleSmem &sm, int s, int k, double invN)
+                                                   const SampleSmem &sm, int s, const TrialIn &in, double invN)
 {
     Trial t;
     const long long off = C.off, N_MAX = sc->N_MAX;
-    const double E = sm.E[s], J = sm.J[s], rj = sm.rj[s], mj = sm.mj[s], c1 = sm.c1[s];
-    const uint4 u = draw_block(C.seed, sc->tcount, SITE_TRIAL, sm.id[s], (unsigned int)(k - 1));
-    const double X = u01(u.x);
+    const double E = sm.E[s], J = sm.J[s], mj = sm.mj[s], c1 = sm.c1[s];
+    const double X = in.X, r = in.r;
     const double s0 = 2.0 * X - 1.0;
-    const double g0 = sm.F[s] * u01(u.y);
-    const double r = sm.c0[s] + c1 * (3.0 * s0 - s0 * s0 * s0);
+    const double g0 = sm.F[s] * u01(in.uy);
     // one correctly rounded 1/r serves every division by r below (div_rcp)
     const double ir = __drcp_rn(r);
     int pok = 1;
     const double *rt = f.r + off, *pt = f.phi + off, *it = f.inv_r + off;
+    const long long rb = dbits(r);
     double pot;
-    if (r >= __ldg(rt + 1)) {
-        const long long i = potential_index(rt, N_MAX, r, ridx_of(C, f));
-        if (i > N_MAX || __ldg(rt + i) > r || __ldg(rt + i + 1) < r) {
+    if (rb >= dbits(__ldg(rt + 1))) {
+        const long long i = in.i >= 0 ? in.i : potential_index(rt, N_MAX, r, ridx_of(C, f));
+        if (i > N_MAX || dbits(__ldg(rt + i)) > rb || dbits(__ldg(rt + i + 1)) < rb) {
             pok = 0;
             pot = 0.0;
         } else {
@@ -401,7 +427,7 @@ static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scala
     } else {
         pot = potential_at(rt, pt, it, N_MAX, r, &pok);
     }
-    pot += (r >= rj) ? __dmul_rn(div_rcp(mj, r, ir), invN) : sm.ps[s];
+    pot += (rb >= sm.rjb[s]) ? __dmul_rn(div_rcp(mj, r, ir), invN) : sm.ps[s];
     t.X = X;
     t.r = r;
     t.ir = ir;
@@ -449,19 +475,17 @@ static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scala
 // Radii at or below r_1, a failed search, neighbours within 4 ulps (whose
 // reciprocals may round equal) and non-finite values are unsure.
 static __device__ __forceinline__ int filter_trial(const Cluster &C, const Scalars *sc, const Fields &f,
-                                                   const SampleSmem &sm, int s, int k)
+                                                   const SampleSmem &sm, int s, TrialIn &in)
 {
-    const uint4 u = draw_block(C.seed, sc->tcount, SITE_TRIAL, sm.id[s], (unsigned int)(k - 1));
     const float fc1 = sm.fc1[s];
-    if (u.x == 0u || !(fc1 > 0.0f)) return TRIAL_UNSURE;
-    const double X = u01(u.x);
-    const double s0 = 2.0 * X - 1.0;
-    const double r = sm.c0[s] + sm.c1[s] * (3.0 * s0 - s0 * s0 * s0);
+    if (in.ux == 0u || !(fc1 > 0.0f)) return TRIAL_UNSURE;
+    const double r = in.r;
     const long long off = C.off, N_MAX = sc->N_MAX;
     const double *rt = f.r + off;
     const long long rb = dbits(r);
     if (rb <= dbits(__ldg(rt + 1))) return TRIAL_UNSURE;
     const long long i = potential_index(rt, N_MAX, r, ridx_of(C, f));
+    in.i = i;
     if (i < 1 || i > N_MAX) return TRIAL_UNSURE;
     const long long bi = dbits(__ldg(rt + i)), bi1 = dbits(__ldg(rt + i + 1));
     if (bi >= rb || bi1 < rb || bi1 - bi <= 4) return TRIAL_UNSURE;
@@ -482,9 +506,9 @@ static __device__ __forceinline__ int filter_trial(const Cluster &C, const Scala
     if (Qhi < 0.0f) return TRIAL_ACCEPT;
     if (!(Qlo > 0.0f)) return TRIAL_UNSURE;
     // 1 - s0^2 = 4 X (1 - X) = u (2^32 - u) 2^-62
-    const float w = __fmul_rn(__fmul_rn((float)u.x, (float)(0u - u.x)), 0x1p-62f);
+    const float w = __fmul_rn(__fmul_rn((float)in.ux, (float)(0u - in.ux)), 0x1p-62f);
     const float drds = __fmul_rn(__fmul_rn(3.0f, fc1), w);
-    const float g0 = __fmul_rn(sm.fF[s], __fmul_rn((float)u.y, 0x1p-32f));
+    const float g0 = __fmul_rn(sm.fF[s], __fmul_rn((float)in.uy, 0x1p-32f));
     const float eta = __fadd_rn(0x1p-17f, __fmul_rn(0x1p-48f, __frcp_rn(w)));
     const float g2 = __fmul_rn(g0, g0), d2 = __fmul_rn(drds, drds);
     if (!(g2 <= 1e30f) || !(d2 <= 1e30f) || !(d2 > 1e-30f)) return TRIAL_UNSURE;
@@ -689,22 +713,28 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
         }
         // 1. the filter on each star's next m trials
         int slot = -1, k = 0, kb = 0;
+        TrialIn in;
         if (t < n * m) {
             slot = sm.list[cur][t / m];
             kb = sm.next[slot];
             k = kb + t % m;
             if (k <= n_try) {
-                const int dec = filter_trial(C, sc, f, sm, slot, k);
+                in = trial_input(C, sc, sm, slot, k);
+                const int dec = filter_trial(C, sc, f, sm, slot, in);
                 if (dec != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
-                if (check && dec != TRIAL_UNSURE && eval_trial(C, sc, f, sm, slot, k, invN).code != dec)
+                if (check && dec != TRIAL_UNSURE && eval_trial(C, sc, f, sm, slot, in, invN).code != dec)
                     set_error(sc, CMCG_ERR_FILTER, j0 + slot);
             }
         }
         __syncthreads();
-        // 2. candidates listed; stars whose m trials were all rejected go on
+        // 2. candidates listed (with their inputs); stars whose m trials were all rejected go on
         if (slot >= 0) {
             const int fst = sm.first[slot];
             if (k == fst) {
+                sm.wX[slot] = in.X;
+                sm.wr[slot] = in.r;
+                sm.wi[slot] = in.i;
+                sm.wuy[slot] = in.uy;
                 sm.wl[atomicAdd(&sm.nw, 1)] = slot;
             } else if (t % m == 0 && fst == INT_MAX) {
                 if (kb + m - 1 >= n_try) {
@@ -720,7 +750,13 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
         if (t < sm.nw) {
             const int s = sm.wl[t];
             const int kk = sm.first[s];
-            const Trial tr = eval_trial(C, sc, f, sm, s, kk, invN);
+            TrialIn cin;
+            cin.X = sm.wX[s];
+            cin.r = sm.wr[s];
+            cin.i = sm.wi[s];
+            cin.uy = sm.wuy[s];
+            cin.ux = 0u;  // not used by the exact evaluation
+            const Trial tr = eval_trial(C, sc, f, sm, s, cin, invN);
             if (tr.code == TRIAL_ACCEPT) {
                 commit_trial(C, sc, f, sm, s, off + j0 + s, tr, &max_rad);
             } else if (tr.code != TRIAL_REJECT) {

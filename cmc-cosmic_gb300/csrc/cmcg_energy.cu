@@ -81,7 +81,11 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
         if (slot < EXCESS_CAP) eb.list[(size_t)ct.x * EXCESS_CAP + slot] = i;
     } else {
         eb.a[g] = -1.0;
-        const double alpha = sqrt(vnew2 / (sqr(vr) + sqr(vt)));
+        // alpha = sqrt(vnew2 / v^2) (cmc_utils.c:291) as vnew2 rsqrt(vnew2 v^2): one
+        // reciprocal square root instead of a division and a square root, within
+        // 4 ulps of the reference's value
+        const double v2 = sqr(vr) + sqr(vt);
+        const double alpha = vnew2 * rsqrt(vnew2 * v2);
         vr *= alpha;
         vt *= alpha;
         f.vr[g] = vr;
@@ -281,13 +285,14 @@ __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict
         P += ph * m * madhoc;
         P += pc;
     }
-    const double tK = block_sum<EN_THREADS>(K, red);
-    const double tP = block_sum<EN_THREADS>(P, red);
+    __shared__ double s_KP[EN_THREADS / 32][2];
+    double KP[2] = {K, P};
+    block_sums<EN_THREADS>(KP, s_KP);
     __shared__ int s_last;
     if (threadIdx.x == 0) {
         double *slot = partials + (size_t)blockIdx.x * 2;
-        slot[0] = tK;
-        slot[1] = tP;
+        slot[0] = KP[0];
+        slot[1] = KP[1];
     }
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
         const double sK = reduce_partials_sum<EN_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], 2, 0, red);

@@ -555,8 +555,20 @@ __global__ void __launch_bounds__(ORB_T) k_orbit_pre(const Cluster *__restrict__
     const double E = Ej + ps;
     int slot = PQ_POSITIVE;
     if (!(mj < CMCG_ZERO) && E < 0.0) {
-        const OrbitCtx o = make_orbit_ctx(C, f, j, E, f.J[g], rj, mj, ps);
-        if (fq_sign(o, j) <= 0) {
+        // the FP32 stage from the few floats it reads; the whole certified test
+        // (and its context) only when that stage is undecided
+        QF32 q;
+        q.E = (float)E;
+        q.El = (float)(E - (double)q.E);
+        q.J = (float)f.J[g];
+        q.mjN = (float)(mj * sc->madhoc);
+        q.pj = (float)ps;
+        int sg = fq_sign_f32(q, __ldg(f.rphif + g), true);
+        if (sg == 0) {
+            const OrbitCtx o = make_orbit_ctx(C, f, j, E, f.J[g], rj, mj, ps);
+            sg = fq_sign(o, j);
+        }
+        if (sg <= 0) {
             const unsigned int e = atomicAdd(pq.count, 1u);
             if (e < PQ_CAP) {
                 pq.cl[e] = ct.x;

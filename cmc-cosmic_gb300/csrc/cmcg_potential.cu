@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
 {
     __shared__ double s_w[POT_THREADS / 32];
     __shared__ double s_lastinv[POT_THREADS / 32];
-    __shared__ double red[POT_THREADS / 32];
+    __shared__ double s_S[POT_THREADS / 32][4];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
@@ -118,16 +118,14 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
         td += d[i];
         tm_ += mm[i];
     }
-    const double Sq = block_sum<POT_THREADS>(tq, red);
-    const double Sd = block_sum<POT_THREADS>(td, red);
-    const double Sc = block_sum<POT_THREADS>(tc, red);
-    const double Sm = block_sum<POT_THREADS>(tm_, red);
+    double S[4] = {tq, td, tc, tm_};
+    block_sums<POT_THREADS>(S, s_S);
     if (t == 0) {
         double *a = pb.agg + (size_t)blockIdx.x * POT_AGG;
-        a[0] = Sq;
-        a[1] = Sd;
-        a[2] = Sc;
-        a[3] = Sm;
+        a[0] = S[0];
+        a[1] = S[1];
+        a[2] = S[2];
+        a[3] = S[3];
         a[4] = bad ? 1.0 : 0.0;
     }
 }

@@ -60,7 +60,26 @@ __global__ void __launch_bounds__(128) k_timestep(const Cluster *__restrict__ cl
             if (si < s_lo) continue;
             const long long simin = si - p, simax = simin + (2 * p - 1);
             double Mv2ave = 0.0, Mave = 0.0, M2ave = 0.0;
-            for (long long k = simin; k <= simax; k++) {
+            // the reference's sequential sums; the loads of eight stars are
+            // issued ahead of their additions so that their latencies overlap
+            long long k = simin;
+            for (; k + 7 <= simax; k += 8) {
+                double mq[8], aq[8], bq[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    mq[q] = m[k + q];
+                    aq[q] = vr[k + q];
+                    bq[q] = vt[k + q];
+                }
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const double tmp = mq[q] * madhoc;
+                    Mv2ave += tmp * (sqr(aq[q]) + sqr(bq[q]));
+                    Mave += tmp;
+                    M2ave += sqr(tmp);
+                }
+            }
+            for (; k <= simax; k++) {
                 const double tmp = m[k] * madhoc;
                 Mv2ave += tmp * (sqr(vr[k]) + sqr(vt[k]));
                 Mave += tmp;

@@ -61,7 +61,7 @@ struct cmcg_ctx {
     int ridx_Bmax = 0;
     Ec3Bufs eb{};
     double *d_query = nullptr;
-    TileTable t128, t256, t1024, t2048, t5120;
+    TileTable t128, t256, t1024, t2048;
     void *arena = nullptr;
     size_t arena_bytes = 0;
     int relax_fp32 = 0;
@@ -199,7 +199,7 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     np = std::max(np, (size_t)c->t128.ntiles * ORB_NPART);
     np = std::max(np, (size_t)c->t2048.ntiles * 4);
     np = std::max(np, (size_t)c->t256.ntiles * 2);
-    np = std::max(np, (size_t)c->t5120.ntiles * 1);
+    np = std::max(np, (size_t)c->t1024.ntiles * 1);
     c->partials = cv.take<double>(np);
     c->tickets = cv.take<unsigned int>(c->ncl);
     c->gbar = cv.take<unsigned int>(2);
@@ -211,8 +211,8 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->d_sc = cv.take<Scalars>(c->ncl);
     c->d_cls = cv.take<Cluster>(c->ncl);
     c->d_query = cv.take<double>(2);
-    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t5120};
-    for (int i = 0; i < 5; ++i) {
+    TileTable *tts[4] = {&c->t128, &c->t256, &c->t1024, &c->t2048};
+    for (int i = 0; i < 4; ++i) {
         tts[i]->d_tiles = cv.take<int2>(tabs[i].size());
         tts[i]->d_first = cv.take<int>(c->ncl);
         tts[i]->d_count = cv.take<int>(c->ncl);
@@ -292,12 +292,11 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         c->ridx_total += ridx_buckets(capacity[k]) + 1;
         c->ridx_Bmax = std::max(c->ridx_Bmax, ridx_buckets(capacity[k]));
     }
-    std::vector<int2> tabs[5];
+    std::vector<int2> tabs[4];
     build_table(c->t128, c->cap, ORB_T, tabs[0]);
     build_table(c->t256, c->cap, RELAX_T, tabs[1]);
     build_table(c->t1024, c->cap, POT_T, tabs[2]);
     build_table(c->t2048, c->cap, SORT_T, tabs[3]);
-    build_table(c->t5120, c->cap, TS_T, tabs[4]);
     size_t bytes = 0;
     carve_all(c, nullptr, tabs, &bytes);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -344,8 +343,8 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         ridx_off += C.ridx_B + 1;
     }
     CK(cudaMemcpyAsync(c->d_cls, c->h_cls.data(), nclusters * sizeof(Cluster), cudaMemcpyHostToDevice, c->stream));
-    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t5120};
-    for (int i = 0; i < 5; ++i) {
+    TileTable *tts[4] = {&c->t128, &c->t256, &c->t1024, &c->t2048};
+    for (int i = 0; i < 4; ++i) {
         CK(cudaMemcpyAsync(tts[i]->d_tiles, tabs[i].data(), tabs[i].size() * sizeof(int2), cudaMemcpyHostToDevice,
                            c->stream));
         CK(cudaMemcpyAsync(tts[i]->d_first, tts[i]->first.data(), nclusters * sizeof(int), cudaMemcpyHostToDevice,
@@ -547,7 +546,7 @@ static int L_end(cmcg_ctx *c)
 static int L_timestep(cmcg_ctx *c)
 {
     fam_begin(c, F_TIMESTEP);
-    k_timestep<<<c->t5120.ntiles, 128, 0, c->stream>>>(c->d_cls, c->t5120.view(), c->f, c->partials, c->tickets);
+    k_timestep<<<c->t1024.ntiles, TS_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->f, c->partials, c->tickets);
     fam_end(c);
     c->launches += 1;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;

@@ -6,13 +6,14 @@ namespace cmcg {
 
 // ---- tile sizes (stars per block) of the launch families
 constexpr int RELAX_T = 256, RELAX_THREADS = 128, PMAX = 64, RELAX_NPART = 17;
-constexpr int TS_T = 5120;
+constexpr int TS_T = 1024, TS_THREADS = 128;  // time step: the potential's 1024-star tiles
 constexpr int ORB_T = 128, ORB_NPART = 5;
 constexpr int TID_T = 2048, TID_THREADS = 256, TID_NPART = 4;
 constexpr int SORT_THREADS = 256, SORT_ITEMS = 8, SORT_T = SORT_THREADS * SORT_ITEMS, RADIX = 256;
 constexpr int OS_THREADS = 512;  // onesweep digit pass: 4 keys per thread, 32 warps per SM
 constexpr int GATHER_T = 256;
 constexpr int POT_THREADS = 256, POT_ITEMS = 4, POT_T = POT_THREADS * POT_ITEMS;
+static_assert(TS_T == POT_T, "the time step runs on the potential's tile table");
 constexpr int EC3_T = 256, EN_T = 2048, EN_THREADS = 256;
 constexpr int EXCESS_CAP = 4096;      // listed unphysical predictions per cluster (else full replay)
 constexpr int EC3_FIX_THREADS = 512;

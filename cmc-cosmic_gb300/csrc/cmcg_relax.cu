@@ -1,8 +1,9 @@
 // cmcg_relax.cu -- time step and the fused relaxation kernel.
 //
 // k_timestep restates simul_relax_new (cmc_dynamics_helper.c:2526-2579) and
-// calc_timestep (cmc_utils.c:2132-2148): one thread per 2p-star block, the
-// block sums taken in the reference's order, so Dt is bit-identical.
+// calc_timestep (cmc_utils.c:2132-2148): the per-star terms are formed by all
+// threads, then one thread per 2p-star window adds them in the reference's
+// order, so Dt is bit-identical.
 //
 // k_relax restates dynamics_apply (cmc_dynamics.c:17-542, relaxation branch
 // 427-497) with calc_encounter_dyns, calc_n_local and set_star_EJ
@@ -37,10 +38,17 @@ static __device__ __forceinline__ double n_local_at(const double *__restrict__ r
 }
 
 // ------------------------------------------------------------ time step --
-__global__ void __launch_bounds__(128) k_timestep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                  double *partials, unsigned int *tickets)
+// A block owns the windows (2p stars each, centres si = 1 + p + 2 p w) whose
+// centre lies in its 1024-star tile.  All threads form the per-star terms
+// m/N (vr^2 + vt^2), m/N and (m/N)^2 of those windows' stars into shared
+// memory; then one thread per window adds its terms in the reference's
+// order, so every sum, and Dt, is bit-identical.
+__global__ void __launch_bounds__(TS_THREADS) k_timestep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                         double *partials, unsigned int *tickets)
 {
-    __shared__ double red[4];
+    constexpr int LMAX = TS_T + 2 * PMAX;  // stars of the windows centred in one tile
+    __shared__ double s_mv[LMAX], s_mm[LMAX], s_m2[LMAX];
+    __shared__ double red[TS_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
@@ -50,40 +58,29 @@ __global__ void __launch_bounds__(128) k_timestep(const Cluster *__restrict__ cl
     const double *r = f.r + C.off, *m = f.m + C.off, *vr = f.vr + C.off, *vt = f.vt + C.off;
     double dtmin = INFINITY;
     if (C.RELAXATION && N >= 2 * p + 2) {
-        // windows si = 1 + p + 2p w whose si lies in this block's star range
+        // windows w with s_lo <= si < min(s_hi, N + 1 - p)
         const long long s_lo = 1 + (long long)ct.y * TS_T, s_hi = s_lo + TS_T;
-        long long w0 = (s_lo - 1 - p + 2 * p - 1) / (2 * p);
-        if (s_lo - 1 - p < 0) w0 = 0;
-        for (long long w = w0 + threadIdx.x;; w += blockDim.x) {
+        const long long lim = s_hi < N + 1 - p ? s_hi : N + 1 - p;
+        const long long w0 = (s_lo - 1 - p <= 0) ? 0 : (s_lo - 1 - p + 2 * p - 1) / (2 * p);
+        const long long w1 = (lim - 1 - p <= 0) ? -1 : (lim - 1 - p + 2 * p - 1) / (2 * p) - 1;
+        const long long k0 = 1 + 2 * p * w0;  // first star of window w0
+        const int L = w1 >= w0 ? (int)(2 * p * (w1 - w0 + 1)) : 0;
+        for (int i = threadIdx.x; i < L; i += TS_THREADS) {
+            const long long k = k0 + i;
+            const double tmp = m[k] * madhoc;
+            s_mv[i] = tmp * (sqr(vr[k]) + sqr(vt[k]));
+            s_mm[i] = tmp;
+            s_m2[i] = sqr(tmp);
+        }
+        __syncthreads();
+        for (long long w = w0 + threadIdx.x; w <= w1; w += TS_THREADS) {
             const long long si = 1 + p + 2 * p * w;
-            if (si >= s_hi || !(si < N + 1 - p)) break;
-            if (si < s_lo) continue;
-            const long long simin = si - p, simax = simin + (2 * p - 1);
+            const int b = (int)(2 * p * (w - w0));
             double Mv2ave = 0.0, Mave = 0.0, M2ave = 0.0;
-            // the reference's sequential sums; the loads of eight stars are
-            // issued ahead of their additions so that their latencies overlap
-            long long k = simin;
-            for (; k + 7 <= simax; k += 8) {
-                double mq[8], aq[8], bq[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    mq[q] = m[k + q];
-                    aq[q] = vr[k + q];
-                    bq[q] = vt[k + q];
-                }
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const double tmp = mq[q] * madhoc;
-                    Mv2ave += tmp * (sqr(aq[q]) + sqr(bq[q]));
-                    Mave += tmp;
-                    M2ave += sqr(tmp);
-                }
-            }
-            for (; k <= simax; k++) {
-                const double tmp = m[k] * madhoc;
-                Mv2ave += tmp * (sqr(vr[k]) + sqr(vt[k]));
-                Mave += tmp;
-                M2ave += sqr(tmp);
+            for (int q = 0; q < 2 * p; ++q) {
+                Mv2ave += s_mv[b + q];
+                Mave += s_mm[b + q];
+                M2ave += s_m2[b + q];
             }
             Mv2ave /= (double)(2 * p);
             Mave /= (double)(2 * p);
@@ -98,11 +95,11 @@ __global__ void __launch_bounds__(128) k_timestep(const Cluster *__restrict__ cl
     }
     // exact min over blocks (min is order independent)
     __shared__ int s_last;
-    const double bmin = -block_max<128>(-dtmin, red);
+    const double bmin = -block_max<TS_THREADS>(-dtmin, red);
     // min over blocks as the negated max of negated block minima (order independent)
     if (threadIdx.x == 0) partials[blockIdx.x] = -bmin;
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
-        const double Dtmin = -reduce_partials_max<128>(partials, tm.first[ct.x], tm.count[ct.x], 1, 0, red);
+        const double Dtmin = -reduce_partials_max<TS_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], 1, 0, red);
         if (threadIdx.x == 0) {
             double Dt = C.RELAXATION ? Dtmin : INFINITY;
             // GetTimeStep, cmc_evolution_thr.c:420: all other time scales are infinite

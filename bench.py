@@ -39,9 +39,9 @@ UNIT = "star-updates/s"
 ALG_BYTES = {"sort": 116, "potential": 24, "relax": 72, "orbit": 80, "ec3": 72, "energy": 56,
              "timestep": 24, "tidal": 16, "begin": 0, "end": 0}
 # DRAM bytes per star of one launch, dram__bytes_read.sum + dram__bytes_write.sum
-# from one ncu capture, scaled by stars: k_orbit 956.0 MB over 1,913,988 stars
-# (King W0=6 + Kroupa, N=2e6; profiles/orbit_king6_kroupa_2e6.md), k_relax64
-# 56.9 MB over 962,913 stars (profiles/kernels_king6_kroupa_1e6.md)
+# from one ncu capture (summaries under profiles/), scaled by stars: k_orbit
+# 956.0 MB over 1,913,988 stars (King W0=6 + Kroupa, N=2e6), k_relax64 56.9 MB
+# over 962,913 stars (the same model at N=1e6)
 NCU_TRAFFIC_PER_STAR = {"orbit": 956.0e6 / 1913988, "relax": 56.9e6 / 962913}
 # share of cycles the FP64 pipe was busy in the same captures: the kernels'
 # real bound on GB300 (1/64-rate FP64), reported beside the HBM roofline

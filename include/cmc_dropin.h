@@ -8,9 +8,9 @@
  * scalars.  This library cannot include the reference's headers, so the host
  * describes where those live once, with cmcx_bind(): the base of star[],
  * sizeof(star_t) and offsetof(star_t, field) of the fields the hot path
- * reads or writes, and pointers to the arrays and scalars.  The glue a
- * maintainer compiles with the reference's headers is shown in
- * INTEGRATION.md.
+ * reads or writes, and pointers to the arrays and scalars.  The glue is one
+ * small C file compiled with the reference's headers: it fills cmcx_host with
+ * &star[0], sizeof(star_t), offsetof(star_t, ...) and the globals' addresses.
  *
  * Ownership and sync.  cmcx_bind() copies star[1..N] to the GPU, which is
  * then authoritative for the hot fields.  With sync_each = 1 (the default

@@ -32,6 +32,7 @@ CUDA_SOURCES = [
     "cmcg_phi.cu",
     "cmcg_energy.cu",
     "cmcg_noalloc.cu",
+    "cmcg_diag.cu",
 ]
 C_SOURCES = ["cmcg_ic.c"]
 # the reference-named drop-in layer: a second library on the public C ABI

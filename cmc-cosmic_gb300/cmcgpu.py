@@ -52,6 +52,54 @@ class Params(C.Structure):
     ]
 
 
+CMCG_MASS_PC_MAX = 64
+# the reference's example MASS_PC (examples/KingProfile.ini, PlummerSphere.ini)
+MASS_PC = (0.0001, 0.0003, 0.0005, 0.0007, 0.0009, 0.001, 0.003, 0.005, 0.007, 0.009, 0.01, 0.03, 0.05, 0.07, 0.09,
+           0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 0.99)
+
+
+class Diag(C.Structure):
+    """cmcg_diag (cmcgpu.h)."""
+    _fields_ = ([("TotalTime", C.c_double), ("Dt", C.c_double), ("tcount", C.c_long), ("N_MAX", C.c_long)]
+                + [(n, C.c_double) for n in ("Mtotal", "Etot", "KE", "PE", "E_cenma", "Eescaped", "Eoops", "max_r")]
+                + [("nave", C.c_long), ("rh", C.c_double)]
+                + [(n, C.c_double) for n in ("rho_0", "v0_rms", "core_radius", "rc_nb", "m_ave", "n_central",
+                                            "rc_spitzer", "N_core", "N_core_nb", "Trc")]
+                + [("n_pc", C.c_int), ("n_set", C.c_int)]
+                + [(n, C.c_double * CMCG_MASS_PC_MAX) for n in ("mass_pc", "mass_r", "ave_mass_r", "no_star_r",
+                                                                "densities_r", "ke_rad_r", "ke_tan_r", "v2_rad_r",
+                                                                "v2_tan_r")])
+
+    def arr(self, name: str):
+        return np.array(getattr(self, name)[:self.n_pc])
+
+
+def _fmt(fn, *args) -> str:
+    buf = C.create_string_buffer(1 << 16)
+    n = fn(*args, buf, len(buf))
+    if n < 0:
+        raise RuntimeError("format buffer too small")
+    return buf.value.decode()
+
+
+def dyn_header() -> str:
+    return _fmt(lib().cmcg_format_dyn_header)
+
+
+def lagrad_header(mass_pc=MASS_PC) -> str:
+    pc = np.ascontiguousarray(mass_pc, dtype=np.float64)
+    return _fmt(lib().cmcg_format_lagrad_header, pc.ctypes.data, len(pc))
+
+
+def dyn_line(start: "Diag", end: "Diag") -> str:
+    """dyn.dat line: core quantities from `start` (before the step), the rest from `end`."""
+    return _fmt(lib().cmcg_format_dyn_line, C.byref(start), C.byref(end))
+
+
+def lagrad_line(d: "Diag") -> str:
+    return _fmt(lib().cmcg_format_lagrad_line, C.byref(d))
+
+
 class ICSpec(C.Structure):
     _fields_ = [("model", C.c_int), ("N", C.c_long), ("w0", C.c_double), ("imf", C.c_int),
                 ("binary_fraction", C.c_double), ("seed", C.c_uint64)]
@@ -164,6 +212,15 @@ def lib() -> C.CDLL:
         L.cmcg_draw.argtypes = [C.c_uint64, l, i, C.c_int64, C.c_uint32, i]
         L.cmcg_draw.restype = d
         L.cmcg_sign_stages.argtypes = [vp, vp, vp, vp, d, vp, vp, l, vp]
+        L.cmcg_diagnostics.argtypes = [vp, i, vp, i, i, d, vp]
+        L.cmcg_format_dyn_line.argtypes = [vp, vp, vp, l]
+        L.cmcg_format_dyn_line.restype = l
+        L.cmcg_format_lagrad_line.argtypes = [vp, vp, l]
+        L.cmcg_format_lagrad_line.restype = l
+        L.cmcg_format_dyn_header.argtypes = [vp, l]
+        L.cmcg_format_dyn_header.restype = l
+        L.cmcg_format_lagrad_header.argtypes = [vp, i, vp, l]
+        L.cmcg_format_lagrad_header.restype = l
         L.cmcg_sort_radii_noalloc.argtypes = [vp, l, vp, C.POINTER(l), vp]
         L.cmcg_put_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.cmcg_get_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
@@ -314,6 +371,14 @@ class Context:
         v = C.c_double()
         self._check(lib().cmcg_potential(self._h, cluster, float(r), C.byref(v)), "potential")
         return v.value
+
+    def diagnostics(self, cluster: int = 0, mass_pc=None, bh_include: int = 1, minimum_r: float = 0.0) -> "Diag":
+        """The dyn.dat / lagrad.dat quantities of the cluster's current state (cmcg_diagnostics)."""
+        pc = np.ascontiguousarray(MASS_PC if mass_pc is None else mass_pc, dtype=np.float64)
+        d = Diag()
+        self._check(lib().cmcg_diagnostics(self._h, cluster, pc.ctypes.data, len(pc), int(bh_include),
+                                           float(minimum_r), C.byref(d)), "diagnostics")
+        return d
 
     # -- phases (reference names)
     def initialize(self):

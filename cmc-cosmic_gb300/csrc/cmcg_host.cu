@@ -6,6 +6,7 @@
 // partial sums.  Nothing is allocated while stepping.
 #include <algorithm>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -61,6 +62,7 @@ struct cmcg_ctx {
     int ridx_Bmax = 0;
     Ec3Bufs eb{};
     double *d_query = nullptr;
+    DiagDev *d_diag = nullptr;
     TileTable t128, t256, t1024, t2048;
     void *arena = nullptr;
     size_t arena_bytes = 0;
@@ -211,6 +213,7 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->d_sc = cv.take<Scalars>(c->ncl);
     c->d_cls = cv.take<Cluster>(c->ncl);
     c->d_query = cv.take<double>(2);
+    c->d_diag = cv.take<DiagDev>(1);
     TileTable *tts[4] = {&c->t128, &c->t256, &c->t1024, &c->t2048};
     for (int i = 0; i < 4; ++i) {
         tts[i]->d_tiles = cv.take<int2>(tabs[i].size());
@@ -789,6 +792,154 @@ int cmcg_kernel_time(cmcg_ctx *c, const char *family, double *ms_total, long *la
         }
     }
     return CMCG_ERR_ARG;
+}
+
+int cmcg_diagnostics(cmcg_ctx *c, int k, const double *mass_pc, int n_pc, int bh_include, double minimum_r,
+                     cmcg_diag *out)
+{
+    if (!c || k < 0 || k >= c->ncl || !out || n_pc < 0 || n_pc > CMCG_MASS_PC_MAX || (n_pc > 0 && !mass_pc))
+        return CMCG_ERR_ARG;
+    static_assert(CMCG_MASS_PC_MAX == DIAG_PC_MAX, "one limit on the mass fractions");
+    for (int i = 0; i < n_pc; ++i)
+        if (!(mass_pc[i] >= 0.0) || (i > 0 && !(mass_pc[i] >= mass_pc[i - 1]))) return CMCG_ERR_ARG;
+    DiagDev h;
+    memset(&h, 0, sizeof(h));
+    h.n_pc = n_pc;
+    h.bh_include = bh_include ? 1 : 0;
+    h.minimum_r = minimum_r;
+    h.status = CMCG_ERR_STATE;  // cleared by the last block of k_diag_central
+    for (int i = 0; i < n_pc; ++i) h.pc[i] = mass_pc[i];
+    CK(cudaMemcpyAsync(c->d_diag, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    const Tiles tv = c->t1024.view();
+    const int b0 = c->t1024.first[k], nt = c->t1024.count[k];
+    DiagScratch ds;
+    ds.col[0] = c->pb.sapx;
+    ds.col[1] = c->pb.mapx;
+    ds.col[2] = c->pb.papx;
+    ds.col[3] = c->pb.t;
+    ds.col[4] = reinterpret_cast<double *>(c->sb.keys[0]);
+    k_diag_sum<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, b0, c->partials);
+    k_diag_carry<<<1, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, k, b0, nt, c->partials);
+    k_diag_prefix<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, b0, c->partials, ds);
+    k_diag_find<<<1, POT_THREADS, 0, c->stream>>>(c->d_cls, c->f, k, ds, c->d_diag);
+    k_diag_central<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, k, b0, nt, c->partials, c->tickets, ds,
+                                                      c->d_diag);
+    CK(cudaGetLastError());
+    Scalars sc;
+    CK(cudaMemcpyAsync(&h, c->d_diag, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&sc, c->d_sc + k, sizeof(sc), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    memset(out, 0, sizeof(*out));
+    out->TotalTime = sc.TotalTime;
+    out->Dt = sc.Dt;
+    out->tcount = (long)sc.tcount;
+    out->N_MAX = (long)sc.N_MAX;
+    out->Mtotal = sc.Mtotal;
+    out->Etot = sc.Etot;
+    out->KE = sc.KE;
+    out->PE = sc.PE;
+    out->E_cenma = sc.cenma_E;
+    out->Eescaped = sc.Eescaped;
+    out->Eoops = sc.Eoops;
+    out->max_r = sc.max_r;
+    out->nave = (long)h.nave;
+    out->rh = h.rh;
+    out->rho_0 = h.rho;
+    out->v0_rms = h.v_rms;
+    out->core_radius = h.rc;
+    out->rc_nb = h.rc_nb;
+    out->m_ave = h.m_ave;
+    out->n_central = h.n;
+    out->rc_spitzer = h.rc_spitzer;
+    out->N_core = h.N_core;
+    out->N_core_nb = h.N_core_nb;
+    out->Trc = h.Trc;
+    out->n_pc = n_pc;
+    out->n_set = h.n_set;
+    for (int i = 0; i < n_pc; ++i) {
+        out->mass_pc[i] = mass_pc[i];
+        out->mass_r[i] = h.mass_r[i];
+        out->ave_mass_r[i] = h.ave_mass_r[i];
+        out->no_star_r[i] = h.no_star_r[i];
+        out->densities_r[i] = h.densities_r[i];
+        out->ke_rad_r[i] = h.ke_rad_r[i];
+        out->ke_tan_r[i] = h.ke_tan_r[i];
+        out->v2_rad_r[i] = h.v2_rad_r[i];
+        out->v2_tan_r[i] = h.v2_tan_r[i];
+    }
+    return h.status ? h.status : CMCG_OK;
+}
+
+// snprintf into buf at *len; false once the buffer is full
+static bool append(char *buf, long cap, long *len, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    const int n = vsnprintf(buf + *len, (size_t)(cap - *len), fmt, ap);
+    va_end(ap);
+    if (n < 0 || *len + n >= cap) return false;
+    *len += n;
+    return true;
+}
+
+long cmcg_format_dyn_line(const cmcg_diag *a, const cmcg_diag *d, char *buf, long cap)
+{
+    if (!a || !d || !buf || cap < 1) return -1;
+    long len = 0;
+    buf[0] = 0;
+    // PrintFileOutput, cmc_io.c:320-323; without binaries and stellar evolution
+    // Etotal.Eint, Etotal.Eb, Ebescaped, Eintescaped, DMse and DMrejuv are 0
+    const double z = 0.0;
+    if (!append(buf, cap, &len,
+                "%.8g %.8g %ld %ld %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g "
+                "%.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g\n",
+                d->TotalTime, d->Dt, d->tcount, d->N_MAX, d->Mtotal, -2.0 * d->KE / d->PE, a->N_core,
+                a->core_radius, d->max_r, d->Etot, d->KE, d->PE, z, z, d->E_cenma, d->Eescaped, z, z, d->Eoops,
+                d->Etot + d->Eoops, d->rh, a->rho_0, a->rc_spitzer, a->v0_rms, a->rc_nb, z, z, a->N_core_nb))
+        return -1;
+    return len;
+}
+
+long cmcg_format_lagrad_line(const cmcg_diag *d, char *buf, long cap)
+{
+    if (!d || !buf || cap < 1) return -1;
+    long len = 0;
+    buf[0] = 0;
+    if (!append(buf, cap, &len, "%.9e ", d->TotalTime)) return -1;
+    for (int i = 0; i < d->n_pc; ++i)
+        if (!append(buf, cap, &len, "%e ", d->mass_r[i])) return -1;
+    if (!append(buf, cap, &len, "\n")) return -1;
+    return len;
+}
+
+long cmcg_format_dyn_header(char *buf, long cap)
+{
+    if (!buf || cap < 1) return -1;
+    long len = 0;
+    buf[0] = 0;
+    // cmc_io.c:2346-2347
+    if (!append(buf, cap, &len, "# Dynamical information [code units]\n") ||
+        !append(buf, cap, &len,
+                "#1:t #2:Dt #3:tcount #4:N #5:M #6:VR #7:N_c #8:r_c #9:r_max #10:Etot #11:KE #12:PE "
+                "#13:Etot_int #14:Etot_bin #15:E_cenma #16:Eesc #17:Ebesc #18:Eintesc #19:Eoops #20:Etot+Eoops "
+                "#21:r_h #22:rho_0 #23:rc_spitzer #24:v0_rms #25:rc_nb #26.DMse(MSUN) #27.DMrejuv(MSUN) "
+                "#28.N_c_nb\n"))
+        return -1;
+    return len;
+}
+
+long cmcg_format_lagrad_header(const double *mass_pc, int n_pc, char *buf, long cap)
+{
+    if (!buf || cap < 1 || n_pc < 0 || (n_pc > 0 && !mass_pc)) return -1;
+    long len = 0;
+    buf[0] = 0;
+    // cmc_io.c:2294, 2306, 2319, 2332
+    if (!append(buf, cap, &len, "# Lagrange radii [code units]\n") || !append(buf, cap, &len, "#1:t"))
+        return -1;
+    for (long i = 0; i < n_pc; ++i)
+        if (!append(buf, cap, &len, " %ld:r(%g)", i + 2, mass_pc[i])) return -1;
+    if (!append(buf, cap, &len, "\n")) return -1;
+    return len;
 }
 
 int cmcg_potential(cmcg_ctx *c, int k, double r, double *out)

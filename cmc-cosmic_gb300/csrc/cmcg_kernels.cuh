@@ -131,4 +131,35 @@ __global__ void k_ec3_fix(const Cluster *cls, Fields f, Ec3Bufs eb, int ncluster
 __global__ void k_energy(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets);
 __global__ void k_potential_query(const Cluster *cls, Fields f, int c, double x, double *out);
 
+// ---- step diagnostics of dyn.dat and lagrad.dat (cmcg_diag.cu)
+constexpr int DIAG_PC_MAX = 64, DIAG_COLS = 5, DIAG_CCOLS = 6;
+struct DiagDev {
+    // inputs
+    int n_pc, bh_include;
+    double minimum_r;
+    double pc[DIAG_PC_MAX];
+    // found by k_diag_find
+    long long first[DIAG_PC_MAX];  // first star whose mass sum exceeds each fraction (0: none)
+    long long jhalf;               // first star whose mass sum reaches half the mass (0: none)
+    // results
+    int status;                    // 0, or the reason the reference would stop
+    long long nave;
+    double rh, rho, v_rms, rc, rc_nb, m_ave, n, rc_spitzer, N_core, N_core_nb, Trc;
+    int n_set;                     // fractions assigned (the rest were not reached)
+    double mass_r[DIAG_PC_MAX], ave_mass_r[DIAG_PC_MAX], no_star_r[DIAG_PC_MAX], densities_r[DIAG_PC_MAX];
+    double ke_rad_r[DIAG_PC_MAX], ke_tan_r[DIAG_PC_MAX], v2_rad_r[DIAG_PC_MAX], v2_tan_r[DIAG_PC_MAX];
+};
+// per-star running sums the diagnostics keep between their passes (the
+// potential's and the sort's scratch arrays, which every step rewrites)
+struct DiagScratch {
+    double *col[DIAG_COLS];
+};
+__global__ void k_diag_sum(const Cluster *cls, Tiles tm, Fields f, int b0, double *partials);
+__global__ void k_diag_carry(const Cluster *cls, Tiles tm, int c, int b0, int nt, double *partials);
+__global__ void k_diag_prefix(const Cluster *cls, Tiles tm, Fields f, int b0, const double *partials,
+                              DiagScratch ds);
+__global__ void k_diag_find(const Cluster *cls, Fields f, int c, DiagScratch ds, DiagDev *dd);
+__global__ void k_diag_central(const Cluster *cls, Tiles tm, Fields f, int c, int b0, int nt, double *partials,
+                               unsigned int *tickets, DiagScratch ds, DiagDev *dd);
+
 }  // namespace cmcg

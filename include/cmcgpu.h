@@ -193,6 +193,62 @@ double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, i
 int cmcg_sign_stages(const double *E, const double *J, const double *rj, const double *mj, double invN,
                      const double *rk, const double *phik, long n, int *out);
 
+/* ------------------------------------------------- step diagnostics ---
+ * What the reference writes to dyn.dat and lagrad.dat every step
+ * (PrintFileOutput, cmc_io.c:260-323), reduced on the device from the
+ * cluster's current state:
+ *   central_calculate (cmc_utils.c:1239-1345): Casertano & Hut local
+ *     densities out to the half-mass radius and their density-weighted
+ *     averages (core density, rms velocity, core radius, rc_nb, N_core);
+ *   clusdyn_calculate (cmc_utils.c:1613-1624): the half-mass radius rh;
+ *   comp_mass_percent (cmc_utils.c:872-968): Lagrange radii and the running
+ *     kinetic sums at each mass fraction.
+ * The reference takes central_calculate at the start of a step and the rest
+ * after energy_conservation3, so a dyn.dat line for a step takes its core
+ * quantities from a call made before the step and the rest from one made
+ * after it (cmcg_format_dyn_line has a parameter for each).  Sums are tree
+ * sums: they agree with the reference's sequential ones to a few ulps of
+ * their magnitude.  The kernels use the potential's and the sort's scratch
+ * arrays, so call between steps. */
+#define CMCG_MASS_PC_MAX 64
+typedef struct {
+    /* the step (dyn.dat columns; cmc_io.c:320-323) */
+    double TotalTime, Dt;
+    long tcount, N_MAX;
+    double Mtotal, Etot, KE, PE, E_cenma, Eescaped, Eoops, max_r;
+    /* central_calculate and clusdyn_calculate */
+    long nave;                 /* index just beyond the half-mass radius       */
+    double rh;                 /* clusdyn.rh                                   */
+    double rho_0, v0_rms, core_radius, rc_nb, m_ave, n_central, rc_spitzer;
+    double N_core, N_core_nb, Trc;
+    /* comp_mass_percent, one entry per mass fraction */
+    int n_pc;                  /* fractions asked for                          */
+    int n_set;                 /* fractions reached (the rest are left at 0)   */
+    double mass_pc[CMCG_MASS_PC_MAX];
+    double mass_r[CMCG_MASS_PC_MAX], ave_mass_r[CMCG_MASS_PC_MAX], no_star_r[CMCG_MASS_PC_MAX];
+    double densities_r[CMCG_MASS_PC_MAX], ke_rad_r[CMCG_MASS_PC_MAX], ke_tan_r[CMCG_MASS_PC_MAX];
+    double v2_rad_r[CMCG_MASS_PC_MAX], v2_tan_r[CMCG_MASS_PC_MAX];
+} cmcg_diag;
+
+/* mass_pc: n_pc <= CMCG_MASS_PC_MAX fractions in non-decreasing order (the
+ * .ini key MASS_PC); bh_include and minimum_r: MASS_PC_BH_INCLUDE and
+ * MINIMUM_R.  Returns CMCG_ERR_STATE where central_calculate would stop
+ * (cmc_utils.c:1254). */
+int cmcg_diagnostics(cmcg_ctx *ctx, int cluster, const double *mass_pc, int n_pc, int bh_include, double minimum_r,
+                     cmcg_diag *out);
+/* One line of dyn.dat (the 28 columns of cmc_io.c:320-323): core quantities
+ * from `start` (a call before the step), everything else from `end`.
+ * Columns this build does not model (binary and internal energies, stellar
+ * evolution mass loss) are 0, as the reference writes them without those
+ * physics.  Returns the length written (with the newline), or -1 if `cap`
+ * is too small. */
+long cmcg_format_dyn_line(const cmcg_diag *start, const cmcg_diag *end, char *buf, long cap);
+/* One line of lagrad.dat (cmc_io.c:266, 287, 301). */
+long cmcg_format_lagrad_line(const cmcg_diag *d, char *buf, long cap);
+/* The files' header lines (cmc_io.c:2294-2347). */
+long cmcg_format_dyn_header(char *buf, long cap);
+long cmcg_format_lagrad_header(const double *mass_pc, int n_pc, char *buf, long cap);
+
 /* --------------------------------------------- allocation-free variant ---
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory once running -- a host code embedding this library in a process

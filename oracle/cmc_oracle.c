@@ -1193,6 +1193,128 @@ int ocmc_step(ocmc_state *s)
 
 /* ------------------------------------------------------------ access ---- */
 
+/* ------------------------------------------------------- diagnostics ---- */
+/* comp_mass_percent (cmc_utils.c:872-968), one rank: the radius at which the
+ * forward mass sum first exceeds each fraction of Mtotal, with the running
+ * kinetic sums there; at most one fraction is assigned per star (an if, not
+ * a while).  clusdyn_calculate (cmc_utils.c:1613-1624): rh = star_r just past
+ * half the mass.  central_calculate (cmc_utils.c:1239-1345): Casertano & Hut
+ * (1985) local densities over the J = 6 neighbours of every star out to that
+ * index, and their density-weighted averages. */
+int ocmc_diagnostics(ocmc_state *s, const double *mass_pc, int n_pc, int bh_include, double minimum_r,
+                     ocmc_diag *d)
+{
+    memset(d, 0, sizeof(*d));
+    if (n_pc < 0 || n_pc > OCMC_MASS_PC_MAX) return fail(s, OCMC_ERR_CAPACITY, n_pc);
+    d->n_pc = n_pc;
+    const double madhoc = s->madhoc, Mtotal = s->Mtotal;
+    const long J = 6;
+    /* central_calculate: nave just beyond the half-mass radius */
+    double m = 0.0;
+    long nave = 1;
+    while (m < 0.5 * Mtotal) {
+        m += s->star_m[nave] / s->N_STAR;
+        nave++;
+    }
+    if (s->N_STAR <= 2 * J || nave >= s->N_STAR - 6) return fail(s, OCMC_ERR_CAPACITY, nave);
+    d->nave = nave;
+    double rhojsum = 0.0, rhoj2sum = 0.0, rho = 0.0, v_rms = 0.0, rc = 0.0, rc_nb = 0.0, m_ave = 0.0;
+    for (long i = 1; i <= nave; i++) {
+        const long jmin = (i - J / 2 > 1) ? i - J / 2 : 1, jmax = jmin + J;
+        double mrho = 0.0;
+        for (long j = jmin + 1; j <= jmax - 1; j++) mrho += s->star_m[j] * madhoc;
+        const double Vrj = 4.0 / 3.0 * PI * (cub(s->star_r[jmax]) - cub(s->star_r[jmin]));
+        const double rhoj = mrho / Vrj;
+        rhojsum += rhoj;
+        rhoj2sum += sqr(rhoj);
+        rho += sqr(rhoj);
+        v_rms += rhoj * (sqr(s->star[i].vr) + sqr(s->star[i].vt));
+        rc += rhoj * s->star_r[i];
+        rc_nb += sqr(rhoj * s->star_r[i]);
+        m_ave += rhoj * s->star_m[i] * madhoc;
+    }
+    rho /= rhojsum;
+    rho *= 4.0 / 5.0;
+    rho *= 2.0;
+    v_rms /= rhojsum;
+    v_rms = sqrt(v_rms);
+    rc /= rhojsum;
+    rc_nb = sqrt(rc_nb / rhoj2sum);
+    m_ave /= rhojsum;
+    d->rho = rho;
+    d->v_rms = v_rms;
+    d->rc = rc;
+    d->rc_nb = rc_nb;
+    d->m_ave = m_ave;
+    d->n = rho / m_ave;
+    d->rc_spitzer = sqrt(3.0 * sqr(v_rms) / (4.0 * PI * rho));
+    d->N_core = 4.0 / 3.0 * PI * cub(rc) * (d->n / 2.0);
+    d->N_core_nb = 4.0 / 3.0 * PI * cub(rc_nb) * (d->n / 2.0);
+    d->Trc = 0.065 * cub(v_rms) / (rho * m_ave);
+    /* clusdyn_calculate */
+    m = 0.0;
+    long k = 1;
+    while (m < 0.5 * Mtotal) {
+        m += s->star_m[k] / s->N_STAR;
+        k++;
+    }
+    d->rh = s->star_r[k];
+    /* comp_mass_percent */
+    double mprev;
+    long mcount = 0;
+    if (bh_include) {
+        mprev = s->cenma_m * madhoc;
+        for (mcount = 0; mcount < n_pc; mcount++) {
+            if (mprev / Mtotal > mass_pc[mcount]) {
+                d->mass_r[mcount] = minimum_r;
+            } else {
+                break;
+            }
+        }
+    } else {
+        mprev = 0.0;
+    }
+    const long NN = s->N_MAX_NEW;
+    double *kr = calloc((size_t)NN + 1, sizeof(double)), *kt = calloc((size_t)NN + 1, sizeof(double));
+    double *vr2 = calloc((size_t)NN + 1, sizeof(double)), *vt2 = calloc((size_t)NN + 1, sizeof(double));
+    if (!kr || !kt || !vr2 || !vt2) {
+        free(kr);
+        free(kt);
+        free(vr2);
+        free(vt2);
+        return fail(s, OCMC_ERR_CAPACITY, NN);
+    }
+    for (k = 1; k <= NN; k++) {
+        const struct ostar *st = &s->star[k];
+        kr[k] = kr[k - 1] + 0.5 * s->star_m[k] * madhoc * st->vr * st->vr;
+        kt[k] = kt[k - 1] + 0.5 * s->star_m[k] * madhoc * st->vt * st->vt;
+        vr2[k] = vr2[k - 1] + st->vr * st->vr;
+        vt2[k] = vt2[k - 1] + st->vt * st->vt;
+    }
+    if (mcount < n_pc) {
+        for (k = 1; k <= s->N_MAX; k++) {
+            mprev += s->star_m[k] / s->N_STAR;
+            if (mprev > mass_pc[mcount] * Mtotal) {
+                d->mass_r[mcount] = s->star_r[k];
+                d->ave_mass_r[mcount] = mprev / Mtotal / k * 1.0;  /* initial_total_mass = 1 */
+                d->no_star_r[mcount] = k;
+                d->densities_r[mcount] = mprev / (4.0 / 3.0 * PI * pow(s->star_r[k], 3));
+                d->ke_rad_r[mcount] = kr[k];
+                d->ke_tan_r[mcount] = kt[k];
+                d->v2_rad_r[mcount] = vr2[k];
+                d->v2_tan_r[mcount] = vt2[k];
+                mcount++;
+                if (mcount == n_pc) break;
+            }
+        }
+    }
+    free(kr);
+    free(kt);
+    free(vr2);
+    free(vt2);
+    return 0;
+}
+
 static double *global_array(const ocmc_state *s, const char *name)
 {
     if (!strcmp(name, "star_r")) return s->star_r;

@@ -113,6 +113,24 @@ int ocmc_step(ocmc_state *s);
 
 /* Point queries. */
 double ocmc_potential(ocmc_state *s, double r);   /* cmc_utils.c:112        */
+
+/* Per-step diagnostics of the dyn.dat and lagrad.dat outputs: the
+ * density-weighted core of central_calculate (cmc_utils.c:1239-1345),
+ * clusdyn_calculate's half-mass radius (cmc_utils.c:1613-1624) and
+ * comp_mass_percent (cmc_utils.c:872-968), single rank, sequential sums. */
+#define OCMC_MASS_PC_MAX 64
+typedef struct {
+    long nave;                 /* index just beyond the half-mass radius      */
+    double rh;                 /* clusdyn.rh                                  */
+    double rho, v_rms, rc, rc_nb, m_ave, n, rc_spitzer;  /* central.*         */
+    double N_core, N_core_nb, Trc;
+    int n_pc;
+    double mass_r[OCMC_MASS_PC_MAX], ave_mass_r[OCMC_MASS_PC_MAX], no_star_r[OCMC_MASS_PC_MAX];
+    double densities_r[OCMC_MASS_PC_MAX], ke_rad_r[OCMC_MASS_PC_MAX], ke_tan_r[OCMC_MASS_PC_MAX];
+    double v2_rad_r[OCMC_MASS_PC_MAX], v2_tan_r[OCMC_MASS_PC_MAX];
+} ocmc_diag;
+int ocmc_diagnostics(ocmc_state *s, const double *mass_pc, int n_pc, int bh_include, double minimum_r,
+                     ocmc_diag *d);
 double ocmc_draw(const ocmc_state *s, int site, int64_t id, uint32_t n, int word);
 
 /* Field access.  Per-star fields (index 1..N_MAX_NEW) are copied into out[0..n-1];

@@ -60,6 +60,19 @@ class OParams(C.Structure):
     ]
 
 
+OCMC_MASS_PC_MAX = 64
+
+
+class ODiag(C.Structure):
+    """ocmc_diag (cmc_oracle.h)."""
+    _fields_ = ([("nave", C.c_long), ("rh", C.c_double)]
+                + [(n, C.c_double) for n in ("rho", "v_rms", "rc", "rc_nb", "m_ave", "n", "rc_spitzer",
+                                            "N_core", "N_core_nb", "Trc")]
+                + [("n_pc", C.c_int)]
+                + [(n, C.c_double * OCMC_MASS_PC_MAX) for n in ("mass_r", "ave_mass_r", "no_star_r", "densities_r",
+                                                                "ke_rad_r", "ke_tan_r", "v2_rad_r", "v2_tan_r")])
+
+
 _lib = None
 
 
@@ -100,6 +113,7 @@ def lib() -> C.CDLL:
         L.ocmc_taus113_seed.argtypes = [vp, C.c_ulong]
         L.ocmc_taus113_next.argtypes = [vp]
         L.ocmc_taus113_next.restype = C.c_uint32
+        L.ocmc_diagnostics.argtypes = [vp, vp, C.c_int, C.c_int, C.c_double, C.POINTER(ODiag)]
         _lib = L
     return _lib
 
@@ -180,6 +194,21 @@ class Oracle:
 
     def potential(self, r: float) -> float:
         return float(lib().ocmc_potential(self._h, float(r)))
+
+    def diagnostics(self, mass_pc, bh_include: int = 1, minimum_r: float = 0.0) -> dict:
+        """central_calculate, clusdyn_calculate and comp_mass_percent, sequentially."""
+        pc = np.ascontiguousarray(mass_pc, dtype=np.float64)
+        d = ODiag()
+        if lib().ocmc_diagnostics(self._h, pc.ctypes.data, len(pc), int(bh_include), float(minimum_r),
+                                  C.byref(d)):
+            raise OracleError(lib().ocmc_last_error(self._h), "diagnostics", lib().ocmc_last_error_index(self._h))
+        n = len(pc)
+        out = {k: getattr(d, k) for k in ("nave", "rh", "rho", "v_rms", "rc", "rc_nb", "m_ave", "n", "rc_spitzer",
+                                          "N_core", "N_core_nb", "Trc")}
+        for k in ("mass_r", "ave_mass_r", "no_star_r", "densities_r", "ke_rad_r", "ke_tan_r", "v2_rad_r",
+                  "v2_tan_r"):
+            out[k] = np.array(getattr(d, k)[:n])
+        return out
 
     def nstars(self) -> int:
         return int(lib().ocmc_nstars(self._h))

@@ -176,6 +176,9 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->sb.tile_next = cv.take<unsigned int>(SORT_MAX_PASSES);
     c->sb.epoch = cv.take<unsigned int>(1);
     c->sb.npass = cv.take<int>(c->ncl);
+    c->sb.shift = cv.take<int>(c->ncl);
+    c->sb.nlong = cv.take<unsigned int>(c->ncl);
+    c->sb.lstart = cv.take<long long>((size_t)(tot / 32 + 64 * (c->ncl + 1)));  // cluster c from off[c] / 32 + 64 c
     c->sb.kmin = cv.take<unsigned long long>(c->ncl);
     c->sb.kmax = cv.take<unsigned long long>(c->ncl);
     c->pb.q = cv.take<double>(tot);
@@ -626,15 +629,18 @@ static int L_sort(cmcg_ctx *c)
     CK(cudaMemsetAsync(c->sb.ghist, 0, (size_t)c->ncl * SORT_MAX_PASSES * RADIX * sizeof(unsigned long long),
                        c->stream));
     CK(cudaMemsetAsync(c->sb.tile_next, 0, SORT_MAX_PASSES * sizeof(unsigned int), c->stream));
+    CK(cudaMemsetAsync(c->sb.nlong, 0, c->ncl * sizeof(unsigned int), c->stream));
     k_sort_prep<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb,
                                                                    c->partials, c->tickets);
     k_sort_ghist<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb);
     for (int p = 0; p < SORT_MAX_PASSES; ++p)
         k_sort_onesweep<<<c->t2048.ntiles, OS_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
+    k_sort_fix<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb);
+    k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb);
     k_sort_gather<<<c->t256.ntiles, GATHER_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->sb);
     k_sort_commit<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
     fam_end(c);
-    c->launches += 4 + SORT_MAX_PASSES;
+    c->launches += 6 + SORT_MAX_PASSES;
     swap_sorted(c);
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }

@@ -18,7 +18,11 @@ constexpr int EC3_T = 256, EN_T = 2048, EN_THREADS = 256;
 constexpr int EXCESS_CAP = 4096;      // listed unphysical predictions per cluster (else full replay)
 constexpr int EC3_FIX_THREADS = 512;
 constexpr int FIX_WINDOW = 512;       // stars staged per window of the excess-energy replay
-constexpr int SORT_MAX_PASSES = 8;
+// The digit passes sort the top SORT_PREFIX_BITS bits of the keys; k_sort_fix
+// then sorts each run of keys sharing them by the full key.
+constexpr int SORT_PREFIX_BITS = 24, SORT_MAX_PASSES = SORT_PREFIX_BITS / 8;
+constexpr int FIX_SHORT = 32;   // runs up to this length are sorted by one thread
+constexpr int FIX_BLOCK = 2048; // longer runs up to this length in shared memory, the rest in place
 constexpr int TIDAL_PASSES = 32;  // bound on the stripping iteration (it settles in a few)
 
 struct SortBufs {
@@ -29,6 +33,9 @@ struct SortBufs {
     unsigned int *tile_next;     // [SORT_MAX_PASSES] tile counters, zeroed before each sort
     unsigned int *epoch;         // sorts so far (advanced by k_sort_prep): tags the status words
     int *npass;                  // per cluster: passes needed
+    int *shift;                  // per cluster: bits below the sorted prefix (0: the passes sort every bit)
+    unsigned int *nlong;         // per cluster: runs longer than FIX_SHORT, zeroed before each sort
+    long long *lstart;           // their first positions: cluster c from off[c] / 32 + 64 c
     unsigned long long *kmin, *kmax;
 };
 
@@ -111,6 +118,8 @@ __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb,
                             unsigned int *tickets);
 __global__ void k_sort_ghist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
 __global__ void k_sort_onesweep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, int pass);
+__global__ void k_sort_fix(const Cluster *cls, Tiles tm, SortBufs sb);
+__global__ void k_sort_fix_long(const Cluster *cls, Tiles tm, SortBufs sb);
 __global__ void k_sort_gather(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
 __global__ void k_sort_commit(const Cluster *cls, int nclusters);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);

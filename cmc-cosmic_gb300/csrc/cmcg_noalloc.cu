@@ -37,8 +37,10 @@ constexpr size_t NA_V1 = na_align(NA_V0 + sizeof(unsigned int) * NA_MAX);
 constexpr size_t NA_STATUS = na_align(NA_V1 + sizeof(unsigned int) * NA_MAX);      // look-back words
 constexpr size_t NA_GHIST = na_align(NA_STATUS + sizeof(unsigned long long) * RADIX * NA_TILES);
 constexpr size_t NA_MISC = na_align(NA_GHIST + sizeof(unsigned long long) * SORT_MAX_PASSES * RADIX);
-// NA_MISC: epoch (+0), npass (+8), kmin (+16), kmax (+24), tile counters (+32)
-constexpr size_t NA_PART = na_align(NA_MISC + 32 + sizeof(unsigned int) * SORT_MAX_PASSES);
+// NA_MISC: epoch (+0), npass (+8), kmin (+16), kmax (+24), shift (+32), long-run count (+40),
+// tile counters (+48)
+constexpr size_t NA_LRUN = na_align(NA_MISC + 48 + sizeof(unsigned int) * SORT_MAX_PASSES);  // long-run starts
+constexpr size_t NA_PART = na_align(NA_LRUN + sizeof(long long) * (NA_MAX / 32 + 64));
 constexpr size_t NA_TICK = na_align(NA_PART + sizeof(double) * 3 * NA_TILES);
 constexpr size_t NA_SC = na_align(NA_TICK + sizeof(unsigned int));
 constexpr size_t NA_CL = na_align(NA_SC + sizeof(Scalars));
@@ -129,7 +131,10 @@ extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_pe
     sb.ghist = (unsigned long long *)(base + NA_GHIST);
     sb.epoch = (unsigned int *)(base + NA_MISC);
     sb.npass = (int *)(base + NA_MISC + 8);
-    sb.tile_next = (unsigned int *)(base + NA_MISC + 32);
+    sb.shift = (int *)(base + NA_MISC + 32);
+    sb.nlong = (unsigned int *)(base + NA_MISC + 40);
+    sb.lstart = (long long *)(base + NA_LRUN);
+    sb.tile_next = (unsigned int *)(base + NA_MISC + 48);
     sb.kmin = (unsigned long long *)(base + NA_MISC + 16);
     sb.kmax = (unsigned long long *)(base + NA_MISC + 24);
     const Cluster *cls = (const Cluster *)(base + NA_CL);
@@ -137,11 +142,14 @@ extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_pe
     double *partials = (double *)(base + NA_PART);
     unsigned int *tickets = (unsigned int *)(base + NA_TICK);
     if (cudaMemsetAsync(sb.ghist, 0, sizeof(unsigned long long) * SORT_MAX_PASSES * RADIX, s) != cudaSuccess ||
-        cudaMemsetAsync(sb.tile_next, 0, sizeof(unsigned int) * SORT_MAX_PASSES, s) != cudaSuccess)
+        cudaMemsetAsync(sb.tile_next, 0, sizeof(unsigned int) * SORT_MAX_PASSES, s) != cudaSuccess ||
+        cudaMemsetAsync(sb.nlong, 0, sizeof(unsigned int), s) != cudaSuccess)
         return CMCG_ERR_CUDA;
     k_sort_prep<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, partials, tickets);
     k_sort_ghist<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb);
     for (int p = 0; p < SORT_MAX_PASSES; ++p) k_sort_onesweep<<<ntiles, OS_THREADS, 0, s>>>(cls, tm, f, sb, p);
+    k_sort_fix<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, sb);
+    k_sort_fix_long<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, sb);
     k_na_perm<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(base, n, d_perm);
     if (cudaGetLastError() != cudaSuccess) return CMCG_ERR_CUDA;
     if (n_bound) {

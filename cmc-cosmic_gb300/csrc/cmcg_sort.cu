@@ -8,15 +8,17 @@
 //
 // Keys are the IEEE bit patterns of rnew (positive doubles order like their
 // bits) less the cluster's smallest, with every escaper (rnew = SF_INFINITY)
-// one past the largest bound key; values the star's slot.
+// one past the largest bound key; values the star's slot.  The digit passes
+// sort the keys' top 24 bits (3 passes); keys that share them then form runs
+// in input order, which k_sort_fix sorts by the full key (runs are a star or
+// two at the densities of these clusters).
 //   k_sort_ghist     every 8-bit digit's histogram in one read of the keys
 //   k_sort_onesweep  one kernel per digit pass: stable in-tile ranking (warp
 //                    match + per-warp counters), tile offsets by decoupled
 //                    look-back, staging through shared memory so runs of one
 //                    digit leave the block as contiguous stores
 // Tiles never straddle clusters, so one launch sorts every cluster of an
-// ensemble independently.  Only the digits that span a cluster's key range
-// are sorted (7 for radii spanning up to 2^4 binades).
+// ensemble independently.
 // k_sort_gather then moves the payload (rnew, m, vrnew, vtnew, id, r, ec_pre)
 // into radial order with 128-bit-aligned SoA loads and drops the escapers
 // (r == SF_INFINITY), which sort last.
@@ -120,7 +122,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
             sb.kmin[ct.x] = a;
             sb.kmax[ct.x] = top;
             const int bits = top ? 64 - __clzll((long long)top) : 0;
-            sb.npass[ct.x] = (bits + 7) / 8;
+            const int sh = bits > SORT_PREFIX_BITS ? bits - SORT_PREFIX_BITS : 0;
+            sb.shift[ct.x] = sh;
+            sb.npass[ct.x] = (bits - sh + 7) / 8;
         }
     }
 }
@@ -154,6 +158,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_ghist(const Cluster *__re
     if (np == 0) return;
     const long long N = C.sc->N_MAX_NEW;
     const unsigned long long kmin = sb.kmin[ct.x], kesc = sb.kmax[ct.x];
+    const int sh = sb.shift[ct.x];
     for (int i = threadIdx.x; i < SORT_MAX_PASSES * RADIX; i += SORT_THREADS) (&h[0][0])[i] = 0u;
     __syncthreads();
     const long long base = (long long)ct.y * SORT_T;
@@ -161,7 +166,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_ghist(const Cluster *__re
         const long long pos = base + i;
         if (pos >= N) break;
         const unsigned long long k = radius_key(f.rnew[C.off + 1 + pos], kmin, kesc);
-        for (int p = 0; p < np; ++p) atomicAdd(&h[p][(unsigned int)(k >> (8 * p)) & (RADIX - 1)], 1u);
+        for (int p = 0; p < np; ++p) atomicAdd(&h[p][(unsigned int)(k >> (sh + 8 * p)) & (RADIX - 1)], 1u);
     }
     __syncthreads();
     unsigned long long *g = sb.ghist + (size_t)ct.x * SORT_MAX_PASSES * RADIX;
@@ -213,7 +218,7 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
     const long long N = C.sc->N_MAX_NEW;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int cur = pass & 1, nxt = cur ^ 1;
-    const int shift = 8 * pass;
+    const int shift = sb.shift[ct.x] + 8 * pass;
     const long long base = (long long)ct.y * SORT_T;
     for (int i = threadIdx.x; i < NWARP * RADIX; i += OS_THREADS) (&wcnt[0][0])[i] = 0u;
     __syncthreads();
@@ -336,6 +341,147 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
         }
         kout[C.off + dst] = k;
         vout[C.off + dst] = sv[i];
+    }
+}
+
+// After the digit passes, runs of keys sharing their sorted prefix are in
+// input order; each is sorted here by its full key.  The thread at a run's
+// start takes it: a run of one is done, a sorted run is done, runs up to
+// FIX_SHORT are insertion-sorted (stable), longer runs are listed for
+// k_sort_fix_long.
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_fix(const Cluster *__restrict__ cls, Tiles tm, SortBufs sb)
+{
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
+    const int sh = sb.shift[ct.x];
+    if (sh == 0) return;  // the passes sorted every bit
+    const int np = sb.npass[ct.x];
+    const long long N = C.sc->N_MAX_NEW;
+    unsigned long long *K = ((np & 1) ? sb.keys[1] : sb.keys[0]) + C.off;
+    unsigned int *V = ((np & 1) ? sb.vals[1] : sb.vals[0]) + C.off;
+    for (int it = 0; it < SORT_T / SORT_THREADS; ++it) {
+        const long long i = (long long)ct.y * SORT_T + it * SORT_THREADS + threadIdx.x;
+        if (i >= N) break;
+        const unsigned long long p = K[i] >> sh;
+        if (i > 0 && (K[i - 1] >> sh) == p) continue;  // not a run start
+        long long j = i + 1;
+        bool sorted = true;
+        unsigned long long prev = K[i];
+        while (j < N && j - i <= FIX_SHORT) {
+            const unsigned long long kj = K[j];
+            if ((kj >> sh) != p) break;
+            if (kj < prev) sorted = false;
+            prev = kj;
+            ++j;
+        }
+        if (j - i > FIX_SHORT) {  // the run goes on past FIX_SHORT keys
+            const unsigned int e = atomicAdd(sb.nlong + ct.x, 1u);
+            sb.lstart[C.off / 32 + 64 * ct.x + e] = i;  // at most N / (FIX_SHORT + 1) runs fit
+            continue;
+        }
+        if (sorted) continue;
+        for (long long a = i + 1; a < j; ++a) {  // insertion sort: equal keys keep their order
+            const unsigned long long ka = K[a];
+            const unsigned int va = V[a];
+            long long b = a - 1;
+            while (b >= i && K[b] > ka) {
+                K[b + 1] = K[b];
+                V[b + 1] = V[b];
+                --b;
+            }
+            K[b + 1] = ka;
+            V[b + 1] = va;
+        }
+    }
+}
+
+// (key, slot) pairs ordered by key, then by slot: the slots are the input
+// positions, so this order is the stable one and no two pairs are equal.
+__device__ __forceinline__ bool pair_less(unsigned long long ka, unsigned int va, unsigned long long kb,
+                                          unsigned int vb)
+{
+    return ka < kb || (ka == kb && va < vb);
+}
+
+// Runs longer than FIX_SHORT, each by one block (a cluster's tiles share its
+// list): a bitonic network in the form whose first comparison of each merge
+// pairs i with its mirror i ^ (k - 1), so every comparison is ascending and
+// lengths need no padding.  Up to FIX_BLOCK keys in shared memory, longer
+// runs in place in global memory.
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *__restrict__ cls, Tiles tm,
+                                                                SortBufs sb)
+{
+    __shared__ unsigned long long s_k[FIX_BLOCK];
+    __shared__ unsigned int s_v[FIX_BLOCK];
+    __shared__ long long s_len;
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
+    const int sh = sb.shift[ct.x];
+    if (sh == 0) return;
+    const int np = sb.npass[ct.x];
+    const long long N = C.sc->N_MAX_NEW;
+    unsigned long long *K = ((np & 1) ? sb.keys[1] : sb.keys[0]) + C.off;
+    unsigned int *V = ((np & 1) ? sb.vals[1] : sb.vals[0]) + C.off;
+    const unsigned int nl = *(volatile unsigned int *)(sb.nlong + ct.x);
+    for (unsigned int e = ct.y; e < nl; e += tm.count[ct.x]) {
+        const long long s = sb.lstart[C.off / 32 + 64 * ct.x + e];
+        if (threadIdx.x == 0) {
+            const unsigned long long p = K[s] >> sh;
+            long long j = s + 1;
+            while (j < N && (K[j] >> sh) == p) ++j;
+            s_len = j - s;
+        }
+        __syncthreads();
+        const long long L = s_len;
+        if (L <= FIX_BLOCK) {
+            for (long long t = threadIdx.x; t < L; t += SORT_THREADS) {
+                s_k[t] = K[s + t];
+                s_v[t] = V[s + t];
+            }
+            __syncthreads();
+            for (long long k = 2; k < 2 * L; k <<= 1) {
+                for (long long jj = k >> 1; jj > 0; jj >>= 1) {
+                    for (long long i = threadIdx.x; i < L; i += SORT_THREADS) {
+                        const long long l = (jj == (k >> 1)) ? (i ^ (k - 1)) : (i ^ jj);
+                        if (l > i && l < L && pair_less(s_k[l], s_v[l], s_k[i], s_v[i])) {
+                            const unsigned long long tk = s_k[i];
+                            const unsigned int tv = s_v[i];
+                            s_k[i] = s_k[l];
+                            s_v[i] = s_v[l];
+                            s_k[l] = tk;
+                            s_v[l] = tv;
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (long long t = threadIdx.x; t < L; t += SORT_THREADS) {
+                K[s + t] = s_k[t];
+                V[s + t] = s_v[t];
+            }
+        } else {
+            unsigned long long *k0 = K + s;
+            unsigned int *v0 = V + s;
+            for (long long k = 2; k < 2 * L; k <<= 1) {
+                for (long long jj = k >> 1; jj > 0; jj >>= 1) {
+                    for (long long i = threadIdx.x; i < L; i += SORT_THREADS) {
+                        const long long l = (jj == (k >> 1)) ? (i ^ (k - 1)) : (i ^ jj);
+                        if (l > i && l < L && pair_less(k0[l], v0[l], k0[i], v0[i])) {
+                            const unsigned long long tk = k0[i];
+                            const unsigned int tv = v0[i];
+                            k0[i] = k0[l];
+                            v0[i] = v0[l];
+                            k0[l] = tk;
+                            v0[l] = tv;
+                        }
+                    }
+                    __syncthreads();  // orders the block's global writes between stages
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 

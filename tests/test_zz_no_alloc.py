@@ -54,6 +54,31 @@ def test_noalloc_sort_matches_regular_sort_twice(gpulib):
         assert np.all(radii[got[nb:]] == 1e10)
 
 
+def test_sort_runs_sharing_the_sorted_prefix(gpulib):
+    """The digit passes sort the keys' top 24 bits; keys sharing them form runs
+    that a fix-up sorts by the full key.  Planted groups of radii within 1e-12
+    of a centre give runs of every kind: a few keys (one thread), hundreds
+    (shared memory) and 5000 (in place), with exact ties inside them."""
+    rng = np.random.default_rng(77)
+    n = 60000
+    radii = np.exp(rng.uniform(-6.0, 5.0, size=n))
+    pos = rng.permutation(n)
+    at = 0
+    for size, count in ((7, 400), (300, 20), (5000, 1)):
+        for _ in range(count):
+            c = np.exp(rng.uniform(-5.0, 4.0))
+            grp = c * (1.0 + rng.uniform(0.0, 1e-12, size))
+            grp[: size // 10] = grp[size // 2]  # exact ties keep input order
+            radii[pos[at:at + size]] = grp
+            at += size
+    radii[pos[at:at + 300]] = 1e10  # escapers
+    want_all = np.argsort(radii, kind="stable")
+    want = want_all[radii[want_all] < 1e10]
+    assert np.array_equal(_context_order(gpulib, radii), want)
+    got, nb = _noalloc_order(gpulib, radii)
+    assert nb == len(want) and np.array_equal(got[:nb], want)
+
+
 def test_noalloc_rejects_oversize(gpulib):
     rc = gpulib.lib().cmcg_sort_radii_noalloc(C.c_void_p(16), (1 << 20) + 1, C.c_void_p(16), None, None)
     assert rc == -3  # CMCG_ERR_CAPACITY, before any device work

@@ -62,11 +62,11 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     const double phis_i = __dmul_rn(div_rcp(m, ri, iri), invN);
     double Unewrold;
     const double *rt = f.r + off, *pt = f.phi + off, *it = f.inv_r + off;
-    if (rold > 0.0 && rold >= rt[1]) {
+    if (gt0(rold) && ge_pos(rold, rt[1])) {  // rold > 0 && rold >= r_1 (r_1 > 0)
         const double iro = __drcp_rn(rold);
         Unewrold = potential_in(rt, pt, it, sc->N_MAX, rold, potential_index(rt, sc->N_MAX, rold, ridx_of(C, f)), &pok,
                                 iro) +
-                   ((rold >= ri) ? __dmul_rn(div_rcp(m, rold, iro), invN) : phis_i);
+                   (ge_pos(rold, ri) ? __dmul_rn(div_rcp(m, rold, iro), invN) : phis_i);
     } else {
         Unewrold = potential_at(rt, pt, it, sc->N_MAX, rold, &pok, ridx_of(C, f)) + phi_s(rold, ri, m, invN);
     }
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     const double q = 0.5;
     const double vnew2 = f.ec_pre[g] + 2.0 * q * (Unewrold - Unewrnew);
     double vr = f.vr[g], vt = f.vt[g];
-    if (vnew2 <= 0.0) {
+    if (le0(vnew2)) {
         eb.a[g] = 0.5 * (sqr(vr) + sqr(vt) - vnew2) * m;
         const unsigned int slot = atomicAdd(eb.nlist + ct.x, 1u);
         if (slot < EXCESS_CAP) eb.list[(size_t)ct.x * EXCESS_CAP + slot] = i;

@@ -214,6 +214,49 @@ __device__ __forceinline__ dd dd_div_d_dd(double a, dd b)
 // ------------------------------------------------------ table lookups ---
 // Orders positive doubles by their bit patterns (integer compare, no FP64 pipe).
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+constexpr unsigned long long SIGN_BIT = 0x8000000000000000ull, INF_BITS = 0x7ff0000000000000ull;
+
+// FP64 comparisons decided on the operands' bit patterns with integer
+// instructions: on this GPU a DSETP occupies the FP64 pipe like an FMA.  Each
+// returns exactly what the IEEE comparison returns, for signed zeros,
+// infinities and NaNs too; c is a positive finite double.
+__device__ __forceinline__ unsigned long long ubits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ bool ge0(double x)  // x >= 0.0
+{
+    const unsigned long long b = ubits(x);
+    return b <= INF_BITS || b == SIGN_BIT;
+}
+__device__ __forceinline__ bool lt0(double x)  // x < 0.0
+{
+    const unsigned long long b = ubits(x);
+    return b > SIGN_BIT && b <= (SIGN_BIT | INF_BITS);
+}
+__device__ __forceinline__ bool le0(double x)  // x <= 0.0
+{
+    const unsigned long long b = ubits(x);
+    return b == 0 || (b >= SIGN_BIT && b <= (SIGN_BIT | INF_BITS));
+}
+__device__ __forceinline__ bool gt0(double x)  // x > 0.0
+{
+    const unsigned long long b = ubits(x);
+    return b != 0 && b <= INF_BITS;
+}
+__device__ __forceinline__ bool eq0(double x) { return (ubits(x) & ~SIGN_BIT) == 0; }  // x == 0.0
+__device__ __forceinline__ bool lt_pos(double x, double c)  // x < c
+{
+    const unsigned long long b = ubits(x);
+    return b < SIGN_BIT ? b < ubits(c) : b <= (SIGN_BIT | INF_BITS);
+}
+__device__ __forceinline__ bool ge_pos(double x, double c)  // x >= c
+{
+    const unsigned long long b = ubits(x);
+    return b >= ubits(c) && b <= INF_BITS;
+}
+__device__ __forceinline__ bool gt_pos(double x, double c)  // x > c
+{
+    const unsigned long long b = ubits(x);
+    return b > ubits(c) && b <= INF_BITS;
+}
 
 // FindZero_r, cmc_nr.c:62-82: largest k in [kmin,kmax] with r[k] < x (x > 0),
 // for kmin < kmax (the only way the reference calls it).  The bisection

@@ -288,7 +288,7 @@ static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, long lo
     double a, b, rmin, rmax, inside_sqrt;
     set_a_b(o, kmin, &a, &b);
     inside_sqrt = a * a - 2.0 * J * J * (b - E);
-    if (inside_sqrt < 0.0) {
+    if (lt0(inside_sqrt)) {
         rmin = -1.0 * J * J / a;
         if ((rmin < rkmin) || (rmin > rk1min)) {
             rmin = find_root_vr(o, kmin, prec, maxit, err);
@@ -300,7 +300,7 @@ static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, long lo
     const double dQdr_min = 2.0 * J * J / (rmin * rmin * rmin) + 2.0 * a / (rmin * rmin);
     set_a_b(o, kmax, &a, &b);
     inside_sqrt = a * a - 2.0 * J * J * (b - E);
-    if (inside_sqrt < 0.0) {
+    if (lt0(inside_sqrt)) {
         rmax = -a / (2.0 * (b - E));
         if ((rmax < rkmax) || (rmax > rk1max)) {
             rmax = find_root_vr(o, kmax, prec, maxit, err);
@@ -310,7 +310,7 @@ static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, long lo
         rmax = (-a + sqrt(inside_sqrt)) / (2.0 * (b - E));
     }
     const double dQdr_max = 2.0 * J * J / (rmax * rmax * rmax) + 2.0 * a / (rmax * rmax);
-    if ((rmin > rmax) || (dQdr_min <= 0.) || (dQdr_max >= 0.)) return res;
+    if ((rmin > rmax) || le0(dQdr_min) || ge0(dQdr_max)) return res;
     res.circular = 0;
     res.rp = rmin;
     res.ra = rmax;
@@ -440,7 +440,7 @@ static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scala
     const double drds = c1 * (3.0 - 3.0 * s0 * s0);  // 0.25 (rmax - rmin) (3 - 3 s0^2)
     const double Q = 2.0 * E - 2.0 * pot - div_rcp(div_rcp(J * J, r, ir), r, ir);
     double vr;
-    if (Q >= 0.0) {
+    if (ge0(Q)) {
         vr = sqrt(Q);
     } else {
         if (isnan(Q)) {
@@ -530,7 +530,7 @@ static __device__ __forceinline__ void commit_trial(const Cluster &C, const Scal
     f.rnew[g] = t.r;
     f.vrnew[g] = vr;
     f.vtnew[g] = div_rcp(sm.J[s], t.r, t.ir);
-    if (t.r > *max_rad) *max_rad = t.r;
+    if (dbits(t.r) > dbits(*max_rad)) *max_rad = t.r;  // both non-negative
     // energy_conservation2: Uoldrnew = potential(rnew) + PHI_S(rnew)
     f.ec_pre[g] = sm.vold2[s] + 2.0 * (1.0 - 0.5) * (sm.Uold[s] - t.pot);
 }
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(ORB_T) k_orbit_pre(const Cluster *__restrict__
     const double ps = __dmul_rn(div_rcp(mj, rj, f.inv_r[g]), sc->madhoc);
     const double E = Ej + ps;
     int slot = PQ_POSITIVE;
-    if (!(mj < CMCG_ZERO) && E < 0.0) {
+    if (!lt_pos(mj, CMCG_ZERO) && lt0(E)) {
         // the FP32 stage from the few floats it reads; the whole certified test
         // (and its context) only when that stage is undecided
         QF32 q;
@@ -632,9 +632,9 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
         // energy_conservation1: vtold, vrold, Uoldrold
         const double Uoldrold = phij + ps;
         const double vold2 = vt0 * vt0 + vr0 * vr0;
-        if (mj < CMCG_ZERO) {
+        if (lt_pos(mj, CMCG_ZERO)) {  // mj < ZERO, E >= 0 (integer forms of the comparisons)
             destroy_obj(f, g);
-        } else if (E >= 0.0) {
+        } else if (ge0(E)) {
             // remove_star, cmc_evolution_thr.c:655-716
             acc_E = Ej * mj / (double)sc->N_STAR;
             acc_J = Jj * mj / (double)sc->N_STAR;
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
                 ok = pok;
                 if (!ok) set_error(sc, CMCG_ERR_FINDZERO_R, j);
                 f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - Uoldrnew);
-            } else if (orb.ra >= Rtidal) {
+            } else if (ge_pos(orb.ra, Rtidal)) {  // Rtidal > 0
                 acc_E = Ej * mj / (double)sc->N_STAR;
                 acc_J = Jj * mj / (double)sc->N_STAR;
                 acc_M = mj / (double)sc->N_STAR;

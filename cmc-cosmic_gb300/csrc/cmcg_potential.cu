@@ -84,8 +84,12 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
             inv[i] = __drcp_rn(rk);
             pb.q[off + k] = q[i];
             f.inv_r[off + k] = inv[i];
-            if (!(mm[i] >= 0.0) || !(mm[i] < INFINITY) || !(rk > 0.0) || !(rk < CMCG_SF_INFINITY) ||
-                !(inv[i] < INFINITY))
+            // !(m >= 0) || !(m < inf) || !(r > 0) || !(r < SF_INFINITY) || !(1/r < inf), decided on
+            // the bit patterns with integer instructions (FP64 comparisons take the scarce FP64 pipe):
+            // m is +-0 or positive finite, r lies strictly between 0 and SF_INFINITY, 1/r is finite
+            const unsigned long long bm = dbits(mm[i]), br = dbits(rk), bi = dbits(inv[i]);
+            if (!((bm < INF_BITS || bm == SIGN_BIT) && (long long)br > 0 && br < dbits(CMCG_SF_INFINITY) &&
+                  bi < INF_BITS))
                 bad = 1;
         } else {
             mm[i] = q[i] = inv[i] = 0.0;
@@ -102,7 +106,9 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
         const long long k = kstart - POT_ITEMS * t - i;
         const double innext = (i == 0) ? up : inv[i - 1];
         d[i] = (k >= 1) ? inv[i] - innext : 0.0;
-        if (k >= 1 && !(d[i] >= 0.0)) bad = 1;  // radii out of order
+        // radii out of order: !(d >= 0), i.e. d neither +-0 nor positive (infinity included)
+        const unsigned long long bd = dbits(d[i]);
+        if (k >= 1 && !((bd & ~SIGN_BIT) == 0 || bd <= INF_BITS)) bad = 1;
     }
     bad = __syncthreads_or(bad);
     // exclusive prefix of q in processing order -> C = sum Qexcl * d

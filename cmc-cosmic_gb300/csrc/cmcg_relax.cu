@@ -219,7 +219,9 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
             const double Mv2 = s_w[b] - (a >= 0 ? s_w[a] : 0.0);
             const double Mm = s_m[b] - (a >= 0 ? s_m[a] : 0.0);
             sig_r[si] = r[si];
-            sig[si] = sqrt(Mv2 / Mm);
+            // sqrt(Mv2 / Mm) (calc_sigma_r, cmc_dynamics_helper.c:2977) as Mv2 rsqrt(Mv2 Mm): one
+            // reciprocal square root for a division and a square root, within 3 ulps
+            sig[si] = Mv2 * rsqrt(Mv2 * Mm);
         }
     }
 
@@ -267,7 +269,7 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                 w3 = (double)((float)vp3 - (float)v3);
                 W = (double)sqrtf((float)(w1 * w1 + w2 * w2 + w3 * w3));
             }
-            if (W == 0.0) {
+            if (eq0(W)) {
                 set_error(sc, CMCG_ERR_W_ZERO, k);
                 ok = false;
             }
@@ -283,11 +285,11 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                 beta = (CMCG_PI / 2.0) * sqrt(dt / Trel12);
                 const double relbeta[4] = {CMCG_PI / 2.0, CMCG_PI / 4.0, CMCG_PI / 8.0, CMCG_PI / 16.0};
                 part[0] += 1.0;
-                if (beta > relbeta[3]) {  // the smallest threshold: the ratio is formed once per pair
+                if (gt_pos(beta, relbeta[3])) {  // the smallest threshold: the ratio is formed once per pair
                     const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
-                        if (beta > relbeta[i]) {
+                        if (gt_pos(beta, relbeta[i])) {
                             part[1 + i] += 1.0;
                             part[5 + i] += qratio;
                             part[9 + i] += (mass_k + mass_kp) / 2.0;
@@ -295,11 +297,11 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                         }
                     }
                 }
-                if (beta > CMCG_PI / 2.0) beta = CMCG_PI / 2.0;
+                if (gt_pos(beta, CMCG_PI / 2.0)) beta = CMCG_PI / 2.0;
                 const double psi = u01(draw_block(C.seed, tcount, SITE_PSI, idk, 0u).x) * 2 * CMCG_PI;
                 if (!FP32) {
                     const double wp = sqrt(sqr(w1) + sqr(w2));
-                    if (wp == 0.0) {
+                    if (eq0(wp)) {
                         set_error(sc, CMCG_ERR_WP_ZERO, k);
                         ok = false;
                     } else {

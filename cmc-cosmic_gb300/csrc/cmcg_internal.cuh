@@ -151,8 +151,16 @@ __device__ __forceinline__ uint4 draw_block(unsigned long long seed, long long t
     return philox4x32_10(make_uint4((unsigned int)uid, (unsigned int)(uid >> 32), (unsigned int)site, n), key);
 }
 
-// u32 -> [0,1) with the reference's 32-bit resolution (taus113-v2.c:186)
-__device__ __forceinline__ double u01(unsigned int u) { return (double)u / 4294967296.0; }
+// u32 -> [0,1) with the reference's 32-bit resolution (taus113-v2.c:186):
+// u / 2^32, which is exact, assembled from its bits with integer instructions
+// (the same double as (double)u / 4294967296.0, without the FP64 pipe).
+__device__ __forceinline__ double u01(unsigned int u)
+{
+    if (u == 0u) return 0.0;
+    const int lz = __clz(u);  // the leading 1 is bit 31 - lz: u 2^-32 = 2^(-1-lz) (1.f)
+    const unsigned long long frac = (unsigned long long)(lz == 31 ? 0u : (u << (lz + 1))) << 20;
+    return __longlong_as_double((long long)(((unsigned long long)(1022 - lz) << 52) | frac));
+}
 
 // ------------------------------------------------------- double-double --
 // Error-free transformations (Knuth two-sum, FMA two-product) used to

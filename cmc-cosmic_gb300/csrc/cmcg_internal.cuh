@@ -266,6 +266,43 @@ __device__ __forceinline__ bool gt_pos(double x, double c)  // x > c
     return b > ubits(c) && b <= INF_BITS;
 }
 
+// hi = (float)x and lo = (float)(x - (double)hi), both rounded to nearest
+// even, from x's bits with integer instructions (FP64 conversions take the
+// FP64 pipe).  hi keeps the top 24 of the 53 significand bits, rounded on the
+// 29 below; x - hi is then D 2^(e-1075) exactly (|D| <= 2^28, e the biased
+// exponent), and RN(D) scaled by a power of two is RN(x - hi).  The fast path
+// takes 2^-74 <= |x| < 2^127, where hi and a nonzero lo are normal floats;
+// other x go through the FP64 conversions.
+__device__ __forceinline__ void f2_split(double x, float &hi, float &lo)
+{
+    const unsigned long long b = ubits(x);
+    const int ed = (int)((b >> 52) & 0x7ffu);
+    if (ed < 949 || ed > 1149) {
+        hi = (float)x;
+        lo = (float)(x - (double)hi);
+        return;
+    }
+    const unsigned long long S = (b & 0x000fffffffffffffull) | (1ull << 52);
+    unsigned long long H = S >> 29;
+    const unsigned long long rem = S & ((1ull << 29) - 1);
+    if (rem > (1ull << 28) || (rem == (1ull << 28) && (H & 1ull))) ++H;  // H in [2^23, 2^24]
+    const long long D = (long long)S - (long long)(H << 29);
+    const unsigned int sgn = (unsigned int)(b >> 32) & 0x80000000u;
+    // (e_f << 23) + (H - 2^23): a carry of H to 2^24 moves into the exponent
+    hi = __uint_as_float(((unsigned int)(ed - 896) << 23) + (unsigned int)(H - (1ull << 23)) | sgn);
+    const float scale = __uint_as_float((unsigned int)(ed - 1075 + 127) << 23);  // 2^(ed-1075), normal here
+    const float l = __fmul_rn(__ll2float_rn(D), scale);
+    lo = sgn ? -l : l;
+}
+
+// (float)x, rounded to nearest even (the hi part of f2_split).
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    float hi, lo;
+    f2_split(x, hi, lo);
+    return hi;
+}
+
 // FindZero_r, cmc_nr.c:62-82: largest k in [kmin,kmax] with r[k] < x (x > 0),
 // for kmin < kmax (the only way the reference calls it).  The bisection
 // halves a range of at most 2^63, so 64 rounds bound it.
@@ -427,8 +464,10 @@ struct QF32 {
 // 2^-48 of the double it stands for
 __device__ __forceinline__ float4 rphi_entry(double r, double phi)
 {
-    const float hi = (float)phi, rh = (float)r;
-    return make_float4(rh, hi, (float)(phi - (double)hi), (float)(r - (double)rh));
+    float ph, pl, rh, rl;
+    f2_split(phi, ph, pl);
+    f2_split(r, rh, rl);
+    return make_float4(rh, ph, pl, rl);
 }
 
 // E - Phi is formed in float-float (exact difference of the high parts plus

@@ -231,6 +231,8 @@ static __device__ __forceinline__ OrbitCtx make_orbit_ctx(const Cluster &C, cons
     o.invN = sc->madhoc;
     o.cenma_m = sc->cenma_m;
     o.madhoc = sc->madhoc;
+    // the float pairs (hardware conversions here: the integer split of f2_split
+    // measured no faster in this kernel, where it adds registers)
     o.s.E = (float)E;
     o.s.El = (float)(E - (double)o.s.E);
     o.s.J = (float)J;
@@ -558,11 +560,10 @@ __global__ void __launch_bounds__(ORB_T) k_orbit_pre(const Cluster *__restrict__
         // the FP32 stage from the few floats it reads; the whole certified test
         // (and its context) only when that stage is undecided
         QF32 q;
-        q.E = (float)E;
-        q.El = (float)(E - (double)q.E);
-        q.J = (float)f.J[g];
-        q.mjN = (float)(mj * sc->madhoc);
-        q.pj = (float)ps;
+        f2_split(E, q.E, q.El);
+        q.J = d2f_rn(f.J[g]);
+        q.mjN = d2f_rn(mj * sc->madhoc);
+        q.pj = d2f_rn(ps);
         int sg = fq_sign_f32(q, __ldg(f.rphif + g), true);
         if (sg == 0) {
             const OrbitCtx o = make_orbit_ctx(C, f, j, E, f.J[g], rj, mj, ps);

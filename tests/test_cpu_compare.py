@@ -79,3 +79,43 @@ def test_positive_constant_comparisons_match_ieee():
             assert np.array_equal(gt_pos(x, c), x > c), c
     # the kernels' constant helpers and these restatements read the same patterns
     assert bits(0.0) == 0 and bits(-0.0) == SIGN and bits(np.inf) == INF
+
+
+def f2_split(x):
+    """hi = RN(x) to float and lo = RN(x - hi), as cmcg_internal.cuh forms them
+    from the bits (fast path for 2^-74 <= |x| < 2^127, else conversions)."""
+    x = float(x)
+    b = int(np.array([x]).view(np.uint64)[0])
+    ed = (b >> 52) & 0x7FF
+    if ed < 949 or ed > 1149:
+        hi = np.float32(x)
+        return hi, np.float32(x - float(hi))
+    S = (b & 0x000FFFFFFFFFFFFF) | (1 << 52)
+    H = S >> 29
+    rem = S & ((1 << 29) - 1)
+    if rem > (1 << 28) or (rem == (1 << 28) and (H & 1)):
+        H += 1
+    D = S - (H << 29)
+    sgn = (b >> 32) & 0x80000000
+    hb = (((ed - 896) << 23) + (H - (1 << 23))) | sgn
+    hi = np.array([hb], dtype=np.uint32).view(np.float32)[0]
+    scale = np.array([(ed - 1075 + 127) << 23], dtype=np.uint32).view(np.float32)[0]
+    lo = np.float32(np.float32(D) * scale)  # D as float rounds to nearest; the scaling is exact
+    return hi, (-lo if sgn else lo)
+
+
+def test_float_split_matches_conversions():
+    rng = np.random.default_rng(9)
+    xs = list(rng.normal(size=20000) * 10.0 ** rng.integers(-22, 30, size=20000))
+    # ties of the 29 dropped bits, the float range edges and both fallbacks
+    for k in (1, 3, 1 << 20, (1 << 23) - 1):
+        for e in (0, -40, 60):
+            t = (k + 0.5) * 2.0 ** (e - 23)  # exactly halfway between floats
+            xs += [t, -t, np.nextafter(t, 0), np.nextafter(t, 1e300)]
+    xs += [0.0, -0.0, 2.0 ** -74, 2.0 ** -75, 2.0 ** 126 * 1.999, 2.0 ** 127, 3.4e38, 1e-40, 5e-324]
+    for x in xs:
+        hi, lo = f2_split(x)
+        want_hi = np.float32(x)
+        assert hi == want_hi and np.signbit(hi) == np.signbit(want_hi), x
+        want_lo = np.float32(x - float(want_hi))
+        assert lo == want_lo, (x, lo, want_lo)

@@ -417,7 +417,9 @@ def main():
     rank, ws, local, dist = dist_setup()
 
     if a.impl == "reference":
-        if rank != 0:
+        if rank != 0:  # the CPU arm runs on rank 0 alone; the other ranks leave without work
+            if dist is not None:
+                dist.destroy_process_group()
             return
         procs = min(os.cpu_count() or 1, 16)
         cfg = CONFIGS[a.config]
@@ -432,6 +434,8 @@ def main():
                                           f"model, {a.steps} timed steps each (reference algorithm, taus113 draws)"},
                "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
+        if dist is not None:
+            dist.destroy_process_group()
         return
 
     out = run_ours(a, rank, ws, dist)

@@ -37,7 +37,9 @@ UNIT = "star-updates/s"
 # algorithmic HBM bytes per star for each kernel family (compulsory FP64 SoA
 # traffic: reads + writes of the fields the phase consumes and produces)
 ALG_BYTES = {"sort": 116, "potential": 24, "relax": 72, "orbit": 80, "ec3": 72, "energy": 56,
-             "timestep": 24, "tidal": 16, "begin": 0, "end": 0}
+             "timestep": 24, "tidal": 16, "begin": 0, "end": 0, "mlp": 0}
+# the proposal network's algorithmic FLOPs per star: 2 (8*64 + 64*64 + 64*33)
+MLP_FLOPS_PER_STAR = 2 * (8 * 64 + 64 * 64 + 64 * 33)
 # DRAM bytes per star of one launch, dram__bytes_read.sum + dram__bytes_write.sum
 # from one ncu capture (summaries under profiles/), scaled by stars: k_orbit
 # 956.0 MB over 1,913,988 stars (King W0=6 + Kroupa, N=2e6), k_relax64 56.9 MB
@@ -48,13 +50,13 @@ NCU_TRAFFIC_PER_STAR = {"orbit": 956.0e6 / 1913988, "relax": 56.9e6 / 962913}
 NCU_FP64_PIPE_ACTIVE = {"orbit": 0.706, "relax": 0.713}
 
 
-def measured_peak():
+def measured_peak(key="hbm_gbs", fallback=6800.0):
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         d = json.load(open(p))
-        return float(d["hbm_gbs"]), "measured"
+        return float(d[key]), "measured"
     except Exception:
-        return 6800.0, "fallback"
+        return fallback, "fallback"
 
 
 class ClockSampler:
@@ -251,6 +253,108 @@ def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int, cfg_name: s
 
 
 # ------------------------------------------------------------ GPU leg ----
+# ------------------------------------------------------ learned proposal ---
+def train_proposal(a):
+    """The orbit sampler's proposal network, trained as the learned
+    configuration specifies: records (features, accepted X, trials) of the
+    plain sampler on the Plummer N=1e5 model, Adam at lr 1e-3, batch 8192."""
+    import numpy as np
+
+    import cmcgpu
+
+    cfg = CONFIGS["plummer1e5"]
+    N = cfg["N"]
+    ic = make_model(N, 20240611, cfg)
+    g = cmcgpu.Context([N], cmcgpu.default_params(orbit_r=ic["rtid"], seed=cmcgpu.derive_seed(779, 0)))
+    g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    g.initialize()
+    g.set_learned(cmcgpu.LEARN_COLLECT)
+    t0 = time.perf_counter()
+    feats, bins, nts = [], [], []
+    n = 0
+    while n < a.learn_records:
+        g.step(1)
+        f, X, nt = g.learned_samples()
+        feats.append(f)
+        bins.append(np.minimum((X * 32).astype(np.int32), 31))
+        nts.append(nt)
+        n += len(X)
+    g.check_device("collect")
+    feat, b, nt = np.concatenate(feats), np.concatenate(bins), np.concatenate(nts)
+    t1 = time.perf_counter()
+    g.mlp_init(7)
+    loss = g.mlp_train(feat, b, nt, steps=a.learn_steps, batch=8192, lr=1e-3, seed=11)
+    w = g.mlp_params()
+    t2 = time.perf_counter()
+    g.close()
+    return w, {"records": int(len(b)), "model": "Plummer N=1e5 (plain sampler)", "adam_steps": a.learn_steps,
+               "batch": 8192, "lr": 1e-3, "plain_trials_per_star": float(nt.mean()),
+               "loss_first": [float(x) for x in loss[:20].mean(axis=0)],
+               "loss_last": [float(x) for x in loss[-100:].mean(axis=0)],
+               "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2)}
+
+
+def learned_leg(a, cfg, clusters, params, ctx, timed, stars):
+    """Learned-proposal step on the same context (after the plain legs), and
+    one step from a common state with each sampler for the distribution test."""
+    import numpy as np
+    from scipy.stats import ks_2samp
+
+    import cmcgpu
+
+    w, info = train_proposal(a)
+    ctx.mlp_set_params(w)
+    ctx.set_learned(cmcgpu.LEARN_ON, a.kappa)
+    ctx.use_graph(True)
+    ctx.step(a.warmup)
+    ctx.check_device("learned warmup")
+    n0 = stars()
+    ms, launches = timed(a.steps, True)
+    ctx.check_device("learned steps")
+    st = ctx.learned_stats()
+    ctx.profile(True)
+    ctx.kernel_time("reset")
+    timed(a.steps, False)
+    fam = {name: ctx.kernel_time(name) for name in ALG_BYTES}
+    ctx.profile(False)
+    ctx.set_learned(cmcgpu.LEARN_OFF)
+    mlp_ms = fam["mlp"][0] / max(fam["mlp"][1], 1)
+    peak, peak_kind = measured_peak("bf16_tflops", 1900.0)
+    achieved = MLP_FLOPS_PER_STAR * n0 / (mlp_ms * 1e-3) / 1e12
+    # the same state through both samplers: one step each
+    n, ic, seed = clusters[0]
+    pair = []
+    for mode in (cmcgpu.LEARN_COLLECT, cmcgpu.LEARN_ON):
+        g = cmcgpu.Context([n], [params[0]])
+        g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+        g.initialize()
+        g.mlp_set_params(w)
+        g.set_learned(mode, a.kappa)
+        g.step(1)
+        g.check_device("learned pair")
+        _, X, nt = g.learned_samples()
+        pair.append((X, nt, g.learned_stats()))
+        g.close()
+    (Xa, nta, _), (Xb, _, stb) = pair
+    trials = (stb["trials"] + stb["plain_trials"]) / max(stb["accepted"] + stb["plain_stars"], 1)
+    return {
+        "what": "orbit sampler with the learned proposal (exact rejection against min(g, F) under "
+                "kappa F P q; envelope failures go back to the plain sampler)",
+        "kappa": a.kappa,
+        "value": n0 * a.steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / a.steps,
+        "gpu_launches": launches,
+        "trials_per_star": trials, "plain_trials_per_star": float(nta.mean()),
+        "failed_frac": stb["failed"] / max(stb["stars"], 1),
+        "ks_p_X": float(ks_2samp(Xa, Xb).pvalue), "ks_samples": [int(len(Xa)), int(len(Xb))],
+        "last_step_stats": st,
+        "kernels": {k: {"ms_per_step": round(v[0] / a.steps, 4), "launches": v[1]} for k, v in fam.items() if v[1]},
+        "mlp_roofline": {"bound": "tensor", "kernel": "k_mlp_infer", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_kind + " (bf16 burst)",
+                         "flops_per_star": MLP_FLOPS_PER_STAR, "ms_per_launch": mlp_ms},
+        "train": info,
+    }
+
+
 def run_ours(a, rank, ws, dist):
     import numpy as np
     import torch
@@ -387,6 +491,11 @@ def run_ours(a, rank, ws, dist):
         "profiled_ms_per_step": ms_prof / a.steps,
         "clocks": clk,
     }
+    if a.learned and rank == 0 and ws == 1:
+        try:
+            out["learned"] = learned_leg(a, cfg, clusters, params, ctx, timed, stars)
+        except Exception as e:  # the headline stands without it
+            out["learned"] = {"error": repr(e)}
     ctx.close()
     return out
 
@@ -402,6 +511,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000, help="stars per CPU-baseline process")
     ap.add_argument("--cpu-steps", type=int, default=2, help="timed oracle steps of the 1-core CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--learned", action="store_true",
+                    help="also train the proposal network and time the learned-proposal step")
+    ap.add_argument("--kappa", type=float, default=1.2, help="envelope factor of the learned proposal")
+    ap.add_argument("--learn-records", type=int, default=20_000_000, help="plain-sampler records to train on")
+    ap.add_argument("--learn-steps", type=int, default=2500, help="Adam steps of batch 8192")
     ap.add_argument("--probe-rates", action="store_true",
                     help="build and run the FP64/FP32/INT64 pipe-rate probe, then exit")
     a = ap.parse_args()

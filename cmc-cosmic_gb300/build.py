@@ -33,6 +33,7 @@ CUDA_SOURCES = [
     "cmcg_energy.cu",
     "cmcg_noalloc.cu",
     "cmcg_diag.cu",
+    "cmcg_mlp.cu",
 ]
 C_SOURCES = ["cmcg_ic.c"]
 # the reference-named drop-in layer: a second library on the public C ABI

@@ -225,6 +225,16 @@ def lib() -> C.CDLL:
         L.cmcg_put_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.cmcg_get_stars.argtypes = [vp, i, l, vp, vp, vp, vp, vp, vp, vp]
         L.cmcg_get_stars.restype = l
+        L.cmcg_set_learned.argtypes = [vp, i, d]
+        L.cmcg_mlp_init.argtypes = [vp, C.c_uint64]
+        L.cmcg_mlp_set_params.argtypes = [vp, vp]
+        L.cmcg_mlp_get_params.argtypes = [vp, vp]
+        L.cmcg_mlp_forward.argtypes = [vp, vp, l, vp, vp]
+        L.cmcg_mlp_gradient.argtypes = [vp, vp, vp, vp, l, vp]
+        L.cmcg_mlp_train.argtypes = [vp, vp, vp, vp, l, i, i, d, C.c_uint64, vp]
+        L.cmcg_learned_samples.argtypes = [vp, i, vp, vp, vp, l]
+        L.cmcg_learned_samples.restype = l
+        L.cmcg_learned_stats.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -277,6 +287,11 @@ def sign_stages(E, J, rj, mj, invN, rk, phik):
     if rc != 0:
         raise RuntimeError(f"cmcg_sign_stages failed: {rc}")
     return out
+
+
+LEARN_OFF, LEARN_ON, LEARN_COLLECT = 0, 1, 2
+MLP_NPARAM, MLP_NIN, MLP_NOUT, MLP_BINS = 6881, 8, 33, 32
+LSTAT_NAMES = ("trials", "accepted", "failed", "stars", "plain_trials", "plain_stars")
 
 
 class Context:
@@ -381,6 +396,70 @@ class Context:
         return d
 
     # -- phases (reference names)
+    # -- learned proposal of the orbit sampler
+    def set_learned(self, mode: int, kappa: float = 1.2):
+        self._check(lib().cmcg_set_learned(self._h, mode, kappa), "cmcg_set_learned")
+
+    def mlp_init(self, seed: int = 1):
+        self._check(lib().cmcg_mlp_init(self._h, seed), "cmcg_mlp_init")
+
+    def mlp_set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == MLP_NPARAM
+        self._check(lib().cmcg_mlp_set_params(self._h, w.ctypes.data), "cmcg_mlp_set_params")
+
+    def mlp_params(self) -> np.ndarray:
+        w = np.zeros(MLP_NPARAM, np.float32)
+        self._check(lib().cmcg_mlp_get_params(self._h, w.ctypes.data), "cmcg_mlp_get_params")
+        return w
+
+    def mlp_forward(self, feat):
+        """(logits n x 33, proposal n x 32) of the network on feature rows n x 8."""
+        feat = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, MLP_NIN)
+        n = feat.shape[0]
+        z = np.zeros((n, MLP_NOUT), np.float32)
+        p = np.zeros((n, MLP_BINS), np.float32)
+        self._check(lib().cmcg_mlp_forward(self._h, feat.ctypes.data, n, z.ctypes.data, p.ctypes.data),
+                    "cmcg_mlp_forward")
+        return z, p
+
+    def mlp_gradient(self, feat, bins, ntrial):
+        """(mean gradient, (mean bin loss, mean trial loss)) over the records, no update."""
+        feat = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, MLP_NIN)
+        bins = np.ascontiguousarray(bins, dtype=np.int32)
+        ntrial = np.ascontiguousarray(ntrial, dtype=np.int32)
+        g = np.zeros(MLP_NPARAM + 2, np.float32)
+        self._check(lib().cmcg_mlp_gradient(self._h, feat.ctypes.data, bins.ctypes.data, ntrial.ctypes.data,
+                                            feat.shape[0], g.ctypes.data), "cmcg_mlp_gradient")
+        return g[:MLP_NPARAM], (float(g[MLP_NPARAM]), float(g[MLP_NPARAM + 1]))
+
+    def mlp_train(self, feat, bins, ntrial, steps: int, batch: int = 8192, lr: float = 1e-3, seed: int = 1):
+        """Adam steps on minibatches; returns the losses (steps x 2)."""
+        feat = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, MLP_NIN)
+        bins = np.ascontiguousarray(bins, dtype=np.int32)
+        ntrial = np.ascontiguousarray(ntrial, dtype=np.int32)
+        loss = np.zeros((max(steps, 1), 2), np.float32)
+        self._check(lib().cmcg_mlp_train(self._h, feat.ctypes.data, bins.ctypes.data, ntrial.ctypes.data,
+                                         feat.shape[0], steps, batch, lr, seed, loss.ctypes.data), "cmcg_mlp_train")
+        return loss[:steps]
+
+    def learned_samples(self, cluster: int = 0):
+        """(features n x 8, accepted X, trials) of the last step's sampled stars."""
+        cap = self.nstars(cluster) + 2 + 128
+        feat = np.zeros((cap, MLP_NIN), np.float32)
+        X = np.zeros(cap)
+        nt = np.zeros(cap, np.int32)
+        n = lib().cmcg_learned_samples(self._h, cluster, feat.ctypes.data, X.ctypes.data, nt.ctypes.data, cap)
+        if n < 0:
+            raise CmcError(int(n), "cmcg_learned_samples")
+        n = min(n, cap)
+        return feat[:n], X[:n], nt[:n]
+
+    def learned_stats(self) -> dict:
+        out = np.zeros(8, np.uint64)
+        self._check(lib().cmcg_learned_stats(self._h, out.ctypes.data), "cmcg_learned_stats")
+        return {k: int(out[i]) for i, k in enumerate(LSTAT_NAMES)}
+
     def initialize(self):
         self._check(lib().cmcg_initialize(self._h), "initialize")
 

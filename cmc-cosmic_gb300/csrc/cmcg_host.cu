@@ -27,9 +27,9 @@ struct TileTable {
     Tiles view() const { return Tiles{d_tiles, d_first, d_count, ntiles}; }
 };
 
-enum Family { F_BEGIN, F_TIMESTEP, F_RELAX, F_ORBIT, F_TIDAL, F_SORT, F_POT, F_EC3, F_ENERGY, F_END, F_COUNT };
+enum Family { F_BEGIN, F_TIMESTEP, F_RELAX, F_ORBIT, F_TIDAL, F_SORT, F_POT, F_EC3, F_ENERGY, F_END, F_MLP, F_COUNT };
 const char *kFamilyNames[F_COUNT] = {"begin", "timestep", "relax", "orbit", "tidal",
-                                     "sort",  "potential", "ec3", "energy", "end"};
+                                     "sort",  "potential", "ec3", "energy", "end", "mlp"};
 
 struct ProfRec {
     int fam;
@@ -67,6 +67,15 @@ struct cmcg_ctx {
     void *arena = nullptr;
     size_t arena_bytes = 0;
     int relax_fp32 = 0;
+    int nsm = 1;
+    // learned proposal: the network (always), the per-star buffers (on first use)
+    MlpNet net{};
+    void *net_mem = nullptr;
+    int adam_t = 0;             // Adam steps taken since the parameters were set
+    int learn_mode = LEARN_OFF;
+    double learn_kappa = 1.2;
+    Learn lrn{};
+    void *lrn_mem = nullptr;
     // graphs
     // The sort swaps the field pointers every step, so a captured two-step
     // graph is tied to the pointer parity it was captured at: one per parity.
@@ -227,6 +236,62 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     return 0;
 }
 
+// The network's parameters, Adam moments, packed image and training partials.
+static int alloc_net(cmcg_ctx *c)
+{
+    Carver cv{nullptr};
+    for (int pass = 0; pass < 2; ++pass) {
+        cv.used = 0;
+        MlpNet &n = c->net;
+        n.w = cv.take<float>(MLP_NPARAM);
+        n.m = cv.take<float>(MLP_NPARAM);
+        n.v = cv.take<float>(MLP_NPARAM);
+        n.img = cv.take<unsigned char>(IMG_TOTAL);
+        n.partials = cv.take<float>((size_t)MLP_TRAIN_GRID_MAX * MLP_PSTRIDE);
+        n.status = cv.take<int>(1);
+        if (pass == 0) {
+            if (cudaMalloc(&c->net_mem, cv.used + 256) != cudaSuccess) {
+                cudaGetLastError();
+                return CMCG_ERR_NOMEM;
+            }
+            CK(cudaMemsetAsync(c->net_mem, 0, cv.used + 256, c->stream));
+            cv.base = (char *)c->net_mem;
+        }
+    }
+    CK(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, MLP_TRAIN_SMEM));
+    CK(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, MLP_INFER_SMEM));
+    return CMCG_OK;
+}
+
+// Per-star buffers of the learned proposal, allocated when it is first enabled.
+static int ensure_learn(cmcg_ctx *c)
+{
+    if (c->lrn_mem) return CMCG_OK;
+    const size_t tot = (size_t)c->total;
+    Carver cv{nullptr};
+    for (int pass = 0; pass < 2; ++pass) {
+        cv.used = 0;
+        Learn &L = c->lrn;
+        L.feat = cv.take<uint4>(tot);
+        L.F = cv.take<double>(tot);
+        L.prop = cv.take<float>(tot * MLP_BINS);
+        L.ntrial = cv.take<int>(tot);
+        L.stats = cv.take<unsigned long long>(LSTAT_N);
+        L.stride = (long long)tot;
+        L.mlp_status = c->net.status;
+        if (pass == 0) {
+            if (cudaMalloc(&c->lrn_mem, cv.used + 256) != cudaSuccess) {
+                cudaGetLastError();
+                fprintf(stderr, "cmcgpu: cannot allocate %zu bytes for the learned proposal\n", cv.used);
+                return CMCG_ERR_NOMEM;
+            }
+            CK(cudaMemsetAsync(c->lrn_mem, 0, cv.used + 256, c->stream));
+            cv.base = (char *)c->lrn_mem;
+        }
+    }
+    return CMCG_OK;
+}
+
 extern "C" {
 
 void cmcg_default_params(cmcg_params *p)
@@ -365,6 +430,14 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tidal, TID_THREADS, 0));
     c->tidal_grid = std::max(1, std::min(c->t2048.ntiles, nsm * std::max(per_sm, 1)));
     c->posq_grid = 2 * nsm;
+    c->nsm = nsm;
+    {
+        const int rc = alloc_net(c);
+        if (rc) {
+            cmcg_destroy(c);
+            return rc;
+        }
+    }
     CK(cudaStreamSynchronize(c->stream));
     *out = c;
     return CMCG_OK;
@@ -380,6 +453,8 @@ int cmcg_destroy(cmcg_ctx *c)
     }
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->arena) cudaFree(c->arena);
+    if (c->net_mem) cudaFree(c->net_mem);
+    if (c->lrn_mem) cudaFree(c->lrn_mem);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return CMCG_OK;
@@ -578,10 +653,34 @@ static int L_orbit(cmcg_ctx *c)
     CK(cudaMemsetAsync(c->pq.count, 0, sizeof(unsigned int), c->stream));
     k_orbit_pre<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->pq);
     k_posq_scan<<<c->posq_grid, 256, 0, c->stream>>>(c->d_cls, c->f, c->pq);
-    k_orbit<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials, c->tickets,
-                                                     c->pq);
+    if (c->learn_mode == LEARN_OFF) {
+        k_orbit<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials, c->tickets,
+                                                         c->pq);
+        c->launches += 3;
+    } else {
+        // apsides and features; the network on every star slot; the sampling
+        Learn L = c->lrn;
+        L.mode = c->learn_mode;
+        L.kappa = c->learn_kappa;
+        CK(cudaMemsetAsync(L.stats, 0, LSTAT_N * sizeof(unsigned long long), c->stream));
+        k_orbit_aps<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials,
+                                                             c->tickets, c->pq, L);
+        if (c->learn_mode == LEARN_ON) {
+            fam_end(c);
+            fam_begin(c, F_MLP);
+            const long long ntl = (c->total + MLP_T - 1) / MLP_T;
+            const int grid = (int)std::min<long long>(ntl, 4LL * c->nsm);
+            k_mlp_infer<<<grid, MLP_T, MLP_INFER_SMEM, c->stream>>>(c->net, L.feat, c->total, L.prop, L.stride,
+                                                                    nullptr);
+            c->launches += 1;
+            fam_end(c);
+            fam_begin(c, F_ORBIT);
+        }
+        k_orbit_learn<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials,
+                                                               c->tickets, c->pq, L);
+        c->launches += 4;
+    }
     fam_end(c);
-    c->launches += 3;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
@@ -1153,6 +1252,237 @@ double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, i
     }
     const uint32_t w[4] = {c0, c1, c2, c3};
     return w[word & 3] / 4294967296.0;
+}
+
+// ---------------------------------------------------- learned proposal --
+static uint16_t f2bf(float x)  // round to nearest even (finite inputs)
+{
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+static float bf2f(uint16_t h)
+{
+    const uint32_t u = (uint32_t)h << 16;
+    float x;
+    memcpy(&x, &u, 4);
+    return x;
+}
+static void drop_graphs(cmcg_ctx *c)
+{
+    for (int p = 0; p < 2; ++p) {
+        if (c->gexec[p]) cudaGraphExecDestroy(c->gexec[p]);
+        if (c->graph[p]) cudaGraphDestroy(c->graph[p]);
+        c->gexec[p] = nullptr;
+        c->graph[p] = nullptr;
+        c->graph_ready[p] = false;
+    }
+}
+static int net_status(cmcg_ctx *c)
+{
+    int st = 0;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(&st, c->net.status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) {
+        const int z = 0;
+        CK(cudaMemcpy(c->net.status, &z, sizeof(int), cudaMemcpyHostToDevice));
+        return st;
+    }
+    return CMCG_OK;
+}
+// Device buffers of a training or inference set (features as BF16).
+struct MlpSet {
+    void *mem = nullptr;
+    uint4 *feat = nullptr;
+    int *bin = nullptr, *ntrial = nullptr;
+    ~MlpSet()
+    {
+        if (mem) cudaFree(mem);
+    }
+};
+static int upload_set(cmcg_ctx *c, MlpSet &S, const float *feat, const int *bin, const int *ntrial, long n,
+                      size_t extra, void **extra_ptr)
+{
+    const size_t fb = ((size_t)n * 16 + 255) & ~(size_t)255, ib = ((size_t)n * 4 + 255) & ~(size_t)255;
+    if (cudaMalloc(&S.mem, fb + 2 * ib + extra) != cudaSuccess) {
+        cudaGetLastError();
+        return CMCG_ERR_NOMEM;
+    }
+    S.feat = (uint4 *)S.mem;
+    S.bin = (int *)((char *)S.mem + fb);
+    S.ntrial = (int *)((char *)S.mem + fb + ib);
+    if (extra_ptr) *extra_ptr = (char *)S.mem + fb + 2 * ib;
+    std::vector<uint16_t> h((size_t)n * MLP_IN);
+    for (size_t i = 0; i < h.size(); ++i) h[i] = f2bf(feat[i]);
+    CK(cudaMemcpy(S.feat, h.data(), h.size() * 2, cudaMemcpyHostToDevice));
+    if (bin) CK(cudaMemcpy(S.bin, bin, (size_t)n * 4, cudaMemcpyHostToDevice));
+    if (ntrial) CK(cudaMemcpy(S.ntrial, ntrial, (size_t)n * 4, cudaMemcpyHostToDevice));
+    return CMCG_OK;
+}
+
+int cmcg_set_learned(cmcg_ctx *c, int mode, double kappa)
+{
+    if (!c || mode < LEARN_OFF || mode > LEARN_COLLECT || !(kappa > 0.0)) return CMCG_ERR_ARG;
+    if (mode != LEARN_OFF) RUN(ensure_learn(c));
+    if (mode != c->learn_mode || kappa != c->learn_kappa) drop_graphs(c);  // another launch sequence
+    c->learn_mode = mode;
+    c->learn_kappa = kappa;
+    return CMCG_OK;
+}
+
+int cmcg_mlp_set_params(cmcg_ctx *c, const float *params)
+{
+    if (!c || !params) return CMCG_ERR_ARG;
+    CK(cudaMemcpy(c->net.w, params, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemset(c->net.m, 0, MLP_NPARAM * sizeof(float)));
+    CK(cudaMemset(c->net.v, 0, MLP_NPARAM * sizeof(float)));
+    c->adam_t = 0;
+    k_mlp_pack<<<8, 256, 0, c->stream>>>(c->net);
+    CK(cudaGetLastError());
+    return net_status(c);
+}
+
+int cmcg_mlp_get_params(cmcg_ctx *c, float *params)
+{
+    if (!c || !params) return CMCG_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(params, c->net.w, MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+    return CMCG_OK;
+}
+
+// Uniform initialisation, +-sqrt(6 / fan_in) (+-0.1 sqrt(6 / fan_in) for the
+// output layer, so the first proposals are near uniform); zero biases.
+int cmcg_mlp_init(cmcg_ctx *c, uint64_t seed)
+{
+    if (!c) return CMCG_ERR_ARG;
+    std::vector<float> w(MLP_NPARAM, 0.0f);
+    uint64_t z = seed;
+    auto next = [&z]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto fill = [&](int at, int n, double a) {
+        for (int i = 0; i < n; ++i) w[at + i] = (float)((2.0 * next() - 1.0) * a);
+    };
+    fill(P_W1, MLP_H * MLP_IN, sqrt(6.0 / MLP_IN));
+    fill(P_W2, MLP_H * MLP_H, sqrt(6.0 / MLP_H));
+    fill(P_W3, MLP_OUT * MLP_H, 0.1 * sqrt(6.0 / MLP_H));
+    return cmcg_mlp_set_params(c, w.data());
+}
+
+int cmcg_mlp_forward(cmcg_ctx *c, const float *feat, long n, float *z_out, float *prop_out)
+{
+    if (!c || !feat || n < 1) return CMCG_ERR_ARG;
+    MlpSet S;
+    void *extra = nullptr;
+    const size_t zb = ((size_t)n * MLP_OUT * 4 + 255) & ~(size_t)255;
+    RUN(upload_set(c, S, feat, nullptr, nullptr, n, zb + (size_t)n * MLP_BINS * 4, &extra));
+    float *dz = (float *)extra, *dp = (float *)((char *)extra + zb);
+    const long long ntl = (n + MLP_T - 1) / MLP_T;
+    const int grid = (int)std::min<long long>(ntl, 4LL * c->nsm);
+    k_mlp_infer<<<grid, MLP_T, MLP_INFER_SMEM, c->stream>>>(c->net, S.feat, n, dp, n, z_out ? dz : nullptr);
+    CK(cudaGetLastError());
+    RUN(net_status(c));
+    if (z_out) CK(cudaMemcpy(z_out, dz, (size_t)n * MLP_OUT * 4, cudaMemcpyDeviceToHost));
+    if (prop_out) {
+        std::vector<float> h((size_t)n * MLP_BINS);
+        CK(cudaMemcpy(h.data(), dp, h.size() * 4, cudaMemcpyDeviceToHost));
+        for (long i = 0; i < n; ++i)
+            for (int b = 0; b < MLP_BINS; ++b) prop_out[(size_t)i * MLP_BINS + b] = h[(size_t)b * n + i];
+    }
+    return CMCG_OK;
+}
+
+static int train_pass(cmcg_ctx *c, const MlpSet &S, long n, int batch, uint64_t seed, int step, int ordered,
+                      int *grid_out)
+{
+    const int ntl = (batch + MLP_T - 1) / MLP_T;
+    const int grid = std::max(1, std::min(ntl, std::min(c->nsm, MLP_TRAIN_GRID_MAX)));
+    MlpData d{S.feat, S.bin, S.ntrial, (long long)n, ordered};
+    k_mlp_train<<<grid, MLP_T, MLP_TRAIN_SMEM, c->stream>>>(c->net, d, batch, seed, step);
+    *grid_out = grid;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
+int cmcg_mlp_gradient(cmcg_ctx *c, const float *feat, const int *bin, const int *ntrial, long n, float *grad)
+{
+    if (!c || !feat || !bin || !ntrial || !grad || n < 1 || n > (1L << 30)) return CMCG_ERR_ARG;
+    MlpSet S;
+    void *extra = nullptr;
+    RUN(upload_set(c, S, feat, bin, ntrial, n, (MLP_NPARAM + 2) * sizeof(float), &extra));
+    int grid = 0;
+    RUN(train_pass(c, S, n, (int)n, 0, 0, 1, &grid));
+    k_mlp_adam<<<1, 1024, 0, c->stream>>>(c->net, grid, 0.0f, 1, 1, (float *)extra);
+    CK(cudaGetLastError());
+    RUN(net_status(c));
+    CK(cudaMemcpy(grad, extra, (MLP_NPARAM + 2) * sizeof(float), cudaMemcpyDeviceToHost));
+    return CMCG_OK;
+}
+
+int cmcg_mlp_train(cmcg_ctx *c, const float *feat, const int *bin, const int *ntrial, long n, int steps, int batch,
+                   double lr, uint64_t seed, float *loss)
+{
+    if (!c || !feat || !bin || !ntrial || n < 1 || steps < 0 || batch < 1 || !(lr >= 0.0)) return CMCG_ERR_ARG;
+    MlpSet S;
+    void *extra = nullptr;
+    RUN(upload_set(c, S, feat, bin, ntrial, n, (size_t)std::max(steps, 1) * 2 * sizeof(float), &extra));
+    float *dl = (float *)extra;
+    for (int s = 0; s < steps; ++s) {
+        int grid = 0;
+        RUN(train_pass(c, S, n, batch, seed, c->adam_t, 0, &grid));
+        c->adam_t += 1;
+        k_mlp_adam<<<1, 1024, 0, c->stream>>>(c->net, grid, (float)lr, c->adam_t, 0, dl + 2 * s);
+        CK(cudaGetLastError());
+    }
+    RUN(net_status(c));
+    if (loss && steps > 0) CK(cudaMemcpy(loss, dl, (size_t)steps * 2 * sizeof(float), cudaMemcpyDeviceToHost));
+    return CMCG_OK;
+}
+
+long cmcg_learned_samples(cmcg_ctx *c, int k, float *feat, double *X, int *ntrial, long cap)
+{
+    if (!c || k < 0 || k >= c->ncl || !c->lrn_mem || cap < 0) return CMCG_ERR_ARG;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return CMCG_ERR_CUDA;
+    const long long o = c->off[k], n = c->cap[k] + 2;
+    std::vector<double> F(n), Xd(n), rn(n);
+    std::vector<uint4> fe(n);
+    std::vector<int> nt(n);
+    if (cudaMemcpy(F.data(), c->lrn.F + o, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(Xd.data(), c->f.X + o, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(rn.data(), c->f.rnew + o, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(fe.data(), c->lrn.feat + o, n * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(nt.data(), c->lrn.ntrial + o, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return CMCG_ERR_CUDA;
+    long cnt = 0;
+    for (long long j = 1; j < n; ++j) {
+        if (!(F[j] > 0.0) || rn[j] == CMCG_SF_INFINITY || nt[j] == 0) continue;
+        if (cnt < cap) {
+            const uint16_t *h = (const uint16_t *)&fe[j];
+            if (feat)
+                for (int i = 0; i < MLP_IN; ++i) feat[(size_t)cnt * MLP_IN + i] = bf2f(h[i]);
+            if (X) X[cnt] = Xd[j];
+            if (ntrial) ntrial[cnt] = nt[j];
+        }
+        ++cnt;
+    }
+    return cnt;
+}
+
+int cmcg_learned_stats(cmcg_ctx *c, uint64_t *out)
+{
+    if (!c || !out) return CMCG_ERR_ARG;
+    if (!c->lrn_mem) {
+        memset(out, 0, LSTAT_N * sizeof(uint64_t));
+        return CMCG_OK;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(out, c->lrn.stats, LSTAT_N * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    return CMCG_OK;
 }
 
 }  // extern "C"

@@ -141,7 +141,7 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
     return c;
 }
 
-enum { SITE_Y = 1, SITE_PENC = 2, SITE_PSI = 3, SITE_TRIAL = 4, SITE_SIGN = 5 };
+enum { SITE_Y = 1, SITE_PENC = 2, SITE_PSI = 3, SITE_TRIAL = 4, SITE_SIGN = 5, SITE_LTRIAL = 6 };
 
 __device__ __forceinline__ uint4 draw_block(unsigned long long seed, long long tcount, int site,
                                             long long id, unsigned int n)

@@ -113,6 +113,74 @@ constexpr int PQ_POSITIVE = -1, PQ_SCAN_HERE = -2, PQ_CAP = 1024;
 __global__ void k_orbit_pre(const Cluster *cls, Tiles tm, Fields f, PosQ pq);
 __global__ void k_posq_scan(const Cluster *cls, Fields f, PosQ pq);
 __global__ void k_orbit(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets, PosQ pq);
+
+// ---- learned proposal of the orbit sampler (cmcg_mlp.cu, cmcg_orbit.cu)
+// An MLP 8 -> 64 -> 64 -> 33 (ReLU; BF16 weights and activations, FP32
+// accumulation on the tensor cores) maps a star's orbit features to a
+// 32-bin piecewise-constant density in the sampling variable X (a monotone
+// piecewise-linear CDF) and to P, the predicted acceptance probability of the
+// plain sampler's trial.  The sampler draws X from that density and accepts
+// it against the true clipped density min(g(s), F) under the envelope
+// kappa * F * P * q(X); a trial where the envelope fails sends the star back
+// to the plain sampler.
+constexpr int MLP_IN = 8, MLP_H = 64, MLP_OUT = 33, MLP_BINS = 32;
+constexpr int MLP_T = 128;                 // rows (stars or samples) per tile = threads per CTA
+constexpr int MLP_K1 = 16;                 // layer-1 K: the 8 features, zero-padded
+constexpr int MLP_N3 = 48;                 // layer-3 N: the 33 outputs, zero-padded
+constexpr int MLP_NG = 80, MLP_NG1 = 16;   // weight-gradient N: inputs, a column of ones (bias), padding
+// master parameters (FP32): W1[64][8], b1[64], W2[64][64], b2[64], W3[33][64], b3[33]
+constexpr int P_W1 = 0, P_B1 = P_W1 + MLP_H * MLP_IN, P_W2 = P_B1 + MLP_H, P_B2 = P_W2 + MLP_H * MLP_H,
+              P_W3 = P_B2 + MLP_H, P_B3 = P_W3 + MLP_OUT * MLP_H, MLP_NPARAM = P_B3 + MLP_OUT;
+constexpr int MLP_PSTRIDE = 6912;          // floats per training partial: gradients, then the two loss sums
+static_assert(MLP_NPARAM + 2 <= MLP_PSTRIDE, "partial layout");
+// packed operand image (bytes): the B operands of the forward pass, the
+// biases (FP32), then the transposed weights of the backward pass
+constexpr int IMG_W1 = 0, IMG_W2 = IMG_W1 + MLP_H * MLP_K1 * 2, IMG_W3 = IMG_W2 + MLP_H * MLP_H * 2,
+              IMG_BIAS = IMG_W3 + MLP_N3 * MLP_H * 2, IMG_INFER = IMG_BIAS + 768, IMG_W3T = IMG_INFER,
+              IMG_W2T = IMG_W3T + MLP_H * MLP_N3 * 2, IMG_TOTAL = IMG_W2T + MLP_H * MLP_H * 2;
+static_assert(IMG_INFER % 128 == 0 && IMG_TOTAL % 128 == 0, "bulk copies of 16-byte multiples");
+constexpr float MLP_FLOOR = 1.0f / 64.0f;  // share of the uniform density mixed into every proposal
+constexpr int MLP_TRAIN_GRID_MAX = 152;    // partial slots of the training kernel
+
+struct MlpNet {
+    float *w, *m, *v;     // master parameters and Adam moments
+    unsigned char *img;   // packed operand image (IMG_TOTAL bytes)
+    float *partials;      // [grid][MLP_PSTRIDE]
+    int *status;          // a bounded wait that gave up (CMCG_ERR_SPIN)
+};
+struct MlpData {
+    const uint4 *feat;    // 8 BF16 features per sample
+    const int *bin;       // bin of the accepted X (floor(32 X))
+    const int *ntrial;    // trials the plain sampler used (>= 1)
+    long long n;
+    int ordered;          // 1: batch position p is sample p (gradient checks)
+};
+enum { LEARN_OFF = 0, LEARN_ON = 1, LEARN_COLLECT = 2 };
+constexpr int LSTAT_TRIALS = 0, LSTAT_ACCEPT = 1, LSTAT_FAIL = 2, LSTAT_STARS = 3, LSTAT_PLAIN_TRIALS = 4,
+              LSTAT_PLAIN_STARS = 5, LSTAT_N = 8;
+struct Learn {
+    uint4 *feat;              // per star slot: the 8 BF16 features (zero where no position is sampled)
+    double *F;                // per star slot: the plain envelope F (> 0: the star samples a position)
+    float *prop;              // [32][stride]: C_1 .. C_31 of the proposal's CDF, then P
+    int *ntrial;              // per star slot: accepted trial, plain k > 0 or proposal -k
+    unsigned long long *stats;  // LSTAT_* counters of the last step
+    const int *mlp_status;    // the network's status word (a failed inference)
+    long long stride;
+    double kappa;             // envelope factor
+    int mode;                 // LEARN_ON: proposal first; LEARN_COLLECT: plain trials only
+};
+__global__ void k_mlp_pack(MlpNet net);
+__global__ void k_mlp_infer(MlpNet net, const uint4 *feat, long long nrows, float *prop, long long stride,
+                            float *z_out);
+__global__ void k_mlp_train(MlpNet net, MlpData data, int batch, unsigned long long seed, int step);
+__global__ void k_mlp_adam(MlpNet net, int nparts, float lr, int t, int mode, float *out);
+constexpr int MLP_INFER_SMEM = IMG_INFER + MLP_T * MLP_K1 * 2 + MLP_T * MLP_H * 2 + 64;
+constexpr int MLP_TRAIN_SMEM = IMG_TOTAL + MLP_T * MLP_K1 * 2 + MLP_NG1 * MLP_T * 2 + 2 * MLP_T * MLP_H * 2 +
+                               2 * MLP_NG * MLP_T * 2 + 2 * MLP_T * MLP_T * 2 + 192;
+__global__ void k_orbit_aps(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets, PosQ pq,
+                            Learn L);
+__global__ void k_orbit_learn(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
+                              PosQ pq, Learn L);
 __global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *bar, int nclusters);
 __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, double *partials,
                             unsigned int *tickets);

@@ -15,6 +15,7 @@
 // k_tidal restates the iteration of tidally_strip_stars
 // (cmc_evolution_thr.c:443-646) in one cooperative launch, its passes
 // separated by a bounded grid barrier.
+#include <cuda_bf16.h>
 #include "cmcg_kernels.cuh"
 #include "cmcgpu.h"
 
@@ -252,6 +253,7 @@ static __device__ __forceinline__ OrbitCtx make_orbit_ctx(const Cluster &C, cons
 
 struct OrbitRs {
     double rp, ra, dQdrp, dQdra;
+    long long kmin, kmax;  // the table intervals holding the apsides
     int circular;
 };
 
@@ -314,6 +316,8 @@ static __device__ OrbitRs calc_orbit_new(const OrbitCtx &o, long long j, long lo
     const double dQdr_max = 2.0 * J * J / (rmax * rmax * rmax) + 2.0 * a / (rmax * rmax);
     if ((rmin > rmax) || le0(dQdr_min) || ge0(dQdr_max)) return res;
     res.circular = 0;
+    res.kmin = kmin;
+    res.kmax = kmax;
     res.rp = rmin;
     res.ra = rmax;
     res.dQdrp = dQdr_min;
@@ -374,6 +378,7 @@ constexpr int TRIAL_UNSURE = -1;                  // filter only: left to the ex
 
 struct Trial {
     double X, r, ir, vr, pot;
+    double g;  // 1 / vr * drds, the reference's g(s0)
     int code;
 };
 
@@ -399,18 +404,19 @@ static __device__ __forceinline__ TrialIn trial_input(const Cluster &C, const Sc
     return in;
 }
 
-// A trial of star slot s, evaluated exactly as the reference does, without
-// writing anything.  Radii are positive, so they are compared on their bit
-// patterns (integer instructions, as the FP64 comparisons would decide).
-static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scalars *sc, const Fields &f,
-                                                   const SampleSmem &sm, int s, const TrialIn &in, double invN)
+// The radius of a trial of star slot s, evaluated exactly as the reference
+// does (potential, Q, vr and g = 1 / vr * drds), without writing anything;
+// code TRIAL_REJECT when that succeeded, else a device status.  Radii are
+// positive, so they are compared on their bit patterns (integer
+// instructions, as the FP64 comparisons would decide).
+static __device__ __forceinline__ Trial eval_core(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                  const SampleSmem &sm, int s, const TrialIn &in, double invN)
 {
     Trial t;
     const long long off = C.off, N_MAX = sc->N_MAX;
     const double E = sm.E[s], J = sm.J[s], mj = sm.mj[s], c1 = sm.c1[s];
     const double X = in.X, r = in.r;
     const double s0 = 2.0 * X - 1.0;
-    const double g0 = sm.F[s] * u01(in.uy);
     // one correctly rounded 1/r serves every division by r below (div_rcp)
     const double ir = __drcp_rn(r);
     int pok = 1;
@@ -452,7 +458,17 @@ static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scala
         vr = 0;
     }
     t.vr = vr;
-    t.code = (g0 < 1.0 / vr * drds) ? TRIAL_ACCEPT : TRIAL_REJECT;
+    t.g = 1.0 / vr * drds;
+    t.code = TRIAL_REJECT;
+    return t;
+}
+
+// A plain trial (cmc_evolution_thr.c:860-885): accepted when g0 = F u < g(s0).
+static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                   const SampleSmem &sm, int s, const TrialIn &in, double invN)
+{
+    Trial t = eval_core(C, sc, f, sm, s, in, invN);
+    if (t.code == TRIAL_REJECT) t.code = (sm.F[s] * u01(in.uy) < t.g) ? TRIAL_ACCEPT : TRIAL_REJECT;
     return t;
 }
 
@@ -603,13 +619,142 @@ __global__ void __launch_bounds__(256) k_posq_scan(const Cluster *__restrict__ c
     }
 }
 
-// Five blocks per SM (at most 102 registers a thread; a few bytes spill) keep
-// more warps on the FP64 pipe than the four that 116 registers allow.
-__global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                 double *partials, unsigned int *tickets, PosQ pq)
+// The per-star part of the learned proposal: the orbit's features for the
+// network (normalised, as BF16): rmin / rmax, ln(rmax) / 8, E / Phi_a,
+// J^2 / (2 rmin^2 (E - Phi_a)), and the potential's shape across the orbit,
+// (Phi_k - Phi_a) / (Phi_b - Phi_a) at four table points evenly spaced in
+// index between a = kmin and b = kmax + 1, the table points bracketing the
+// apsides (table reads only: no radius search).
+static __device__ __forceinline__ uint4 orbit_features(const OrbitCtx &o, const OrbitRs &orb)
+{
+    const long long ka = orb.kmin, kb = orb.kmax + 1;
+    const double pa = __ldg(o.phi + ka), pb = __ldg(o.phi + kb), d = pb - pa;
+    float x[MLP_IN];
+    x[0] = (float)(orb.rp / orb.ra);
+    x[1] = 0.125f * logf((float)orb.ra);
+    x[2] = (float)(o.E / pa);
+    x[3] = (float)(o.J * o.J / (2.0 * orb.rp * orb.rp * (o.E - pa)));
+#pragma unroll
+    for (int i = 1; i <= 4; ++i) {
+        const long long k = ka + ((kb - ka) * i) / 5;
+        x[3 + i] = d > 0.0 ? (float)((__ldg(o.phi + k) - pa) / d) : 0.0f;
+    }
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float a = isfinite(x[2 * i]) ? x[2 * i] : 0.0f, b = isfinite(x[2 * i + 1]) ? x[2 * i + 1] : 0.0f;
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        w[i] = *reinterpret_cast<uint32_t *>(&h);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+struct LearnSmem {
+    float cdf[MLP_BINS - 1][ORB_T];  // C_1 .. C_31 of each star's proposal
+    float P[ORB_T];                  // its predicted acceptance probability of a plain trial
+};
+constexpr int TRIAL_FAIL = -2;  // a proposal trial found the envelope below the density
+
+// Trial k of the proposal for star slot s, with draws of its own site keyed
+// by (star id, k): X from the 32-bin density q by inverting its CDF (density
+// 32 (C_b+1 - C_b) on bin b, with the stored knots), g0 uniform under the
+// envelope kappa F P q(X).  Accepted when g0 < min(g(s0), F), the density the
+// plain sampler samples (its g clipped at its envelope F).  Where min(g, F)
+// exceeds the envelope the trial is TRIAL_FAIL and the star goes back to the
+// plain sampler.
+static __device__ __forceinline__ Trial learned_trial(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                      const SampleSmem &sm, const LearnSmem &ls, int s, int k,
+                                                      double invN, double kappa)
+{
+    const uint4 u = draw_block(C.seed, sc->tcount, SITE_LTRIAL, sm.id[s], (unsigned int)(k - 1));
+    const double U = u01(u.x);
+    int b = 0;  // the last bin whose lower knot is <= U (C_0 = 0)
+#pragma unroll
+    for (int h = 16; h > 0; h >>= 1)
+        if (b + h <= MLP_BINS - 1 && (double)ls.cdf[b + h - 1][s] <= U) b += h;
+    const double lo = b > 0 ? (double)ls.cdf[b - 1][s] : 0.0;
+    const double hi = b < MLP_BINS - 1 ? (double)ls.cdf[b][s] : 1.0;
+    const double pb = hi - lo;
+    double X = ((double)b + (U - lo) / pb) * (1.0 / MLP_BINS);
+    if (!(X < 1.0)) X = 0x1.fffffffffffffp-1;
+    TrialIn in;
+    in.X = X;
+    const double s0 = 2.0 * X - 1.0;
+    in.r = sm.c0[s] + sm.c1[s] * (3.0 * s0 - s0 * s0 * s0);  // the reference's map from s0 to r
+    in.i = -1;
+    in.ux = u.x;
+    in.uy = u.y;
+    Trial t = eval_core(C, sc, f, sm, s, in, invN);
+    if (t.code != TRIAL_REJECT) return t;  // a device error
+    const double F = sm.F[s];
+    const double env = kappa * F * (double)ls.P[s] * ((double)MLP_BINS * pb);
+    const double g = isnan(t.g) ? 0.0 : t.g;  // 0 * inf: the reference's comparison rejects
+    const double h = g < F ? g : F;
+    if (h > env)
+        t.code = TRIAL_FAIL;
+    else
+        t.code = (env * u01(u.y) < h) ? TRIAL_ACCEPT : TRIAL_REJECT;
+    return t;
+}
+
+// One star's sampling state in the block's shared memory.
+static __device__ __forceinline__ void stage_star(SampleSmem &sm, int ts, const OrbitCtx &o, double rmin,
+                                                  double rmax, double F, double E, double J, double rj, double mj,
+                                                  double vold2, double Uoldrold, long long idj, double ps)
+{
+    sm.rmin[ts] = rmin;
+    sm.rmax[ts] = rmax;
+    sm.F[ts] = F;
+    sm.E[ts] = E;
+    sm.J[ts] = J;
+    sm.rj[ts] = rj;
+    sm.mj[ts] = mj;
+    sm.vold2[ts] = vold2;
+    sm.Uold[ts] = Uoldrold;
+    sm.id[ts] = idj;
+    sm.ps[ts] = ps;
+    sm.c0[ts] = 0.5 * (rmin + rmax);
+    sm.c1[ts] = 0.25 * (rmax - rmin);
+    sm.rjb[ts] = dbits(rj);
+    // the filter's floats: E as a float pair, the rest rounded once
+    sm.fE[ts] = o.s.E;
+    sm.fEl[ts] = o.s.El;
+    sm.fJ[ts] = o.s.J;
+    sm.fmjN[ts] = o.s.mjN;
+    sm.fpj[ts] = o.s.pj;
+    sm.fF[ts] = (float)F;
+    sm.fc1[ts] = (float)sm.c1[ts];
+}
+
+// Sum of a per-thread counter over the block, added to a global counter by one thread.
+static __device__ __forceinline__ void add_stat(unsigned long long *dst, unsigned int v, unsigned int *s_w)
+{
+    const unsigned int w = __reduce_add_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int q = 0; q < ORB_T / 32; ++q) s += s_w[q];
+        if (s) atomicAdd(dst, s);
+    }
+    __syncthreads();
+}
+
+// MODE 0: the whole of get_positions_loop for the block's stars (k_orbit).
+// MODE 1: everything up to the rejection loop (k_orbit_aps): stars that still
+//         sample a position leave their envelope F and features for the
+//         network (apsides in r_peri / r_apo, which the accepted trial writes
+//         again unchanged); escapers, circular orbits and errors are final.
+// MODE 2: the rejection loop of those stars (k_orbit_learn): proposal trials
+//         first (Learn::mode LEARN_ON), stars whose envelope failed then take
+//         the plain trials of MODE 0 from the first, as every star does in
+//         LEARN_COLLECT.
+template <int MODE>
+static __device__ __forceinline__ void orbit_body(const Cluster *__restrict__ cls, Tiles tm, const Fields &f,
+                                                  double *partials, unsigned int *tickets, const PosQ &pq,
+                                                  const Learn &L, SampleSmem &sm, LearnSmem *ls)
 {
     __shared__ double red[ORB_T / 32];
-    __shared__ SampleSmem sm;
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
@@ -623,6 +768,11 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
 
     double acc_E = 0.0, acc_J = 0.0, acc_M = 0.0, acc_Et = 0.0, max_rad = 0.0;
     bool pend = false;
+    if (MODE == 1 && j <= C.cap) {  // this step's records only (every slot of the cluster)
+        L.F[g] = 0.0;
+        L.feat[g] = make_uint4(0u, 0u, 0u, 0u);
+        L.ntrial[g] = 0;
+    }
     if (j <= N_NEW) {
         const double Ej = f.E[g], Jj = f.J[g], rj = f.r[g], mj = f.m[g], phij = f.phi[g];
         const double vr0 = f.vr_rel[g], vt0 = f.vt_rel[g];
@@ -633,89 +783,164 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
         // energy_conservation1: vtold, vrold, Uoldrold
         const double Uoldrold = phij + ps;
         const double vold2 = vt0 * vt0 + vr0 * vr0;
-        if (lt_pos(mj, CMCG_ZERO)) {  // mj < ZERO, E >= 0 (integer forms of the comparisons)
-            destroy_obj(f, g);
-        } else if (ge0(E)) {
-            // remove_star, cmc_evolution_thr.c:655-716
-            acc_E = Ej * mj / (double)sc->N_STAR;
-            acc_J = Jj * mj / (double)sc->N_STAR;
-            acc_M = mj / (double)sc->N_STAR;
-            acc_Et = Ej * mj / (double)sc->N_STAR;
-            destroy_obj(f, g);
+        if (MODE == 2) {
+            const double F = L.F[g];
+            if (F > 0.0 && C.n_try >= 1) {  // left to sample by the apsides pass
+                const OrbitCtx o = make_orbit_ctx(C, f, j, E, J, rj, mj, ps);
+                stage_star(sm, threadIdx.x, o, f.r_peri[g], f.r_apo[g], F, E, J, rj, mj, vold2, Uoldrold, idj, ps);
+                if (L.mode == LEARN_ON) {
+#pragma unroll
+                    for (int b = 0; b < MLP_BINS - 1; ++b) ls->cdf[b][threadIdx.x] = L.prop[b * L.stride + g];
+                    ls->P[threadIdx.x] = L.prop[(MLP_BINS - 1) * L.stride + g];
+                }
+                pend = true;
+            }
         } else {
-            const OrbitCtx o = make_orbit_ctx(C, f, j, E, J, rj, mj, ps);
-            int err = 0;
-            // Q(j) > 0, or the index the grid-wide scan found (k_orbit_pre, k_posq_scan)
-            const int slot = pq.slot[g];
-            const long long kpos = (slot == PQ_POSITIVE) ? j : (slot >= 0 ? pq.res[slot] : -1);
-            const OrbitRs orb = calc_orbit_new(o, j, kpos, C.apsides_precision, C.apsides_max_iter, &err);
-            if (err) {
-                set_error(sc, err, j);
-            } else if (orb.circular) {
-                // cmc_evolution_thr.c:835-840: position and velocities unchanged
-                f.rnew[g] = rj;
-                f.vrnew[g] = vr0;
-                f.vtnew[g] = vt0;
-                bool ok = true;
-                int pok = 1;
-                const double Uoldrnew =
-                    potential_at(o.r, o.phi, o.inv_r, N_MAX, rj, &pok, ridx_of(C, f)) + ps;
-                ok = pok;
-                if (!ok) set_error(sc, CMCG_ERR_FINDZERO_R, j);
-                f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - Uoldrnew);
-            } else if (ge_pos(orb.ra, Rtidal)) {  // Rtidal > 0
+            if (lt_pos(mj, CMCG_ZERO)) {  // mj < ZERO, E >= 0 (integer forms of the comparisons)
+                destroy_obj(f, g);
+            } else if (ge0(E)) {
+                // remove_star, cmc_evolution_thr.c:655-716
                 acc_E = Ej * mj / (double)sc->N_STAR;
                 acc_J = Jj * mj / (double)sc->N_STAR;
                 acc_M = mj / (double)sc->N_STAR;
                 acc_Et = Ej * mj / (double)sc->N_STAR;
                 destroy_obj(f, g);
             } else {
-                const double rmin = orb.rp, rmax = orb.ra;
-                const double g1 = sqrt(3.0 * (rmax - rmin) / orb.dQdrp);
-                const double g2 = sqrt(-3.0 * (rmax - rmin) / orb.dQdra);
-                const int ts = threadIdx.x;
-                const double F = 1.2 * (g1 >= g2 ? g1 : g2);
-                sm.rmin[ts] = rmin;
-                sm.rmax[ts] = rmax;
-                sm.F[ts] = F;
-                sm.E[ts] = E;
-                sm.J[ts] = J;
-                sm.rj[ts] = rj;
-                sm.mj[ts] = mj;
-                sm.vold2[ts] = vold2;
-                sm.Uold[ts] = Uoldrold;
-                sm.id[ts] = idj;
-                sm.ps[ts] = ps;
-                sm.c0[ts] = 0.5 * (rmin + rmax);
-                sm.c1[ts] = 0.25 * (rmax - rmin);
-                sm.rjb[ts] = dbits(rj);
-                // the filter's floats: E as a float pair, the rest rounded once
-                sm.fE[ts] = o.s.E;
-                sm.fEl[ts] = o.s.El;
-                sm.fJ[ts] = o.s.J;
-                sm.fmjN[ts] = o.s.mjN;
-                sm.fpj[ts] = o.s.pj;
-                sm.fF[ts] = (float)F;
-                sm.fc1[ts] = (float)sm.c1[ts];
-                pend = C.n_try >= 1;
-                if (!pend) set_error(sc, CMCG_ERR_NTRY, j);  // no trial allowed (cmc_evolution_thr.c:888)
+                const OrbitCtx o = make_orbit_ctx(C, f, j, E, J, rj, mj, ps);
+                int err = 0;
+                // Q(j) > 0, or the index the grid-wide scan found (k_orbit_pre, k_posq_scan)
+                const int slot = pq.slot[g];
+                const long long kpos = (slot == PQ_POSITIVE) ? j : (slot >= 0 ? pq.res[slot] : -1);
+                const OrbitRs orb = calc_orbit_new(o, j, kpos, C.apsides_precision, C.apsides_max_iter, &err);
+                if (err) {
+                    set_error(sc, err, j);
+                } else if (orb.circular) {
+                    // cmc_evolution_thr.c:835-840: position and velocities unchanged
+                    f.rnew[g] = rj;
+                    f.vrnew[g] = vr0;
+                    f.vtnew[g] = vt0;
+                    bool ok = true;
+                    int pok = 1;
+                    const double Uoldrnew =
+                        potential_at(o.r, o.phi, o.inv_r, N_MAX, rj, &pok, ridx_of(C, f)) + ps;
+                    ok = pok;
+                    if (!ok) set_error(sc, CMCG_ERR_FINDZERO_R, j);
+                    f.ec_pre[g] = vold2 + 2.0 * (1.0 - 0.5) * (Uoldrold - Uoldrnew);
+                } else if (ge_pos(orb.ra, Rtidal)) {  // Rtidal > 0
+                    acc_E = Ej * mj / (double)sc->N_STAR;
+                    acc_J = Jj * mj / (double)sc->N_STAR;
+                    acc_M = mj / (double)sc->N_STAR;
+                    acc_Et = Ej * mj / (double)sc->N_STAR;
+                    destroy_obj(f, g);
+                } else {
+                    const double rmin = orb.rp, rmax = orb.ra;
+                    const double g1 = sqrt(3.0 * (rmax - rmin) / orb.dQdrp);
+                    const double g2 = sqrt(-3.0 * (rmax - rmin) / orb.dQdra);
+                    const double F = 1.2 * (g1 >= g2 ? g1 : g2);
+                    if (C.n_try < 1) {
+                        set_error(sc, CMCG_ERR_NTRY, j);  // no trial allowed (cmc_evolution_thr.c:888)
+                    } else if (MODE == 1) {
+                        f.r_peri[g] = rmin;
+                        f.r_apo[g] = rmax;
+                        L.F[g] = F;
+                        L.feat[g] = orbit_features(o, orb);
+                    } else {
+                        stage_star(sm, threadIdx.x, o, rmin, rmax, F, E, J, rj, mj, vold2, Uoldrold, idj, ps);
+                        pend = true;
+                    }
+                }
             }
         }
     }
-    // rejection sampling in rounds over the block's pending stars
     const int t = threadIdx.x;
-    if (t == 0) sm.n[0] = 0;
-    __syncthreads();
-    if (pend) {
-        const int p = atomicAdd(&sm.n[0], 1);
-        sm.list[0][p] = t;
-        sm.next[t] = 1;
-        sm.first[t] = INT_MAX;
-    }
-    __syncthreads();
     const long long j0 = 1 + (long long)ct.y * ORB_T;
     const long long n_try = C.n_try;
     const bool check = C.check_filters != 0;
+    if (MODE == 2 && L.mode == LEARN_ON && t == 0 && ct.y == 0 && *L.mlp_status != 0)
+        set_error(sc, CMCG_ERR_SPIN, 0);  // the network's inference gave up: its proposals are not valid
+    unsigned int st_trials = 0, st_acc = 0, st_fail = 0, st_ptrials = 0, st_pstars = 0;
+    if (MODE == 2 && L.mode == LEARN_ON) {
+        // proposal rounds: each pending star's next m trials at once; the first
+        // trial that accepts or fails decides the star
+        if (t == 0) {
+            sm.n[0] = 0;
+            sm.nw = 0;  // stars sent back to the plain sampler collect in wl
+        }
+        __syncthreads();
+        if (pend) {
+            const int p = atomicAdd(&sm.n[0], 1);
+            sm.list[0][p] = t;
+            sm.next[t] = 1;
+            sm.first[t] = INT_MAX;
+        }
+        __syncthreads();
+        for (int cur = 0;; cur ^= 1) {
+            const int n = sm.n[cur];
+            if (n == 0) break;
+            const int m = ORB_T / n;
+            if (t == 0) sm.n[cur ^ 1] = 0;
+            int slot = -1, k = 0, kb = 0;
+            Trial tr;
+            tr.code = TRIAL_REJECT;
+            if (t < n * m) {
+                slot = sm.list[cur][t / m];
+                kb = sm.next[slot];
+                k = kb + t % m;
+                if (k <= n_try) {
+                    tr = learned_trial(C, sc, f, sm, *ls, slot, k, invN, L.kappa);
+                    if (tr.code != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
+                }
+            }
+            __syncthreads();
+            if (slot >= 0) {
+                const int fst = sm.first[slot];
+                if (k == fst) {
+                    st_trials += (unsigned int)k;
+                    if (tr.code == TRIAL_ACCEPT) {
+                        commit_trial(C, sc, f, sm, slot, off + j0 + slot, tr, &max_rad);
+                        L.ntrial[off + j0 + slot] = -k;
+                        st_acc++;
+                    } else if (tr.code == TRIAL_FAIL) {
+                        sm.wl[atomicAdd(&sm.nw, 1)] = slot;
+                        st_fail++;
+                    } else {
+                        set_error(sc, tr.code, j0 + slot);
+                    }
+                } else if (t % m == 0 && fst == INT_MAX) {
+                    if (kb + m - 1 >= n_try) {  // the proposal's trials ran out: the plain sampler decides
+                        st_trials += (unsigned int)n_try;
+                        sm.wl[atomicAdd(&sm.nw, 1)] = slot;
+                        st_fail++;
+                    } else {
+                        sm.next[slot] = kb + m;
+                        sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = slot;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        const int nfb = sm.nw;
+        if (t < nfb) {
+            const int s = sm.wl[t];
+            sm.list[0][t] = s;
+            sm.next[s] = 1;
+            sm.first[s] = INT_MAX;
+        }
+        __syncthreads();
+        if (t == 0) sm.n[0] = nfb;
+        __syncthreads();
+    } else {
+        // rejection sampling in rounds over the block's pending stars
+        if (t == 0) sm.n[0] = 0;
+        __syncthreads();
+        if (pend) {
+            const int p = atomicAdd(&sm.n[0], 1);
+            sm.list[0][p] = t;
+            sm.next[t] = 1;
+            sm.first[t] = INT_MAX;
+        }
+        __syncthreads();
+    }
     for (int cur = 0;; cur ^= 1) {
         const int n = sm.n[cur];
         if (n == 0) break;
@@ -772,6 +997,11 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
             const Trial tr = eval_trial(C, sc, f, sm, s, cin, invN);
             if (tr.code == TRIAL_ACCEPT) {
                 commit_trial(C, sc, f, sm, s, off + j0 + s, tr, &max_rad);
+                if (MODE == 2) {
+                    L.ntrial[off + j0 + s] = kk;
+                    st_ptrials += (unsigned int)kk;
+                    st_pstars++;
+                }
             } else if (tr.code != TRIAL_REJECT) {
                 set_error(sc, tr.code, j0 + s);
             } else if (kk >= n_try) {
@@ -784,6 +1014,15 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
             }
         }
         __syncthreads();
+    }
+    if (MODE == 2) {
+        __shared__ unsigned int s_w[ORB_T / 32];
+        add_stat(L.stats + LSTAT_TRIALS, st_trials, s_w);
+        add_stat(L.stats + LSTAT_ACCEPT, st_acc, s_w);
+        add_stat(L.stats + LSTAT_FAIL, st_fail, s_w);
+        add_stat(L.stats + LSTAT_STARS, (L.mode == LEARN_ON && pend) ? 1u : 0u, s_w);
+        add_stat(L.stats + LSTAT_PLAIN_TRIALS, st_ptrials, s_w);
+        add_stat(L.stats + LSTAT_PLAIN_STARS, st_pstars, s_w);
     }
     // escapers are rare: most warps skip the sums (block_sums)
     __shared__ double s_acc[ORB_T / 32][4];
@@ -806,16 +1045,46 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
         for (int q = 0; q < 4; ++q) a[q] = reduce_partials_sum<ORB_T>(partials, b0, nb, ORB_NPART, q, red);
         a[4] = reduce_partials_max<ORB_T>(partials, b0, nb, ORB_NPART, 4, red);
         if (threadIdx.x == 0) {
-            // new_orbits_calculate, cmc_utils.c:2197-2210
-            sc->OldTidalMassLoss = sc->TidalMassLoss_old;
-            sc->Eescaped += a[0];
-            sc->Jescaped += a[1];
-            sc->TidalMassLoss += a[2];
-            sc->Etidal += a[3];
-            sc->max_r = a[4];
-            sc->TidalMassLoss += sc->TidalMassLoss_old;
+            if (MODE == 2) {
+                // the apsides pass set max_r from the stars it finished (none sampled there)
+                if (a[4] > sc->max_r) sc->max_r = a[4];
+            } else {
+                // new_orbits_calculate, cmc_utils.c:2197-2210
+                sc->OldTidalMassLoss = sc->TidalMassLoss_old;
+                sc->Eescaped += a[0];
+                sc->Jescaped += a[1];
+                sc->TidalMassLoss += a[2];
+                sc->Etidal += a[3];
+                sc->max_r = a[4];
+                sc->TidalMassLoss += sc->TidalMassLoss_old;
+            }
         }
     }
+}
+
+// Five blocks per SM (at most 102 registers a thread; a few bytes spill) keep
+// more warps on the FP64 pipe than the four that 116 registers allow.
+__global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                 double *partials, unsigned int *tickets, PosQ pq)
+{
+    __shared__ SampleSmem sm;
+    const Learn none{};
+    orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr);
+}
+
+__global__ void __launch_bounds__(ORB_T, 5) k_orbit_aps(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                     double *partials, unsigned int *tickets, PosQ pq, Learn L)
+{
+    __shared__ SampleSmem sm;
+    orbit_body<1>(cls, tm, f, partials, tickets, pq, L, sm, nullptr);
+}
+
+__global__ void __launch_bounds__(ORB_T, 4) k_orbit_learn(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                       double *partials, unsigned int *tickets, PosQ pq, Learn L)
+{
+    __shared__ SampleSmem sm;
+    __shared__ LearnSmem ls;
+    orbit_body<2>(cls, tm, f, partials, tickets, pq, L, sm, &ls);
 }
 
 // Grid-wide barrier for a co-resident (cooperatively launched) grid:

@@ -193,6 +193,63 @@ double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, i
 int cmcg_sign_stages(const double *E, const double *J, const double *rj, const double *mj, double invN,
                      const double *rk, const double *phik, long n, int *out);
 
+/* ------------------------------------------------- learned proposal ---
+ * An optional proposal for the orbit sampler's rejection loop
+ * (get_positions_loop, cmc_evolution_thr.c:855-926).  A network 8 -> 64 ->
+ * 64 -> 33 (ReLU; BF16 weights and activations, FP32 accumulation on the
+ * tensor cores) maps a star's orbit features (rmin / rmax, ln rmax / 8,
+ * E / Phi_a, J^2 / (2 rmin^2 (E - Phi_a)) and the potential's shape at four
+ * table points between the apsides, Phi_a being the table value below rmin)
+ * to a 32-bin piecewise-constant density q in the reference's sampling
+ * variable X (s0 = 2X - 1), mixed with 1/64 of the uniform density, and to P,
+ * the predicted acceptance probability of a plain trial.  A proposal trial
+ * draws X from q and g0 uniform under kappa F P q(X), and accepts when
+ * g0 < min(g(s0), F): the density the plain sampler draws from (its g
+ * clipped at its envelope F).  The sampled distribution is therefore the
+ * plain sampler's wherever kappa F P q >= min(g, F).  A trial that finds that
+ * envelope below the density sends the star back to the plain sampler, which
+ * then runs from its first trial with the plain draws (so with kappa small
+ * enough every star takes exactly the plain result).
+ * Modes: CMCG_LEARN_OFF (the plain sampler only), CMCG_LEARN_ON, and
+ * CMCG_LEARN_COLLECT (the plain sampler through the learned launch sequence,
+ * recording each sampled star's features, accepted X and trial count:
+ * training data).  The network is trained by cmcg_mlp_train (Adam, on the
+ * GPU) on (features, floor(32 X), trials) records, minimising
+ * -log softmax(z)_bin - (k - 1) log(1 - P) - log P averaged over the batch. */
+enum { CMCG_LEARN_OFF = 0, CMCG_LEARN_ON = 1, CMCG_LEARN_COLLECT = 2 };
+#define CMCG_MLP_NPARAM 6881  /* W1[64][8], b1[64], W2[64][64], b2[64], W3[33][64], b3[33] */
+#define CMCG_MLP_NIN 8
+#define CMCG_MLP_NOUT 33
+enum {
+    CMCG_LSTAT_TRIALS = 0,       /* proposal trials up to each star's decision  */
+    CMCG_LSTAT_ACCEPT = 1,       /* stars accepted by a proposal trial          */
+    CMCG_LSTAT_FAIL = 2,         /* stars sent back to the plain sampler        */
+    CMCG_LSTAT_STARS = 3,        /* stars that started with the proposal        */
+    CMCG_LSTAT_PLAIN_TRIALS = 4, /* plain trials of stars the plain sampler did */
+    CMCG_LSTAT_PLAIN_STARS = 5,  /* stars the plain sampler did                 */
+    CMCG_LSTAT_N = 8
+};
+/* Select the orbit sampler for the following steps; kappa is the envelope factor (> 0). */
+int cmcg_set_learned(cmcg_ctx *ctx, int mode, double kappa);
+int cmcg_mlp_init(cmcg_ctx *ctx, uint64_t seed);
+int cmcg_mlp_set_params(cmcg_ctx *ctx, const float *params /* CMCG_MLP_NPARAM */);
+int cmcg_mlp_get_params(cmcg_ctx *ctx, float *params);
+/* The network on n feature rows (n x 8): the 33 logits (n x 33) and/or the
+ * stored proposal (n x 32: C_1 .. C_31 of the CDF, then P); either may be NULL. */
+int cmcg_mlp_forward(cmcg_ctx *ctx, const float *feat, long n, float *z_out, float *prop_out);
+/* Mean loss gradient over the n records (CMCG_MLP_NPARAM values) followed by
+ * the two mean loss terms (bins, trial count): no update. */
+int cmcg_mlp_gradient(cmcg_ctx *ctx, const float *feat, const int *bin, const int *ntrial, long n, float *grad);
+/* `steps` Adam steps (beta 0.9, 0.999) on minibatches of `batch` records drawn
+ * with replacement (keyed by seed and step); loss (2 x steps, or NULL). */
+int cmcg_mlp_train(cmcg_ctx *ctx, const float *feat, const int *bin, const int *ntrial, long n, int steps,
+                   int batch, double lr, uint64_t seed, float *loss);
+/* After a step: the records of cluster k's sampled stars (features n x 8,
+ * accepted X, trials: plain k > 0, proposal -k); returns their number (at
+ * most cap written). */
+long cmcg_learned_samples(cmcg_ctx *ctx, int k, float *feat, double *X, int *ntrial, long cap);
+int cmcg_learned_stats(cmcg_ctx *ctx, uint64_t *out /* CMCG_LSTAT_N */);
+
 /* ------------------------------------------------- step diagnostics ---
  * What the reference writes to dyn.dat and lagrad.dat every step
  * (PrintFileOutput, cmc_io.c:260-323), reduced on the device from the

@@ -343,19 +343,8 @@ static __device__ __forceinline__ void destroy_obj(const Fields &f, long long g)
     f.m[g] = CMCG_DBL_MIN;
 }
 
-// Stars of a block that still sample their position (get_positions_loop's
-// rejection loop, cmc_evolution_thr.c:855-926).  A star's trial k uses draws
-// keyed by (star id, k), so its trials are independent of one another and of
-// the order they run in.  Each round gives every pending star m = ORB_T / n
-// threads (n pending stars), which test its next m trials at once with a
-// certified FP32 filter (filter_trial); the first trial the filter does not
-// reject is the only candidate for the star's outcome in the reference's
-// sequential loop, and those candidates, one per star, are then evaluated
-// exactly in FP64 by threads packed into full warps.  A candidate the exact
-// evaluation rejects (the filter was unsure) puts the star back with its
-// next trial.  Rounds stay full of threads, their number falls to about the
-// log of the longest trial sequence, and the FP64 evaluation runs about
-// once per star instead of once per trial.
+// The sampling state of a block's stars that still sample their position,
+// and the lists of its rounds (sample_rounds).
 struct SampleSmem {
     double rmin[ORB_T], rmax[ORB_T], F[ORB_T], E[ORB_T], J[ORB_T], rj[ORB_T], mj[ORB_T], vold2[ORB_T],
         Uold[ORB_T], ps[ORB_T];
@@ -492,21 +481,21 @@ static __device__ __forceinline__ Trial eval_trial(const Cluster &C, const Scala
 //    draw is 0), so the trial is accepted.
 // Radii at or below r_1, a failed search, neighbours within 4 ulps (whose
 // reciprocals may round equal) and non-finite values are unsure.
-static __device__ __forceinline__ int filter_trial(const Cluster &C, const Scalars *sc, const Fields &f,
-                                                   const SampleSmem &sm, int s, TrialIn &in)
+// The bracket [Qlo, Qhi] (first point above); false where it cannot be
+// formed (the trial is then unsure).  Sets in.i once the radius is searched.
+static __device__ __forceinline__ bool q_bracket(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                 const SampleSmem &sm, int s, TrialIn &in, float &Qlo, float &Qhi)
 {
-    const float fc1 = sm.fc1[s];
-    if (in.ux == 0u || !(fc1 > 0.0f)) return TRIAL_UNSURE;
     const double r = in.r;
     const long long off = C.off, N_MAX = sc->N_MAX;
     const double *rt = f.r + off;
     const long long rb = dbits(r);
-    if (rb <= dbits(__ldg(rt + 1))) return TRIAL_UNSURE;
+    if (rb <= dbits(__ldg(rt + 1))) return false;
     const long long i = potential_index(rt, N_MAX, r, ridx_of(C, f));
     in.i = i;
-    if (i < 1 || i > N_MAX) return TRIAL_UNSURE;
+    if (i < 1 || i > N_MAX) return false;
     const long long bi = dbits(__ldg(rt + i)), bi1 = dbits(__ldg(rt + i + 1));
-    if (bi >= rb || bi1 < rb || bi1 - bi <= 4) return TRIAL_UNSURE;
+    if (bi >= rb || bi1 < rb || bi1 - bi <= 4) return false;
     const float4 ta = __ldg(f.rphif + off + i), tb = __ldg(f.rphif + off + i + 1);
     const float plo = fminf(ta.y, tb.y), phi = fmaxf(ta.y, tb.y);
     const float irf = __frcp_rn((float)r);
@@ -518,9 +507,18 @@ static __device__ __forceinline__ int filter_trial(const Cluster &C, const Scala
     const float Ahi = __fsub_rn(__fadd_rn(dhi.x, __fadd_rn(dhi.y, sm.fEl[s])), phis);
     const float M = fabsf(sm.fE[s]) + fmaxf(fabsf(plo), fabsf(phi)) + phis + B + fmaxf(fabsf(Alo), fabsf(Ahi));
     const float eQ = __fmul_rn(0x1p-18f, M);
-    const float Qlo = __fsub_rn(__fsub_rn(__fmul_rn(2.0f, Alo), B), eQ);
-    const float Qhi = __fadd_rn(__fsub_rn(__fmul_rn(2.0f, Ahi), B), eQ);
-    if (!(fabsf(Qlo) <= 1e30f) || !(fabsf(Qhi) <= 1e30f)) return TRIAL_UNSURE;
+    Qlo = __fsub_rn(__fsub_rn(__fmul_rn(2.0f, Alo), B), eQ);
+    Qhi = __fadd_rn(__fsub_rn(__fmul_rn(2.0f, Ahi), B), eQ);
+    return fabsf(Qlo) <= 1e30f && fabsf(Qhi) <= 1e30f;
+}
+
+static __device__ __forceinline__ int filter_trial(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                   const SampleSmem &sm, int s, TrialIn &in)
+{
+    const float fc1 = sm.fc1[s];
+    if (in.ux == 0u || !(fc1 > 0.0f)) return TRIAL_UNSURE;
+    float Qlo, Qhi;
+    if (!q_bracket(C, sc, f, sm, s, in, Qlo, Qhi)) return TRIAL_UNSURE;
     if (Qhi < 0.0f) return TRIAL_ACCEPT;
     if (!(Qlo > 0.0f)) return TRIAL_UNSURE;
     // 1 - s0^2 = 4 X (1 - X) = u (2^32 - u) 2^-62
@@ -652,19 +650,19 @@ static __device__ __forceinline__ uint4 orbit_features(const OrbitCtx &o, const 
 struct LearnSmem {
     float cdf[MLP_BINS - 1][ORB_T];  // C_1 .. C_31 of each star's proposal
     float P[ORB_T];                  // its predicted acceptance probability of a plain trial
+    double wenv[ORB_T];              // a candidate's envelope kappa F P q(X)
+    int fb[ORB_T];                   // stars sent back to the plain sampler
+    int nfb;
 };
 constexpr int TRIAL_FAIL = -2;  // a proposal trial found the envelope below the density
 
 // Trial k of the proposal for star slot s, with draws of its own site keyed
 // by (star id, k): X from the 32-bin density q by inverting its CDF (density
-// 32 (C_b+1 - C_b) on bin b, with the stored knots), g0 uniform under the
-// envelope kappa F P q(X).  Accepted when g0 < min(g(s0), F), the density the
-// plain sampler samples (its g clipped at its envelope F).  Where min(g, F)
-// exceeds the envelope the trial is TRIAL_FAIL and the star goes back to the
-// plain sampler.
-static __device__ __forceinline__ Trial learned_trial(const Cluster &C, const Scalars *sc, const Fields &f,
-                                                      const SampleSmem &sm, const LearnSmem &ls, int s, int k,
-                                                      double invN, double kappa)
+// 32 (C_b+1 - C_b) on bin b, with the stored knots), and the envelope
+// kappa F P q(X) under which g0 is drawn uniformly.
+static __device__ __forceinline__ TrialIn learned_input(const Cluster &C, const Scalars *sc, const SampleSmem &sm,
+                                                        const LearnSmem &ls, int s, int k, double kappa,
+                                                        double *env)
 {
     const uint4 u = draw_block(C.seed, sc->tcount, SITE_LTRIAL, sm.id[s], (unsigned int)(k - 1));
     const double U = u01(u.x);
@@ -684,17 +682,197 @@ static __device__ __forceinline__ Trial learned_trial(const Cluster &C, const Sc
     in.i = -1;
     in.ux = u.x;
     in.uy = u.y;
+    *env = kappa * sm.F[s] * (double)ls.P[s] * ((double)MLP_BINS * pb);
+    return in;
+}
+
+// Exact decision of a proposal trial: accepted when g0 = env u < min(g(s0), F),
+// the density the plain sampler samples (its g clipped at its envelope F);
+// TRIAL_FAIL where min(g, F) exceeds the envelope (the star then goes back to
+// the plain sampler).
+static __device__ __forceinline__ Trial learned_eval(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                     const SampleSmem &sm, int s, const TrialIn &in, double env,
+                                                     double invN)
+{
     Trial t = eval_core(C, sc, f, sm, s, in, invN);
     if (t.code != TRIAL_REJECT) return t;  // a device error
     const double F = sm.F[s];
-    const double env = kappa * F * (double)ls.P[s] * ((double)MLP_BINS * pb);
     const double g = isnan(t.g) ? 0.0 : t.g;  // 0 * inf: the reference's comparison rejects
     const double h = g < F ? g : F;
     if (h > env)
         t.code = TRIAL_FAIL;
     else
-        t.code = (env * u01(u.y) < h) ? TRIAL_ACCEPT : TRIAL_REJECT;
+        t.code = (env * u01(in.uy) < h) ? TRIAL_ACCEPT : TRIAL_REJECT;
     return t;
+}
+
+// Certified FP32 decision of a proposal trial, from filter_trial's bracket of
+// Q: TRIAL_ACCEPT or TRIAL_REJECT only where the exact evaluation must agree
+// and the envelope certainly holds (F <= env, or g < env for every Q in the
+// bracket), TRIAL_UNSURE otherwise.  1 - s0^2 = 4 X (1 - X) is formed in FP64
+// from X (within 2^-51 of its value), so filter_trial's margin eta holds.
+static __device__ __forceinline__ int learned_filter(const Cluster &C, const Scalars *sc, const Fields &f,
+                                                     const SampleSmem &sm, int s, TrialIn &in, double env)
+{
+    const float fc1 = sm.fc1[s];
+    const double X = in.X;
+    if (!(X > 0.0) || !(X < 1.0) || !(fc1 > 0.0f)) return TRIAL_UNSURE;
+    float Qlo, Qhi;
+    if (!q_bracket(C, sc, f, sm, s, in, Qlo, Qhi)) return TRIAL_UNSURE;
+    const double F = sm.F[s];
+    const double g0 = env * u01(in.uy);  // as the exact decision forms it
+    const bool holds_at_F = F <= env;     // min(g, F) <= F <= env
+    if (Qhi < 0.0f) {                     // vr = 0, g = +inf: min(g, F) = F
+        if (!holds_at_F) return TRIAL_UNSURE;
+        return g0 < F ? TRIAL_ACCEPT : TRIAL_REJECT;
+    }
+    if (!(Qlo > 0.0f)) return TRIAL_UNSURE;
+    const float w = (float)(4.0 * X * (1.0 - X));
+    const float drds = __fmul_rn(__fmul_rn(3.0f, fc1), w);
+    const float eta = __fadd_rn(0x1p-17f, __fmul_rn(0x1p-48f, __frcp_rn(w)));
+    const float d2 = __fmul_rn(drds, drds);
+    if (!(d2 <= 1e30f) || !(d2 > 1e-30f)) return TRIAL_UNSURE;
+    if (!holds_at_F) {  // g < env for certain: env^2 Qlo > drds^2 (1 + eta)
+        const float e = (float)env, e2 = __fmul_rn(e, e);
+        if (!(e2 <= 1e30f) || !(__fmul_rn(e2, Qlo) > __fmul_rn(d2, __fadd_rn(1.0f, eta)))) return TRIAL_UNSURE;
+    }
+    if (g0 >= F) return TRIAL_REJECT;  // min(g, F) <= F <= g0
+    const float gf = (float)g0, g2 = __fmul_rn(gf, gf);
+    if (!(g2 <= 1e30f)) return TRIAL_UNSURE;
+    if (__fmul_rn(g2, Qhi) < __fmul_rn(d2, __fsub_rn(1.0f, eta))) return TRIAL_ACCEPT;
+    if (__fmul_rn(g2, Qlo) > __fmul_rn(d2, __fadd_rn(1.0f, eta))) return TRIAL_REJECT;
+    return TRIAL_UNSURE;
+}
+
+// Per-thread counters of the learned sampler (block sums go to Learn::stats).
+struct LStat {
+    unsigned int trials = 0, acc = 0, fail = 0, ptrials = 0, pstars = 0;
+};
+
+// The rounds of a block's rejection loop (get_positions_loop,
+// cmc_evolution_thr.c:855-926) over the sm.n[0] stars listed in sm.list[0]
+// (state staged, next = 1, first = INT_MAX).  A star's trial k uses draws
+// keyed by (star id, k), so its trials are independent of one another and of
+// the order they run in.  Each round gives every pending star m = ORB_T / n
+// threads (n pending stars), which test its next m trials at once with a
+// certified FP32 filter; the first trial the filter does not reject is the
+// only candidate for the star's outcome in the reference's sequential loop,
+// and those candidates, one per star, are then evaluated exactly in FP64 by
+// threads packed into full warps.  A candidate the exact evaluation rejects
+// (the filter was unsure) puts the star back with its next trial.  Rounds
+// stay full of threads, their number falls to about the log of the longest
+// trial sequence, and the FP64 evaluation runs about once per star instead
+// of once per trial.  LEARN: the proposal's trials; a star whose envelope
+// fails, or whose n_try proposal trials are all rejected, is listed in
+// ls->fb for the plain rounds that follow.
+template <int MODE, bool LEARN>
+static __device__ __forceinline__ void sample_rounds(const Cluster &C, Scalars *sc, const Fields &f, SampleSmem &sm,
+                                                     LearnSmem *ls, const Learn &L, long long j0, double invN,
+                                                     double *max_rad, LStat &st)
+{
+    const int t = threadIdx.x;
+    const long long off = C.off, n_try = C.n_try;
+    const bool check = C.check_filters != 0;
+    for (int cur = 0;; cur ^= 1) {
+        const int n = sm.n[cur];
+        if (n == 0) break;
+        const int m = ORB_T / n;  // trials per pending star this round
+        if (t == 0) {
+            sm.n[cur ^ 1] = 0;  // last read at the top of the previous round
+            sm.nw = 0;
+        }
+        // 1. the filter on each star's next m trials
+        int slot = -1, k = 0, kb = 0;
+        TrialIn in;
+        double env = 0.0;
+        if (t < n * m) {
+            slot = sm.list[cur][t / m];
+            kb = sm.next[slot];
+            k = kb + t % m;
+            if (k <= n_try) {
+                int dec;
+                if (LEARN) {
+                    in = learned_input(C, sc, sm, *ls, slot, k, L.kappa, &env);
+                    dec = learned_filter(C, sc, f, sm, slot, in, env);
+                    if (check && dec != TRIAL_UNSURE && learned_eval(C, sc, f, sm, slot, in, env, invN).code != dec)
+                        set_error(sc, CMCG_ERR_FILTER, j0 + slot);
+                } else {
+                    in = trial_input(C, sc, sm, slot, k);
+                    dec = filter_trial(C, sc, f, sm, slot, in);
+                    if (check && dec != TRIAL_UNSURE && eval_trial(C, sc, f, sm, slot, in, invN).code != dec)
+                        set_error(sc, CMCG_ERR_FILTER, j0 + slot);
+                }
+                if (dec != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
+            }
+        }
+        __syncthreads();
+        // 2. candidates listed (with their inputs); stars whose m trials were all rejected go on
+        if (slot >= 0) {
+            const int fst = sm.first[slot];
+            if (k == fst) {
+                sm.wX[slot] = in.X;
+                sm.wr[slot] = in.r;
+                sm.wi[slot] = in.i;
+                sm.wuy[slot] = in.uy;
+                if (LEARN) ls->wenv[slot] = env;
+                sm.wl[atomicAdd(&sm.nw, 1)] = slot;
+            } else if (t % m == 0 && fst == INT_MAX) {
+                if (kb + m - 1 >= n_try) {
+                    if (LEARN) {  // the proposal's trials ran out: the plain sampler decides
+                        ls->fb[atomicAdd(&ls->nfb, 1)] = slot;
+                        st.trials += (unsigned int)n_try;
+                        st.fail++;
+                    } else {
+                        set_error(sc, CMCG_ERR_NTRY, j0 + slot);  // n_try trials, none accepted
+                    }
+                } else {
+                    sm.next[slot] = kb + m;
+                    sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = slot;
+                }
+            }
+        }
+        __syncthreads();
+        // 3. the candidates evaluated exactly, one star per thread
+        if (t < sm.nw) {
+            const int s = sm.wl[t];
+            const int kk = sm.first[s];
+            TrialIn cin;
+            cin.X = sm.wX[s];
+            cin.r = sm.wr[s];
+            cin.i = sm.wi[s];
+            cin.uy = sm.wuy[s];
+            cin.ux = 0u;  // not used by the exact evaluation
+            const Trial tr = LEARN ? learned_eval(C, sc, f, sm, s, cin, ls->wenv[s], invN)
+                                   : eval_trial(C, sc, f, sm, s, cin, invN);
+            if (tr.code == TRIAL_ACCEPT) {
+                commit_trial(C, sc, f, sm, s, off + j0 + s, tr, max_rad);
+                if (MODE == 2) {
+                    L.ntrial[off + j0 + s] = LEARN ? -kk : kk;
+                    if (LEARN) {
+                        st.trials += (unsigned int)kk;
+                        st.acc++;
+                    } else {
+                        st.ptrials += (unsigned int)kk;
+                        st.pstars++;
+                    }
+                }
+            } else if (LEARN && (tr.code == TRIAL_FAIL || (tr.code == TRIAL_REJECT && kk >= n_try))) {
+                ls->fb[atomicAdd(&ls->nfb, 1)] = s;
+                st.trials += (unsigned int)kk;
+                st.fail++;
+            } else if (tr.code != TRIAL_REJECT) {
+                set_error(sc, tr.code, j0 + s);
+            } else if (kk >= n_try) {
+                set_error(sc, CMCG_ERR_NTRY, j0 + s);
+            } else {
+                // the filter was unsure and the trial is rejected: go on from the next one
+                sm.first[s] = INT_MAX;
+                sm.next[s] = kk + 1;
+                sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = s;
+            }
+        }
+        __syncthreads();
+    }
 }
 
 // One star's sampling state in the block's shared memory.
@@ -854,74 +1032,28 @@ static __device__ __forceinline__ void orbit_body(const Cluster *__restrict__ cl
     }
     const int t = threadIdx.x;
     const long long j0 = 1 + (long long)ct.y * ORB_T;
-    const long long n_try = C.n_try;
-    const bool check = C.check_filters != 0;
     if (MODE == 2 && L.mode == LEARN_ON && t == 0 && ct.y == 0 && *L.mlp_status != 0)
         set_error(sc, CMCG_ERR_SPIN, 0);  // the network's inference gave up: its proposals are not valid
-    unsigned int st_trials = 0, st_acc = 0, st_fail = 0, st_ptrials = 0, st_pstars = 0;
+    // rejection sampling in rounds over the block's pending stars
+    if (t == 0) {
+        sm.n[0] = 0;
+        if (MODE == 2) ls->nfb = 0;
+    }
+    __syncthreads();
+    if (pend) {
+        const int p = atomicAdd(&sm.n[0], 1);
+        sm.list[0][p] = t;
+        sm.next[t] = 1;
+        sm.first[t] = INT_MAX;
+    }
+    __syncthreads();
+    LStat st;
     if (MODE == 2 && L.mode == LEARN_ON) {
-        // proposal rounds: each pending star's next m trials at once; the first
-        // trial that accepts or fails decides the star
-        if (t == 0) {
-            sm.n[0] = 0;
-            sm.nw = 0;  // stars sent back to the plain sampler collect in wl
-        }
-        __syncthreads();
-        if (pend) {
-            const int p = atomicAdd(&sm.n[0], 1);
-            sm.list[0][p] = t;
-            sm.next[t] = 1;
-            sm.first[t] = INT_MAX;
-        }
-        __syncthreads();
-        for (int cur = 0;; cur ^= 1) {
-            const int n = sm.n[cur];
-            if (n == 0) break;
-            const int m = ORB_T / n;
-            if (t == 0) sm.n[cur ^ 1] = 0;
-            int slot = -1, k = 0, kb = 0;
-            Trial tr;
-            tr.code = TRIAL_REJECT;
-            if (t < n * m) {
-                slot = sm.list[cur][t / m];
-                kb = sm.next[slot];
-                k = kb + t % m;
-                if (k <= n_try) {
-                    tr = learned_trial(C, sc, f, sm, *ls, slot, k, invN, L.kappa);
-                    if (tr.code != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
-                }
-            }
-            __syncthreads();
-            if (slot >= 0) {
-                const int fst = sm.first[slot];
-                if (k == fst) {
-                    st_trials += (unsigned int)k;
-                    if (tr.code == TRIAL_ACCEPT) {
-                        commit_trial(C, sc, f, sm, slot, off + j0 + slot, tr, &max_rad);
-                        L.ntrial[off + j0 + slot] = -k;
-                        st_acc++;
-                    } else if (tr.code == TRIAL_FAIL) {
-                        sm.wl[atomicAdd(&sm.nw, 1)] = slot;
-                        st_fail++;
-                    } else {
-                        set_error(sc, tr.code, j0 + slot);
-                    }
-                } else if (t % m == 0 && fst == INT_MAX) {
-                    if (kb + m - 1 >= n_try) {  // the proposal's trials ran out: the plain sampler decides
-                        st_trials += (unsigned int)n_try;
-                        sm.wl[atomicAdd(&sm.nw, 1)] = slot;
-                        st_fail++;
-                    } else {
-                        sm.next[slot] = kb + m;
-                        sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = slot;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-        const int nfb = sm.nw;
+        sample_rounds<MODE, true>(C, sc, f, sm, ls, L, j0, invN, &max_rad, st);
+        // the stars sent back start the plain trials from the first
+        const int nfb = ls->nfb;
         if (t < nfb) {
-            const int s = sm.wl[t];
+            const int s = ls->fb[t];
             sm.list[0][t] = s;
             sm.next[s] = 1;
             sm.first[s] = INT_MAX;
@@ -929,100 +1061,16 @@ static __device__ __forceinline__ void orbit_body(const Cluster *__restrict__ cl
         __syncthreads();
         if (t == 0) sm.n[0] = nfb;
         __syncthreads();
-    } else {
-        // rejection sampling in rounds over the block's pending stars
-        if (t == 0) sm.n[0] = 0;
-        __syncthreads();
-        if (pend) {
-            const int p = atomicAdd(&sm.n[0], 1);
-            sm.list[0][p] = t;
-            sm.next[t] = 1;
-            sm.first[t] = INT_MAX;
-        }
-        __syncthreads();
     }
-    for (int cur = 0;; cur ^= 1) {
-        const int n = sm.n[cur];
-        if (n == 0) break;
-        const int m = ORB_T / n;  // trials per pending star this round
-        if (t == 0) {
-            sm.n[cur ^ 1] = 0;  // last read at the top of the previous round
-            sm.nw = 0;
-        }
-        // 1. the filter on each star's next m trials
-        int slot = -1, k = 0, kb = 0;
-        TrialIn in;
-        if (t < n * m) {
-            slot = sm.list[cur][t / m];
-            kb = sm.next[slot];
-            k = kb + t % m;
-            if (k <= n_try) {
-                in = trial_input(C, sc, sm, slot, k);
-                const int dec = filter_trial(C, sc, f, sm, slot, in);
-                if (dec != TRIAL_REJECT) atomicMin(&sm.first[slot], k);
-                if (check && dec != TRIAL_UNSURE && eval_trial(C, sc, f, sm, slot, in, invN).code != dec)
-                    set_error(sc, CMCG_ERR_FILTER, j0 + slot);
-            }
-        }
-        __syncthreads();
-        // 2. candidates listed (with their inputs); stars whose m trials were all rejected go on
-        if (slot >= 0) {
-            const int fst = sm.first[slot];
-            if (k == fst) {
-                sm.wX[slot] = in.X;
-                sm.wr[slot] = in.r;
-                sm.wi[slot] = in.i;
-                sm.wuy[slot] = in.uy;
-                sm.wl[atomicAdd(&sm.nw, 1)] = slot;
-            } else if (t % m == 0 && fst == INT_MAX) {
-                if (kb + m - 1 >= n_try) {
-                    set_error(sc, CMCG_ERR_NTRY, j0 + slot);  // n_try trials, none accepted
-                } else {
-                    sm.next[slot] = kb + m;
-                    sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = slot;
-                }
-            }
-        }
-        __syncthreads();
-        // 3. the candidates evaluated exactly, one star per thread
-        if (t < sm.nw) {
-            const int s = sm.wl[t];
-            const int kk = sm.first[s];
-            TrialIn cin;
-            cin.X = sm.wX[s];
-            cin.r = sm.wr[s];
-            cin.i = sm.wi[s];
-            cin.uy = sm.wuy[s];
-            cin.ux = 0u;  // not used by the exact evaluation
-            const Trial tr = eval_trial(C, sc, f, sm, s, cin, invN);
-            if (tr.code == TRIAL_ACCEPT) {
-                commit_trial(C, sc, f, sm, s, off + j0 + s, tr, &max_rad);
-                if (MODE == 2) {
-                    L.ntrial[off + j0 + s] = kk;
-                    st_ptrials += (unsigned int)kk;
-                    st_pstars++;
-                }
-            } else if (tr.code != TRIAL_REJECT) {
-                set_error(sc, tr.code, j0 + s);
-            } else if (kk >= n_try) {
-                set_error(sc, CMCG_ERR_NTRY, j0 + s);
-            } else {
-                // the filter was unsure and the trial is rejected: go on from the next one
-                sm.first[s] = INT_MAX;
-                sm.next[s] = kk + 1;
-                sm.list[cur ^ 1][atomicAdd(&sm.n[cur ^ 1], 1)] = s;
-            }
-        }
-        __syncthreads();
-    }
+    sample_rounds<MODE, false>(C, sc, f, sm, ls, L, j0, invN, &max_rad, st);
     if (MODE == 2) {
         __shared__ unsigned int s_w[ORB_T / 32];
-        add_stat(L.stats + LSTAT_TRIALS, st_trials, s_w);
-        add_stat(L.stats + LSTAT_ACCEPT, st_acc, s_w);
-        add_stat(L.stats + LSTAT_FAIL, st_fail, s_w);
+        add_stat(L.stats + LSTAT_TRIALS, st.trials, s_w);
+        add_stat(L.stats + LSTAT_ACCEPT, st.acc, s_w);
+        add_stat(L.stats + LSTAT_FAIL, st.fail, s_w);
         add_stat(L.stats + LSTAT_STARS, (L.mode == LEARN_ON && pend) ? 1u : 0u, s_w);
-        add_stat(L.stats + LSTAT_PLAIN_TRIALS, st_ptrials, s_w);
-        add_stat(L.stats + LSTAT_PLAIN_STARS, st_pstars, s_w);
+        add_stat(L.stats + LSTAT_PLAIN_TRIALS, st.ptrials, s_w);
+        add_stat(L.stats + LSTAT_PLAIN_STARS, st.pstars, s_w);
     }
     // escapers are rare: most warps skip the sums (block_sums)
     __shared__ double s_acc[ORB_T / 32][4];
@@ -1079,7 +1127,7 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit_aps(const Cluster *__restric
     orbit_body<1>(cls, tm, f, partials, tickets, pq, L, sm, nullptr);
 }
 
-__global__ void __launch_bounds__(ORB_T, 4) k_orbit_learn(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+__global__ void __launch_bounds__(ORB_T, 5) k_orbit_learn(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                        double *partials, unsigned int *tickets, PosQ pq, Learn L)
 {
     __shared__ SampleSmem sm;

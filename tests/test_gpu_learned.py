@@ -203,3 +203,22 @@ def test_learned_proposal_samples_the_plain_distribution(trained):
     # the plain sampler share its draws, which only makes the test milder)
     p = ks_2samp(Xa, Xb).pvalue
     assert p > 0.01, (p, st)
+
+
+@pytest.mark.parametrize("model,N,imf", [(cmcgpu.PLUMMER, 50000, 0), (cmcgpu.KING, 50000, 1)])
+def test_learned_filter_decisions_match_exact(trained, model, N, imf):
+    """Every certified FP32 decision of a proposal trial (accept, or reject,
+    with the envelope certainly holding) is re-evaluated exactly
+    (check_filters); a disagreement is CMCG_ERR_FILTER."""
+    ic = cmcgpu.generate(model, N, seed=71, imf=imf)
+    g = cmcgpu.Context([N], cmcgpu.default_params(orbit_r=ic["rtid"], seed=72, check_filters=1))
+    g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    g.initialize()
+    g.mlp_set_params(trained["w"])
+    for kappa in (1.05, 1.2, 2.0):
+        g.set_learned(cmcgpu.LEARN_ON, kappa=kappa)
+        g.step(1)
+        g.check_device(f"learned step, kappa {kappa}")
+        st = g.learned_stats()
+        assert st["accepted"] > 0.5 * st["stars"], st  # tight envelopes send more stars back
+    g.close()

@@ -8,10 +8,11 @@
 //
 // Keys are the IEEE bit patterns of rnew (positive doubles order like their
 // bits) less the cluster's smallest, with every escaper (rnew = SF_INFINITY)
-// one past the largest bound key; values the star's slot.  The digit passes
-// sort the keys' top 24 bits (3 passes); keys that share them then form runs
-// in input order, which k_sort_fix sorts by the full key (runs are a star or
-// two at the densities of these clusters).
+// at the first key of the 24-bit prefix after the largest bound key's;
+// values the star's slot.  The digit passes sort the keys' top 24 bits (3
+// passes); keys that share them then form runs in input order, which
+// k_sort_fix sorts by the full key (runs are a star or two at the densities
+// of these clusters; the escapers' run is equal keys, already in order).
 //   k_sort_ghist     every 8-bit digit's histogram in one read of the keys
 //   k_sort_onesweep  one kernel per digit pass: stable in-tile ranking (warp
 //                    match + per-warp counters), tile offsets by decoupled
@@ -110,26 +111,39 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
                 n += s_cnt[q];
             }
             sc->n_bound = n;
-            // sort keys: a bound star's bit pattern minus the smallest one, an
-            // escaper one past the largest (escapers sort after every bound
-            // star, in input order); only the digits that span the range pass
+            // sort keys: a bound star's bit pattern minus the smallest one; the
+            // digit passes sort the top SORT_PREFIX_BITS bits of the range
+            // (bits below the shift are left to k_sort_fix).  Escapers all take
+            // the first key of the prefix after the largest bound key's: they
+            // sort after every bound star as a run of equal keys of their own,
+            // which the stable passes leave in input order.
             unsigned long long top = 0ull;
+            int sh = 0;
             if (n == 0) {
                 a = inf_bits;  // every key the same: nothing to sort
             } else {
-                top = (b - a) + (n < N ? 1ull : 0ull);
+                const unsigned long long R = b - a;
+                const int bitsR = R ? 64 - __clzll((long long)R) : 0;
+                sh = bitsR > SORT_PREFIX_BITS ? bitsR - SORT_PREFIX_BITS : 0;
+                top = R;
+                if (n < N) {
+                    for (;;) {  // at most one more bit of range: settles in two turns
+                        top = ((R >> sh) + 1ull) << sh;
+                        if (64 - __clzll((long long)top) - sh <= SORT_PREFIX_BITS) break;
+                        ++sh;
+                    }
+                }
             }
             sb.kmin[ct.x] = a;
             sb.kmax[ct.x] = top;
             const int bits = top ? 64 - __clzll((long long)top) : 0;
-            const int sh = bits > SORT_PREFIX_BITS ? bits - SORT_PREFIX_BITS : 0;
             sb.shift[ct.x] = sh;
             sb.npass[ct.x] = (bits - sh + 7) / 8;
         }
     }
 }
 
-// The sort key of a radius (k_sort_prep): bits - kmin, escapers kmax.
+// The sort key of a radius (k_sort_prep): bits - kmin, escapers the key kmax.
 static __device__ __forceinline__ unsigned long long radius_key(double r, unsigned long long kmin,
                                                                 unsigned long long kesc)
 {
@@ -360,11 +374,14 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_fix(const Cluster *__rest
     const long long N = C.sc->N_MAX_NEW;
     unsigned long long *K = ((np & 1) ? sb.keys[1] : sb.keys[0]) + C.off;
     unsigned int *V = ((np & 1) ? sb.vals[1] : sb.vals[0]) + C.off;
+    // the escapers' run: equal keys, already in input order
+    const unsigned long long pesc = C.sc->n_bound < N ? sb.kmax[ct.x] >> sh : ~0ull;
     for (int it = 0; it < SORT_T / SORT_THREADS; ++it) {
         const long long i = (long long)ct.y * SORT_T + it * SORT_THREADS + threadIdx.x;
         if (i >= N) break;
         const unsigned long long p = K[i] >> sh;
         if (i > 0 && (K[i - 1] >> sh) == p) continue;  // not a run start
+        if (p == pesc) continue;
         long long j = i + 1;
         bool sorted = true;
         unsigned long long prev = K[i];

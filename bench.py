@@ -309,8 +309,11 @@ def learned_leg(a, cfg, clusters, params, ctx, timed, stars):
     ctx.step(a.warmup)
     ctx.check_device("learned warmup")
     n0 = stars()
+    ncl = len(clusters)
+    e_start = [ctx.scalar("Etot", c) for c in range(ncl)]
     ms, launches = timed(a.steps, True)
     ctx.check_device("learned steps")
+    drift = [(ctx.scalar("Etot", c) - e0) / abs(e0) / a.steps for c, e0 in enumerate(e_start)]
     st = ctx.learned_stats()
     ctx.profile(True)
     ctx.kernel_time("reset")
@@ -343,6 +346,8 @@ def learned_leg(a, cfg, clusters, params, ctx, timed, stars):
         "kappa": a.kappa,
         "value": n0 * a.steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / a.steps,
         "gpu_launches": launches,
+        "energy": {"rel_drift_per_step": drift[0] if ncl == 1 else None,
+                   "max_abs_rel_drift_per_step": max(abs(d) for d in drift)},
         "trials_per_star": trials, "plain_trials_per_star": float(nta.mean()),
         "failed_frac": stb["failed"] / max(stb["stars"], 1),
         "ks_p_X": float(ks_2samp(Xa, Xb).pvalue), "ks_samples": [int(len(Xa)), int(len(Xb))],
@@ -491,7 +496,7 @@ def run_ours(a, rank, ws, dist):
         "profiled_ms_per_step": ms_prof / a.steps,
         "clocks": clk,
     }
-    if a.learned and rank == 0 and ws == 1:
+    if not a.no_learned and rank == 0 and ws == 1:
         try:
             out["learned"] = learned_leg(a, cfg, clusters, params, ctx, timed, stars)
         except Exception as e:  # the headline stands without it
@@ -511,8 +516,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000, help="stars per CPU-baseline process")
     ap.add_argument("--cpu-steps", type=int, default=2, help="timed oracle steps of the 1-core CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--learned", action="store_true",
-                    help="also train the proposal network and time the learned-proposal step")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip training the proposal network and timing the learned-proposal step")
     ap.add_argument("--kappa", type=float, default=1.2, help="envelope factor of the learned proposal")
     ap.add_argument("--learn-records", type=int, default=20_000_000, help="plain-sampler records to train on")
     ap.add_argument("--learn-steps", type=int, default=2500, help="Adam steps of batch 8192")

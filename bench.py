@@ -305,6 +305,7 @@ def learned_leg(a, cfg, clusters, params, ctx, timed, stars):
     w, info = train_proposal(a)
     ctx.mlp_set_params(w)
     ctx.set_learned(cmcgpu.LEARN_ON, a.kappa)
+    tuned = ctx.autotune(2) if not a.no_autotune else "off"
     ctx.use_graph(True)
     ctx.step(a.warmup)
     ctx.check_device("learned warmup")
@@ -348,6 +349,7 @@ def learned_leg(a, cfg, clusters, params, ctx, timed, stars):
         "gpu_launches": launches,
         "energy": {"rel_drift_per_step": drift[0] if ncl == 1 else None,
                    "max_abs_rel_drift_per_step": max(abs(d) for d in drift)},
+        "autotune": tuned,
         "trials_per_star": trials, "plain_trials_per_star": float(nta.mean()),
         "failed_frac": stb["failed"] / max(stb["stars"], 1),
         "ks_p_X": float(ks_2samp(Xa, Xb).pvalue), "ks_samples": [int(len(Xa)), int(len(Xb))],
@@ -394,6 +396,8 @@ def run_ours(a, rank, ws, dist):
         e1.synchronize()
         return e0.elapsed_time(e1), ctx.launch_count()
 
+    # launch variants picked by measurement on this context (real steps)
+    tuned = ctx.autotune(2) if not a.no_autotune else "off"
     # warm-up in the timed mode (the first step captures the graph)
     ctx.use_graph(True)
     ctx.step(a.warmup)
@@ -477,6 +481,7 @@ def run_ours(a, rank, ws, dist):
         "config": {"workload": cfg["desc"], "name": a.config, "N": N if ncl == 1 else None, "clusters": ncl,
                    "stars_at_start": n_start, "parallelism": f"replicas x{ws}",
                    "timing": "CUDA events on the library's stream; whole step replayed from a CUDA graph",
+                   "autotune": tuned,
                    "l2": "state ~250 B/star exceeds the 129 MB L2 at this size: no flush needed"
                          if n_start * 250 > 129e6 else "L2 holds the state: steps read warm data"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // a.steps,
@@ -519,6 +524,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true",
                     help="skip training the proposal network and timing the learned-proposal step")
     ap.add_argument("--kappa", type=float, default=1.2, help="envelope factor of the learned proposal")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch variants")
     ap.add_argument("--learn-records", type=int, default=20_000_000, help="plain-sampler records to train on")
     ap.add_argument("--learn-steps", type=int, default=2500, help="Adam steps of batch 8192")
     ap.add_argument("--probe-rates", action="store_true",

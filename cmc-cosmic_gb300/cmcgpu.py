@@ -235,6 +235,9 @@ def lib() -> C.CDLL:
         L.cmcg_learned_samples.argtypes = [vp, i, vp, vp, vp, l]
         L.cmcg_learned_samples.restype = l
         L.cmcg_learned_stats.argtypes = [vp, vp]
+        L.cmcg_autotune.argtypes = [vp, i, C.c_char_p, l]
+        L.cmcg_set_variant.argtypes = [vp, C.c_char_p, i]
+        L.cmcg_get_variant.argtypes = [vp, C.c_char_p]
         _lib = L
     return _lib
 
@@ -459,6 +462,22 @@ class Context:
         out = np.zeros(8, np.uint64)
         self._check(lib().cmcg_learned_stats(self._h, out.ctypes.data), "cmcg_learned_stats")
         return {k: int(out[i]) for i, k in enumerate(LSTAT_NAMES)}
+
+    # -- autotuner
+    def autotune(self, steps: int = 2) -> str:
+        """Time each launch variant over `steps` steps (real steps of the run), keep the fastest."""
+        buf = C.create_string_buffer(1024)
+        self._check(lib().cmcg_autotune(self._h, steps, buf, len(buf)), "cmcg_autotune")
+        return buf.value.decode()
+
+    def set_variant(self, name: str, v: int):
+        self._check(lib().cmcg_set_variant(self._h, name.encode(), v), "cmcg_set_variant")
+
+    def variant(self, name: str) -> int:
+        v = lib().cmcg_get_variant(self._h, name.encode())
+        if v < 0:
+            raise KeyError(name)
+        return v
 
     def initialize(self):
         self._check(lib().cmcg_initialize(self._h), "initialize")

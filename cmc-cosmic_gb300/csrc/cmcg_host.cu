@@ -31,6 +31,21 @@ enum Family { F_BEGIN, F_TIMESTEP, F_RELAX, F_ORBIT, F_TIDAL, F_SORT, F_POT, F_E
 const char *kFamilyNames[F_COUNT] = {"begin", "timestep", "relax", "orbit", "tidal",
                                      "sort",  "potential", "ec3", "energy", "end", "mlp"};
 
+// Autotuner candidates: per tunable launch, its variants and the kernel family timed.
+const int kMlpGrid[4] = {4, 2, 3, 6};  // persistent CTAs per SM of the network's inference
+struct Tunable {
+    const char *name;
+    int family;
+    int nvar;
+    const char *variant[4];
+};
+const Tunable kTunables[V_COUNT] = {
+    {"orbit", F_ORBIT, 2, {"5 blocks/SM", "4 blocks/SM"}},
+    {"relax", F_RELAX, 2, {"5 blocks/SM", "4 blocks/SM"}},
+    {"orbit_learn", F_ORBIT, 2, {"5 blocks/SM", "4 blocks/SM"}},
+    {"mlp_grid", F_MLP, 4, {"4 CTAs/SM", "2 CTAs/SM", "3 CTAs/SM", "6 CTAs/SM"}},
+};
+
 struct ProfRec {
     int fam;
     cudaEvent_t a, b;
@@ -76,6 +91,8 @@ struct cmcg_ctx {
     double learn_kappa = 1.2;
     Learn lrn{};
     void *lrn_mem = nullptr;
+    // launch variants (autotuner; every variant gives bit-identical results)
+    int var[V_COUNT] = {0, 0, 0, 0};
     // graphs
     // The sort swaps the field pointers every step, so a captured two-step
     // graph is tied to the pointer parity it was captured at: one per parity.
@@ -640,8 +657,8 @@ static int L_relax(cmcg_ctx *c, double dt)
         k_relax32<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials,
                                                                     c->tickets, dt);
     else
-        k_relax64<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials,
-                                                                    c->tickets, dt);
+        (c->var[V_RELAX] ? k_relax64_lb4 : k_relax64)<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(
+            c->d_cls, c->t256.view(), c->f, c->partials, c->tickets, dt);
     fam_end(c);
     c->launches += 1;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
@@ -654,8 +671,8 @@ static int L_orbit(cmcg_ctx *c)
     k_orbit_pre<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->pq);
     k_posq_scan<<<c->posq_grid, 256, 0, c->stream>>>(c->d_cls, c->f, c->pq);
     if (c->learn_mode == LEARN_OFF) {
-        k_orbit<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials, c->tickets,
-                                                         c->pq);
+        (c->var[V_ORBIT] ? k_orbit_lb4 : k_orbit)<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(
+            c->d_cls, c->t128.view(), c->f, c->partials, c->tickets, c->pq);
         c->launches += 3;
     } else {
         // apsides and features; the network on every star slot; the sampling
@@ -669,15 +686,15 @@ static int L_orbit(cmcg_ctx *c)
             fam_end(c);
             fam_begin(c, F_MLP);
             const long long ntl = (c->total + MLP_T - 1) / MLP_T;
-            const int grid = (int)std::min<long long>(ntl, 4LL * c->nsm);
+            const int grid = (int)std::min<long long>(ntl, (long long)kMlpGrid[c->var[V_MLP_GRID]] * c->nsm);
             k_mlp_infer<<<grid, MLP_T, MLP_INFER_SMEM, c->stream>>>(c->net, L.feat, c->total, L.prop, L.stride,
                                                                     nullptr);
             c->launches += 1;
             fam_end(c);
             fam_begin(c, F_ORBIT);
         }
-        k_orbit_learn<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->partials,
-                                                               c->tickets, c->pq, L);
+        (c->var[V_LEARN] ? k_orbit_learn_lb4 : k_orbit_learn)<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(
+            c->d_cls, c->t128.view(), c->f, c->partials, c->tickets, c->pq, L);
         c->launches += 4;
     }
     fam_end(c);
@@ -1482,6 +1499,77 @@ int cmcg_learned_stats(cmcg_ctx *c, uint64_t *out)
     }
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemcpy(out, c->lrn.stats, LSTAT_N * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    return CMCG_OK;
+}
+
+// ------------------------------------------------------------ autotuner --
+int cmcg_set_variant(cmcg_ctx *c, const char *name, int v)
+{
+    if (!c || !name) return CMCG_ERR_ARG;
+    for (int t = 0; t < V_COUNT; ++t) {
+        if (strcmp(name, kTunables[t].name)) continue;
+        if (v < 0 || v >= kTunables[t].nvar) return CMCG_ERR_ARG;
+        if (c->var[t] != v) drop_graphs(c);  // another launch sequence
+        c->var[t] = v;
+        return CMCG_OK;
+    }
+    return CMCG_ERR_ARG;
+}
+
+int cmcg_get_variant(cmcg_ctx *c, const char *name)
+{
+    if (!c || !name) return CMCG_ERR_ARG;
+    for (int t = 0; t < V_COUNT; ++t)
+        if (!strcmp(name, kTunables[t].name)) return c->var[t];
+    return CMCG_ERR_ARG;
+}
+
+// Times every variant of the launches the current configuration uses, over
+// `steps` whole steps each (after one untimed step), with CUDA events around
+// the tuned kernel family, and keeps the fastest.  The steps are real steps
+// of the run: the variants give bit-identical results.
+int cmcg_autotune(cmcg_ctx *c, int steps, char *report, long report_len)
+{
+    if (!c || steps < 1) return CMCG_ERR_ARG;
+    std::string rep;
+    const bool prof0 = c->profile;
+    for (int t = 0; t < V_COUNT; ++t) {
+        const bool used = (t == V_ORBIT && c->learn_mode == LEARN_OFF) || (t == V_RELAX && !c->relax_fp32) ||
+                          (t == V_LEARN && c->learn_mode != LEARN_OFF) ||
+                          (t == V_MLP_GRID && c->learn_mode == LEARN_ON);
+        if (!used) continue;
+        const Tunable &T = kTunables[t];
+        int best = c->var[t];
+        double best_ms = 1e300;
+        char buf[160];
+        snprintf(buf, sizeof buf, "%s:", T.name);
+        rep += buf;
+        for (int v = 0; v < T.nvar; ++v) {
+            c->var[t] = v;
+            c->profile = false;
+            RUN(issue_step(c));
+            c->profile = true;
+            RUN(cmcg_kernel_time(c, "reset", nullptr, nullptr));
+            for (int k = 0; k < steps; ++k) RUN(issue_step(c));
+            double ms = 0.0;
+            long n = 0;
+            RUN(cmcg_kernel_time(c, kFamilyNames[T.family], &ms, &n));
+            ms /= steps;
+            snprintf(buf, sizeof buf, " %s %.4f ms", T.variant[v], ms);
+            rep += buf;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = v;
+            }
+        }
+        c->var[t] = best;
+        snprintf(buf, sizeof buf, " -> %s; ", T.variant[best]);
+        rep += buf;
+    }
+    c->profile = prof0;
+    drop_graphs(c);
+    RUN(cmcg_kernel_time(c, "reset", nullptr, nullptr));
+    if (report && report_len > 0) snprintf(report, (size_t)report_len, "%s", rep.c_str());
     return CMCG_OK;
 }
 

@@ -102,6 +102,8 @@ __global__ void k_relax64(const Cluster *cls, Tiles tm, Fields f, double *partia
                           double dt_override);
 __global__ void k_relax32(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                           double dt_override);
+__global__ void k_relax64_lb4(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
+                              double dt_override);
 // Stars whose Q(j) <= 0 and the first index with Q > 0 found for each (k_posq_scan)
 struct PosQ {
     int *slot;            // per star: PQ_POSITIVE (Q(j) > 0), a list entry, or PQ_SCAN_HERE
@@ -113,6 +115,7 @@ constexpr int PQ_POSITIVE = -1, PQ_SCAN_HERE = -2, PQ_CAP = 1024;
 __global__ void k_orbit_pre(const Cluster *cls, Tiles tm, Fields f, PosQ pq);
 __global__ void k_posq_scan(const Cluster *cls, Fields f, PosQ pq);
 __global__ void k_orbit(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets, PosQ pq);
+__global__ void k_orbit_lb4(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets, PosQ pq);
 
 // ---- learned proposal of the orbit sampler (cmcg_mlp.cu, cmcg_orbit.cu)
 // An MLP 8 -> 64 -> 64 -> 33 (ReLU; BF16 weights and activations, FP32
@@ -181,6 +184,11 @@ __global__ void k_orbit_aps(const Cluster *cls, Tiles tm, Fields f, double *part
                             Learn L);
 __global__ void k_orbit_learn(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                               PosQ pq, Learn L);
+__global__ void k_orbit_learn_lb4(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
+                                  PosQ pq, Learn L);
+
+// ---- launch variants the autotuner chooses between (bit-identical results)
+enum { V_ORBIT, V_RELAX, V_LEARN, V_MLP_GRID, V_COUNT };
 __global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *bar, int nclusters);
 __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, double *partials,
                             unsigned int *tickets);

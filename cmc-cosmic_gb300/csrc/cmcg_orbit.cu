@@ -1120,6 +1120,16 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
     orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr);
 }
 
+// The same kernel with room for 128 registers a thread (four blocks per SM):
+// an autotuner candidate, with bit-identical results.
+__global__ void __launch_bounds__(ORB_T, 4) k_orbit_lb4(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                     double *partials, unsigned int *tickets, PosQ pq)
+{
+    __shared__ SampleSmem sm;
+    const Learn none{};
+    orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr);
+}
+
 __global__ void __launch_bounds__(ORB_T, 5) k_orbit_aps(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                      double *partials, unsigned int *tickets, PosQ pq, Learn L)
 {
@@ -1129,6 +1139,14 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit_aps(const Cluster *__restric
 
 __global__ void __launch_bounds__(ORB_T, 5) k_orbit_learn(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                        double *partials, unsigned int *tickets, PosQ pq, Learn L)
+{
+    __shared__ SampleSmem sm;
+    __shared__ LearnSmem ls;
+    orbit_body<2>(cls, tm, f, partials, tickets, pq, L, sm, &ls);
+}
+
+__global__ void __launch_bounds__(ORB_T, 4) k_orbit_learn_lb4(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                           double *partials, unsigned int *tickets, PosQ pq, Learn L)
 {
     __shared__ SampleSmem sm;
     __shared__ LearnSmem ls;

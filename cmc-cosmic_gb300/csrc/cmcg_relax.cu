@@ -398,6 +398,14 @@ __global__ void __launch_bounds__(RELAX_THREADS, 5) k_relax64(const Cluster *__r
     relax_body<false>(cls, tm, f, partials, tickets, dt);
 }
 
+// Four blocks per SM (room for 128 registers): an autotuner candidate.
+__global__ void __launch_bounds__(RELAX_THREADS, 4) k_relax64_lb4(const Cluster *__restrict__ cls, Tiles tm,
+                                                               Fields f, double *partials, unsigned int *tickets,
+                                                               double dt)
+{
+    relax_body<false>(cls, tm, f, partials, tickets, dt);
+}
+
 __global__ void __launch_bounds__(RELAX_THREADS) k_relax32(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                            double *partials, unsigned int *tickets, double dt)
 {

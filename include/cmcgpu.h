@@ -250,6 +250,19 @@ int cmcg_mlp_train(cmcg_ctx *ctx, const float *feat, const int *bin, const int *
 long cmcg_learned_samples(cmcg_ctx *ctx, int k, float *feat, double *X, int *ntrial, long cap);
 int cmcg_learned_stats(cmcg_ctx *ctx, uint64_t *out /* CMCG_LSTAT_N */);
 
+/* ------------------------------------------------------- autotuner -----
+ * Launch variants with bit-identical results, chosen by measurement on the
+ * context's own clusters: "orbit" and "relax" (5 or 4 blocks per SM, i.e.
+ * register budgets of 102 or 128), "orbit_learn" (the same for the learned
+ * sampling pass) and "mlp_grid" (persistent CTAs per SM of the network's
+ * inference: 4, 2, 3, 6).  cmcg_autotune times every variant of the
+ * launches the current configuration uses over `steps` steps each (plus one
+ * untimed step), keeps the fastest, and writes a one-line report (may be
+ * NULL).  The tuning steps are real steps of the run. */
+int cmcg_autotune(cmcg_ctx *ctx, int steps, char *report, long report_len);
+int cmcg_set_variant(cmcg_ctx *ctx, const char *name, int variant);
+int cmcg_get_variant(cmcg_ctx *ctx, const char *name);   /* the variant, or CMCG_ERR_ARG */
+
 /* ------------------------------------------------- step diagnostics ---
  * What the reference writes to dyn.dat and lagrad.dat every step
  * (PrintFileOutput, cmc_io.c:260-323), reduced on the device from the

@@ -100,6 +100,11 @@ def lagrad_line(d: "Diag") -> str:
     return _fmt(lib().cmcg_format_lagrad_line, C.byref(d))
 
 
+class Stars(C.Structure):
+    """cmcg_stars: one cluster's host star arrays for cmcg_step_host."""
+    _fields_ = [("N", C.c_long), ("cap", C.c_long)] + [(k, C.c_void_p) for k in ("r", "m", "vr", "vt", "E", "J", "id")]
+
+
 class ICSpec(C.Structure):
     _fields_ = [("model", C.c_int), ("N", C.c_long), ("w0", C.c_double), ("imf", C.c_int),
                 ("binary_fraction", C.c_double), ("seed", C.c_uint64)]
@@ -236,6 +241,7 @@ def lib() -> C.CDLL:
         L.cmcg_learned_samples.restype = l
         L.cmcg_learned_stats.argtypes = [vp, vp]
         L.cmcg_autotune.argtypes = [vp, i, C.c_char_p, l]
+        L.cmcg_step_host.argtypes = [vp, C.POINTER(Stars), C.POINTER(Stars)]
         L.cmcg_set_variant.argtypes = [vp, C.c_char_p, i]
         L.cmcg_get_variant.argtypes = [vp, C.c_char_p]
         _lib = L
@@ -540,6 +546,19 @@ class Context:
         """Upload host star state (arrays r, m, vr, vt, E, J, id; m already x N_STAR)."""
         a = [bufs[k].ctypes.data for k in ("r", "m", "vr", "vt", "E", "J", "id")]
         self._check(lib().cmcg_put_stars(self._h, cluster, n, *a), "put_stars")
+
+    def step_host(self, ins, outs):
+        """One step on host arrays: ins[k] = (n, bufs) per cluster, outs[k] = bufs
+        (arrays r, m, vr, vt, E, J, id; cmcg_step_host).  Returns the star
+        counts after the step."""
+        keys = ("r", "m", "vr", "vt", "E", "J", "id")
+        a = (Stars * self.n)()
+        b = (Stars * self.n)()
+        for k, ((n, bi), bo) in enumerate(zip(ins, outs)):
+            a[k] = Stars(n, len(bi["r"]), *[bi[x].ctypes.data for x in keys])
+            b[k] = Stars(0, len(bo["r"]), *[bo[x].ctypes.data for x in keys])
+        self._check(lib().cmcg_step_host(self._h, a, b), "cmcg_step_host")
+        return [int(b[k].N) for k in range(self.n)]
 
     def get_stars(self, cluster: int, bufs: dict) -> int:
         cap = len(bufs["r"])

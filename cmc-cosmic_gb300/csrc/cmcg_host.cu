@@ -93,6 +93,14 @@ struct cmcg_ctx {
     void *lrn_mem = nullptr;
     // launch variants (autotuner; every variant gives bit-identical results)
     int var[V_COUNT] = {0, 0, 0, 0};
+    // host exchange (cmcg_step_host): the step as two graphs, before and after
+    // the sort, per pointer parity at their start; a copy stream for the
+    // read-back that overlaps the second half
+    cudaGraphExec_t hx[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    long hx_launches[2][2] = {{0, 0}, {0, 0}};
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_sorted = nullptr, ev_copied = nullptr;
+    long long *d_nout = nullptr;  // per cluster: stars after the step
     // graphs
     // The sort swaps the field pointers every step, so a captured two-step
     // graph is tied to the pointer parity it was captured at: one per parity.
@@ -455,6 +463,14 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
             return rc;
         }
     }
+    if (cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_sorted, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&c->d_nout, (size_t)nclusters * sizeof(long long)) != cudaSuccess) {
+        cudaGetLastError();
+        cmcg_destroy(c);
+        return CMCG_ERR_CUDA;
+    }
     CK(cudaStreamSynchronize(c->stream));
     *out = c;
     return CMCG_OK;
@@ -472,6 +488,13 @@ int cmcg_destroy(cmcg_ctx *c)
     if (c->arena) cudaFree(c->arena);
     if (c->net_mem) cudaFree(c->net_mem);
     if (c->lrn_mem) cudaFree(c->lrn_mem);
+    for (int a = 0; a < 2; ++a)
+        for (int p = 0; p < 2; ++p)
+            if (c->hx[a][p]) cudaGraphExecDestroy(c->hx[a][p]);
+    if (c->copy) cudaStreamDestroy(c->copy);
+    if (c->ev_sorted) cudaEventDestroy(c->ev_sorted);
+    if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+    if (c->d_nout) cudaFree(c->d_nout);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return CMCG_OK;
@@ -777,18 +800,69 @@ static int L_ec3(cmcg_ctx *c)
         if (rc_) return rc_;  \
     } while (0)
 
+// The step in two parts: up to the sort (which swaps the field pointers),
+// and from the new potential on.
+static int issue_part(cmcg_ctx *c, int part)
+{
+    if (part == 0) {
+        RUN(L_begin(c));
+        RUN(L_timestep(c));
+        RUN(L_relax(c, -1.0));
+        RUN(L_orbit(c));
+        RUN(L_tidal(c));
+        RUN(L_sort(c));
+    } else {
+        RUN(L_pot(c));
+        RUN(L_ec3(c));
+        RUN(L_energy(c));
+        RUN(L_end(c));
+    }
+    return CMCG_OK;
+}
+
 static int issue_step(cmcg_ctx *c)
 {
-    RUN(L_begin(c));
-    RUN(L_timestep(c));
-    RUN(L_relax(c, -1.0));
-    RUN(L_orbit(c));
-    RUN(L_tidal(c));
-    RUN(L_sort(c));
-    RUN(L_pot(c));
-    RUN(L_ec3(c));
-    RUN(L_energy(c));
-    RUN(L_end(c));
+    RUN(issue_part(c, 0));
+    RUN(issue_part(c, 1));
+    return CMCG_OK;
+}
+
+__global__ void k_gather_counts(const Cluster *cls, int nclusters, long long *out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nclusters) out[k] = cls[k].sc->N_MAX_NEW;
+}
+
+// Runs part `part` of a step from a graph captured at the current parity
+// (capturing it first).  Part 0 ends with the sort's pointer swap, which the
+// host mirrors after the launch.
+static int run_part_graph(cmcg_ctx *c, int part)
+{
+    const int p = c->parity;
+    if (!c->hx[part][p]) {
+        const bool prof = c->profile;
+        c->profile = false;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const long l0 = c->launches;
+        const int rc = issue_part(c, part);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        c->profile = prof;
+        c->hx_launches[part][p] = c->launches - l0;
+        c->launches = l0;
+        if (part == 0 && c->parity != p) swap_sorted(c);  // the capture ran no kernel: undo the swap
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return CMCG_ERR_CUDA;
+        const cudaError_t ei = cudaGraphInstantiate(&c->hx[part][p], g, 0);
+        cudaGraphDestroy(g);
+        CK(ei);
+    }
+    CK(cudaGraphLaunch(c->hx[part][p], c->stream));
+    c->launches += c->hx_launches[part][p];
+    if (part == 0) swap_sorted(c);
     return CMCG_OK;
 }
 
@@ -1294,6 +1368,10 @@ static void drop_graphs(cmcg_ctx *c)
         c->gexec[p] = nullptr;
         c->graph[p] = nullptr;
         c->graph_ready[p] = false;
+        for (int a = 0; a < 2; ++a) {
+            if (c->hx[a][p]) cudaGraphExecDestroy(c->hx[a][p]);
+            c->hx[a][p] = nullptr;
+        }
     }
 }
 static int net_status(cmcg_ctx *c)
@@ -1570,6 +1648,65 @@ int cmcg_autotune(cmcg_ctx *c, int steps, char *report, long report_len)
     drop_graphs(c);
     RUN(cmcg_kernel_time(c, "reset", nullptr, nullptr));
     if (report && report_len > 0) snprintf(report, (size_t)report_len, "%s", rep.c_str());
+    return CMCG_OK;
+}
+
+// ------------------------------------------------------- host exchange --
+// One step on host star arrays: the fields go in, the step runs, the fields
+// come back.  r, m and id are final once the sort has run, so their
+// read-back runs on the copy stream while the potential, energy conservation
+// and energies of the step's second half run; the rest follow the step.
+// Each part is replayed from its own graph when graphs are enabled.
+int cmcg_step_host(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
+{
+    if (!c || !in || !out) return CMCG_ERR_ARG;
+    for (int k = 0; k < c->ncl; ++k) {
+        const cmcg_stars &a = in[k], &b = out[k];
+        if (!a.r || !a.m || !a.vr || !a.vt || !a.E || !a.J || !a.id) return CMCG_ERR_ARG;
+        if (!b.r || !b.m || !b.vr || !b.vt || !b.E || !b.J || !b.id || b.cap < a.N) return CMCG_ERR_ARG;
+    }
+    for (int k = 0; k < c->ncl; ++k)
+        RUN(cmcg_put_stars(c, k, in[k].N, in[k].r, in[k].m, in[k].vr, in[k].vt, in[k].E, in[k].J, in[k].id));
+    const bool graphs = c->use_graph && !c->profile;
+    const long l0 = c->launches;
+    if (graphs)
+        RUN(run_part_graph(c, 0));
+    else
+        RUN(issue_part(c, 0));
+    CK(cudaEventRecord(c->ev_sorted, c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->ev_sorted, 0));
+    // a cluster never grows in a step: N given in bounds the stars after it
+    for (int k = 0; k < c->ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        const size_t nb = (size_t)in[k].N * sizeof(double);
+        CK(cudaMemcpyAsync(out[k].r, c->f.r + o, nb, cudaMemcpyDeviceToHost, c->copy));
+        CK(cudaMemcpyAsync(out[k].m, c->f.m + o, nb, cudaMemcpyDeviceToHost, c->copy));
+        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)in[k].N * sizeof(long long), cudaMemcpyDeviceToHost,
+                           c->copy));
+    }
+    CK(cudaEventRecord(c->ev_copied, c->copy));
+    if (graphs)
+        RUN(run_part_graph(c, 1));
+    else
+        RUN(issue_part(c, 1));
+    k_gather_counts<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl, c->d_nout);
+    c->launches += 1;
+    CK(cudaGetLastError());
+    for (int k = 0; k < c->ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        const size_t nb = (size_t)in[k].N * sizeof(double);
+        CK(cudaMemcpyAsync(out[k].vr, c->f.vr + o, nb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(out[k].vt, c->f.vt + o, nb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(out[k].E, c->f.E + o, nb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(out[k].J, c->f.J + o, nb, cudaMemcpyDeviceToHost, c->stream));
+    }
+    std::vector<long long> n(c->ncl);
+    CK(cudaMemcpyAsync(n.data(), c->d_nout, (size_t)c->ncl * sizeof(long long), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_copied, 0));  // the next call's uploads follow the read-back
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < c->ncl; ++k) out[k].N = (long)n[k];
+    c->launches_last = c->launches - l0;
     return CMCG_OK;
 }
 

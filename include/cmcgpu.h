@@ -250,6 +250,22 @@ int cmcg_mlp_train(cmcg_ctx *ctx, const float *feat, const int *bin, const int *
 long cmcg_learned_samples(cmcg_ctx *ctx, int k, float *feat, double *X, int *ntrial, long cap);
 int cmcg_learned_stats(cmcg_ctx *ctx, uint64_t *out /* CMCG_LSTAT_N */);
 
+/* --------------------------------------------------- host exchange -----
+ * One step on host star arrays, one cmcg_stars per cluster: in[k] (N stars,
+ * 1-based order as cmcg_put_stars takes them) is uploaded, the step runs, and
+ * out[k] receives the stars after it (out[k].N set; out[k].cap >= in[k].N).
+ * r, m and id are read back while the second half of the step (potential,
+ * energy conservation, energies) still runs; graphs are used when enabled.
+ * in and out may be the same arrays.  Pinned host memory gives full copy
+ * speed.  Equivalent to cmcg_put_stars + cmcg_step + cmcg_get_stars. */
+typedef struct {
+    long N;                    /* stars (in), stars after the step (out)          */
+    long cap;                  /* capacity of the out arrays                       */
+    double *r, *m, *vr, *vt, *E, *J;
+    int64_t *id;
+} cmcg_stars;
+int cmcg_step_host(cmcg_ctx *ctx, const cmcg_stars *in, cmcg_stars *out);
+
 /* ------------------------------------------------------- autotuner -----
  * Launch variants with bit-identical results, chosen by measurement on the
  * context's own clusters: "orbit" and "relax" (5 or 4 blocks per SM, i.e.

@@ -42,12 +42,19 @@ ALG_BYTES = {"sort": 116, "potential": 24, "relax": 72, "orbit": 80, "ec3": 72, 
 MLP_FLOPS_PER_STAR = 2 * (8 * 64 + 64 * 64 + 64 * 33)
 # DRAM bytes per star of one launch, dram__bytes_read.sum + dram__bytes_write.sum
 # from one ncu capture (summaries under profiles/), scaled by stars: k_orbit
-# 956.0 MB over 1,913,988 stars (King W0=6 + Kroupa, N=2e6), k_relax64 56.9 MB
+# 961.2 MB over 1,912,424 stars (King W0=6 + Kroupa, N=2e6), k_relax64 57.5 MB
 # over 962,913 stars (the same model at N=1e6)
-NCU_TRAFFIC_PER_STAR = {"orbit": 956.0e6 / 1913988, "relax": 56.9e6 / 962913}
+NCU_TRAFFIC_PER_STAR = {"orbit": 961.2e6 / 1912424, "relax": 57.5e6 / 962913}
 # share of cycles the FP64 pipe was busy in the same captures: the kernels'
 # real bound on GB300 (1/64-rate FP64), reported beside the HBM roofline
 NCU_FP64_PIPE_ACTIVE = {"orbit": 0.706, "relax": 0.713}
+# FP64 thread-operations per star of each kernel family (ncu
+# smsp__sass_thread_inst_executed_op_fp64_pred_on.sum over the stars of one
+# step, King W0=6 + Kroupa, N = 1e6), and the measured FP64 FMA rate of this
+# GPU (bench.py --probe-rates: 1.01 TFLOP/s = 5.05e11 DFMA/s)
+NCU_FP64_OPS_PER_STAR = {"orbit": 343.2, "relax": 181.1, "potential": 53.3, "ec3": 45.0, "energy": 11.8,
+                         "timestep": 12.1, "tidal": 7.8}
+FP64_PEAK_OPS = 5.05e11
 
 
 def measured_peak(key="hbm_gbs", fallback=6800.0):
@@ -492,6 +499,15 @@ def run_ours(a, rank, ws, dist):
                      "fp64_pipe_active": NCU_FP64_PIPE_ACTIVE.get(top),
                      "alg_bytes_per_star": ALG_BYTES[top], "ms_per_launch": ms_top / n_top,
                      "timed_in": "the profiled direct-launch pass"},
+        "roofline_fp64": {"bound": "fp64 pipe", "kernel": top,
+                          "achieved": NCU_FP64_OPS_PER_STAR.get(top, 0.0) * n_prof / (ms_top / n_top * 1e-3),
+                          "peak": FP64_PEAK_OPS, "unit": "FP64 ops/s",
+                          "frac": NCU_FP64_OPS_PER_STAR.get(top, 0.0) * n_prof / (ms_top / n_top * 1e-3)
+                          / FP64_PEAK_OPS,
+                          "ops_per_star": NCU_FP64_OPS_PER_STAR.get(top),
+                          "peak_source": "measured DFMA rate (profiles/fp64_rates.md)",
+                          "step_frac": sum(NCU_FP64_OPS_PER_STAR.values()) * n_prof / (step_ms * 1e-3)
+                          / FP64_PEAK_OPS},
         "energy": {"rel_drift_per_step": drift[0] if ncl == 1 else None,
                    "max_abs_rel_drift_per_step": max(abs(d) for d in drift),
                    "what": "(Etot after - Etot before) / |Etot before| / steps over the timed steps"},

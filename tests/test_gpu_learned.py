@@ -222,3 +222,38 @@ def test_learned_filter_decisions_match_exact(trained, model, N, imf):
         st = g.learned_stats()
         assert st["accepted"] > 0.5 * st["stars"], st  # tight envelopes send more stars back
     g.close()
+
+
+def test_ensemble_collect_and_tiny_envelope_are_the_plain_sampler(gpulib):
+    """Three clusters of uneven N in one context: the learned launch sequence
+    with plain trials, and the proposal with an envelope that never holds,
+    both reproduce the plain step bit for bit in every cluster."""
+    sizes = [7000, 16001, 11000]
+    ics = [cmcgpu.generate(cmcgpu.KING if i % 2 else cmcgpu.PLUMMER, n, seed=100 + i, imf=1)
+           for i, n in enumerate(sizes)]
+
+    def make():
+        ps = [cmcgpu.default_params(orbit_r=ic["rtid"], seed=200 + i) for i, ic in enumerate(ics)]
+        g = cmcgpu.Context(sizes, ps)
+        for c, ic in enumerate(ics):
+            g.load(c, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+        g.initialize()
+        return g
+
+    plain, collect, tiny = make(), make(), make()
+    collect.set_learned(cmcgpu.LEARN_COLLECT)
+    tiny.mlp_init(9)
+    tiny.set_learned(cmcgpu.LEARN_ON, kappa=1e-30)
+    for g in (plain, collect, tiny):
+        g.step(2)
+        g.check_device("ensemble steps")
+    for g in (collect, tiny):
+        for c in range(len(sizes)):
+            for name in ("r", "vr", "vt", "E", "J", "X"):
+                assert np.array_equal(g.get(name, c), plain.get(name, c)), (c, name)
+            assert np.array_equal(g.ids(c), plain.ids(c))
+    for c in range(len(sizes)):
+        _, X, nt = collect.learned_samples(c)
+        assert len(X) > 0.9 * collect.nstars(c) and np.all(nt > 0)
+    for g in (plain, collect, tiny):
+        g.close()

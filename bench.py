@@ -442,12 +442,15 @@ def run_ours(a, rank, ws, dist):
 
     # ---- end to end through the public API: host star arrays in pinned memory,
     # copied in before and out after every step
-    cap = max(n for n, _, _ in clusters) + 16
-    bufs = {k: torch.empty(cap, dtype=torch.float64, pin_memory=True).numpy() for k in ("r", "m", "vr", "vt", "E", "J")}
-    bufs["id"] = torch.empty(cap, dtype=torch.int64, pin_memory=True).numpy()
+    # pinned host arrays, one set per cluster: the host owns the star state
+    def pinned(n):
+        b = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in ("r", "m", "vr", "vt", "E", "J")}
+        b["id"] = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy()
+        return b
+
     host = []
-    for c in range(ncl):
-        b = {k: v.copy() if ncl > 1 else v for k, v in bufs.items()}
+    for c, (n, _, _) in enumerate(clusters):
+        b = pinned(n + 16)
         host.append((b, ctx.get_stars(c, b)))
     # cmcg_step_host: the step's two halves replayed from graphs, the read-back of
     # the sorted r, m, id overlapping the second half; one warm-up call captures them

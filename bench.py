@@ -47,7 +47,7 @@ MLP_FLOPS_PER_STAR = 2 * (8 * 64 + 64 * 64 + 64 * 33)
 NCU_TRAFFIC_PER_STAR = {"orbit": 961.2e6 / 1912424, "relax": 57.5e6 / 962913}
 # share of cycles the FP64 pipe was busy in the same captures: the kernels'
 # real bound on GB300 (1/64-rate FP64), reported beside the HBM roofline
-NCU_FP64_PIPE_ACTIVE = {"orbit": 0.706, "relax": 0.713}
+NCU_FP64_PIPE_ACTIVE = {"orbit": 0.685, "relax": 0.703}
 # FP64 thread-operations per star of each kernel family (ncu
 # smsp__sass_thread_inst_executed_op_fp64_pred_on.sum over the stars of one
 # step, King W0=6 + Kroupa, N = 1e6), and the measured FP64 FMA rate of this

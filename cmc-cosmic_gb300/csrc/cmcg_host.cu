@@ -96,10 +96,10 @@ struct cmcg_ctx {
     // host exchange (cmcg_step_host): the step as two graphs, before and after
     // the sort, per pointer parity at their start; a copy stream for the
     // read-back that overlaps the second half
-    cudaGraphExec_t hx[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    long hx_launches[2][2] = {{0, 0}, {0, 0}};
+    cudaGraphExec_t hx[4][2] = {};
+    long hx_launches[4][2] = {};
     cudaStream_t copy = nullptr;
-    cudaEvent_t ev_sorted = nullptr, ev_copied = nullptr;
+    cudaEvent_t ev_sorted = nullptr, ev_copied = nullptr, ev_in = nullptr, ev_ec3 = nullptr;
     long long *d_nout = nullptr;  // per cluster: stars after the step
     // graphs
     // The sort swaps the field pointers every step, so a captured two-step
@@ -466,6 +466,8 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
     if (cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_sorted, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_ec3, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&c->d_nout, (size_t)nclusters * sizeof(long long)) != cudaSuccess) {
         cudaGetLastError();
         cmcg_destroy(c);
@@ -488,12 +490,12 @@ int cmcg_destroy(cmcg_ctx *c)
     if (c->arena) cudaFree(c->arena);
     if (c->net_mem) cudaFree(c->net_mem);
     if (c->lrn_mem) cudaFree(c->lrn_mem);
-    for (int a = 0; a < 2; ++a)
+    for (int a = 0; a < 4; ++a)
         for (int p = 0; p < 2; ++p)
             if (c->hx[a][p]) cudaGraphExecDestroy(c->hx[a][p]);
     if (c->copy) cudaStreamDestroy(c->copy);
-    if (c->ev_sorted) cudaEventDestroy(c->ev_sorted);
-    if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+    for (cudaEvent_t e : {c->ev_sorted, c->ev_copied, c->ev_in, c->ev_ec3})
+        if (e) cudaEventDestroy(e);
     if (c->d_nout) cudaFree(c->d_nout);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -800,20 +802,29 @@ static int L_ec3(cmcg_ctx *c)
         if (rc_) return rc_;  \
     } while (0)
 
-// The step in two parts: up to the sort (which swaps the field pointers),
-// and from the new potential on.
+// The step in four parts, cut where the host exchange overlaps copies with
+// kernels: the time step (which reads r, m, vr, vt only); relaxation to the
+// sort (which swaps the field pointers); potential and energy conservation
+// (r, m, id are final); energies (vr, vt are final).
+constexpr int HX_PARTS = 4, HX_SORT = 1;
 static int issue_part(cmcg_ctx *c, int part)
 {
-    if (part == 0) {
+    switch (part) {
+    case 0:
         RUN(L_begin(c));
         RUN(L_timestep(c));
+        break;
+    case 1:
         RUN(L_relax(c, -1.0));
         RUN(L_orbit(c));
         RUN(L_tidal(c));
         RUN(L_sort(c));
-    } else {
+        break;
+    case 2:
         RUN(L_pot(c));
         RUN(L_ec3(c));
+        break;
+    default:
         RUN(L_energy(c));
         RUN(L_end(c));
     }
@@ -822,8 +833,7 @@ static int issue_part(cmcg_ctx *c, int part)
 
 static int issue_step(cmcg_ctx *c)
 {
-    RUN(issue_part(c, 0));
-    RUN(issue_part(c, 1));
+    for (int part = 0; part < HX_PARTS; ++part) RUN(issue_part(c, part));
     return CMCG_OK;
 }
 
@@ -834,8 +844,8 @@ __global__ void k_gather_counts(const Cluster *cls, int nclusters, long long *ou
 }
 
 // Runs part `part` of a step from a graph captured at the current parity
-// (capturing it first).  Part 0 ends with the sort's pointer swap, which the
-// host mirrors after the launch.
+// (capturing it first).  Part HX_SORT ends with the sort's pointer swap,
+// which the host mirrors after the launch.
 static int run_part_graph(cmcg_ctx *c, int part)
 {
     const int p = c->parity;
@@ -850,7 +860,7 @@ static int run_part_graph(cmcg_ctx *c, int part)
         c->profile = prof;
         c->hx_launches[part][p] = c->launches - l0;
         c->launches = l0;
-        if (part == 0 && c->parity != p) swap_sorted(c);  // the capture ran no kernel: undo the swap
+        if (part == HX_SORT && c->parity != p) swap_sorted(c);  // the capture ran no kernel: undo the swap
         if (rc) {
             if (g) cudaGraphDestroy(g);
             return rc;
@@ -862,7 +872,7 @@ static int run_part_graph(cmcg_ctx *c, int part)
     }
     CK(cudaGraphLaunch(c->hx[part][p], c->stream));
     c->launches += c->hx_launches[part][p];
-    if (part == 0) swap_sorted(c);
+    if (part == HX_SORT) swap_sorted(c);
     return CMCG_OK;
 }
 
@@ -1368,7 +1378,7 @@ static void drop_graphs(cmcg_ctx *c)
         c->gexec[p] = nullptr;
         c->graph[p] = nullptr;
         c->graph_ready[p] = false;
-        for (int a = 0; a < 2; ++a) {
+        for (int a = 0; a < HX_PARTS; ++a) {
             if (c->hx[a][p]) cudaGraphExecDestroy(c->hx[a][p]);
             c->hx[a][p] = nullptr;
         }
@@ -1653,9 +1663,12 @@ int cmcg_autotune(cmcg_ctx *c, int steps, char *report, long report_len)
 
 // ------------------------------------------------------- host exchange --
 // One step on host star arrays: the fields go in, the step runs, the fields
-// come back.  r, m and id are final once the sort has run, so their
-// read-back runs on the copy stream while the potential, energy conservation
-// and energies of the step's second half run; the rest follow the step.
+// come back, with copies overlapping kernels where the data allow:
+//   r, m, vr, vt go up first; the time step runs while id, E, J follow on the
+//   copy stream (relaxation, which writes E and J, waits for them);
+//   r, m, id are final after the sort and come back during the potential
+//   and energy conservation; vr, vt after energy conservation, during the
+//   energies; E, J last.
 // Each part is replayed from its own graph when graphs are enabled.
 int cmcg_step_host(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
 {
@@ -1664,41 +1677,71 @@ int cmcg_step_host(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
         const cmcg_stars &a = in[k], &b = out[k];
         if (!a.r || !a.m || !a.vr || !a.vt || !a.E || !a.J || !a.id) return CMCG_ERR_ARG;
         if (!b.r || !b.m || !b.vr || !b.vt || !b.E || !b.J || !b.id || b.cap < a.N) return CMCG_ERR_ARG;
+        if (a.N > c->cap[k]) return CMCG_ERR_CAPACITY;
+        if (a.N < 2 * c->params[k].AVEKERNEL + 2) return CMCG_ERR_ARG;
     }
-    for (int k = 0; k < c->ncl; ++k)
-        RUN(cmcg_put_stars(c, k, in[k].N, in[k].r, in[k].m, in[k].vr, in[k].vt, in[k].E, in[k].J, in[k].id));
     const bool graphs = c->use_graph && !c->profile;
     const long l0 = c->launches;
-    if (graphs)
-        RUN(run_part_graph(c, 0));
-    else
-        RUN(issue_part(c, 0));
+    auto part = [&](int p) { return graphs ? run_part_graph(c, p) : issue_part(c, p); };
+    auto up = [&](double *dst, const double *src, long n, cudaStream_t s) {
+        return cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s);
+    };
+    auto down = [&](double *dst, const double *src, long n, cudaStream_t s) {
+        return cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s);
+    };
+    static const double sentinel = CMCG_SF_INFINITY;
+    for (int k = 0; k < c->ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        const long N = in[k].N;
+        CK(up(c->f.r + o, in[k].r, N, c->stream));
+        CK(up(c->f.m + o, in[k].m, N, c->stream));
+        CK(up(c->f.vr + o, in[k].vr, N, c->stream));
+        CK(up(c->f.vt + o, in[k].vt, N, c->stream));
+        CK(cudaMemcpyAsync(c->f.r + o + N, &sentinel, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        k_set_count<<<1, 1, 0, c->stream>>>(c->d_cls, k, (long long)N);
+        c->launches += 1;
+    }
+    CK(cudaEventRecord(c->ev_in, c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->ev_in, 0));  // the copy stream's uploads follow the counts
+    for (int k = 0; k < c->ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        const long N = in[k].N;
+        CK(cudaMemcpyAsync(c->f.id + o, in[k].id, (size_t)N * sizeof(long long), cudaMemcpyHostToDevice, c->copy));
+        CK(up(c->f.E + o, in[k].E, N, c->copy));
+        CK(up(c->f.J + o, in[k].J, N, c->copy));
+    }
+    CK(cudaEventRecord(c->ev_in, c->copy));
+    RUN(part(0));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_in, 0));
+    RUN(part(1));
     CK(cudaEventRecord(c->ev_sorted, c->stream));
     CK(cudaStreamWaitEvent(c->copy, c->ev_sorted, 0));
     // a cluster never grows in a step: N given in bounds the stars after it
     for (int k = 0; k < c->ncl; ++k) {
         const long long o = c->off[k] + 1;
-        const size_t nb = (size_t)in[k].N * sizeof(double);
-        CK(cudaMemcpyAsync(out[k].r, c->f.r + o, nb, cudaMemcpyDeviceToHost, c->copy));
-        CK(cudaMemcpyAsync(out[k].m, c->f.m + o, nb, cudaMemcpyDeviceToHost, c->copy));
-        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)in[k].N * sizeof(long long), cudaMemcpyDeviceToHost,
+        const long N = in[k].N;
+        CK(down(out[k].r, c->f.r + o, N, c->copy));
+        CK(down(out[k].m, c->f.m + o, N, c->copy));
+        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)N * sizeof(long long), cudaMemcpyDeviceToHost,
                            c->copy));
     }
+    RUN(part(2));
+    CK(cudaEventRecord(c->ev_ec3, c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->ev_ec3, 0));
+    for (int k = 0; k < c->ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        CK(down(out[k].vr, c->f.vr + o, in[k].N, c->copy));
+        CK(down(out[k].vt, c->f.vt + o, in[k].N, c->copy));
+    }
     CK(cudaEventRecord(c->ev_copied, c->copy));
-    if (graphs)
-        RUN(run_part_graph(c, 1));
-    else
-        RUN(issue_part(c, 1));
+    RUN(part(3));
     k_gather_counts<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl, c->d_nout);
     c->launches += 1;
     CK(cudaGetLastError());
     for (int k = 0; k < c->ncl; ++k) {
         const long long o = c->off[k] + 1;
-        const size_t nb = (size_t)in[k].N * sizeof(double);
-        CK(cudaMemcpyAsync(out[k].vr, c->f.vr + o, nb, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaMemcpyAsync(out[k].vt, c->f.vt + o, nb, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaMemcpyAsync(out[k].E, c->f.E + o, nb, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaMemcpyAsync(out[k].J, c->f.J + o, nb, cudaMemcpyDeviceToHost, c->stream));
+        CK(down(out[k].E, c->f.E + o, in[k].N, c->stream));
+        CK(down(out[k].J, c->f.J + o, in[k].N, c->stream));
     }
     std::vector<long long> n(c->ncl);
     CK(cudaMemcpyAsync(n.data(), c->d_nout, (size_t)c->ncl * sizeof(long long), cudaMemcpyDeviceToHost,

@@ -948,7 +948,15 @@ int cmcg_run(cmcg_ctx *c, int nsteps)
             done += 2;
         }
     }
-    for (; done < nsteps; ++done) RUN(issue_step(c));
+    // single steps (and an odd last step) from the four part graphs
+    const bool parts = c->use_graph && !c->profile;
+    for (; done < nsteps; ++done) {
+        if (parts) {
+            for (int part = 0; part < HX_PARTS; ++part) RUN(run_part_graph(c, part));
+        } else {
+            RUN(issue_step(c));
+        }
+    }
     c->launches_last = c->launches - l0;
     return CMCG_OK;
 }

@@ -55,3 +55,29 @@ def test_step_host_equals_put_step_get(gpulib, sizes):
                 assert np.array_equal(bufs[c][k][:n], state["ref"][1][c][k][:n]), (name, c, k)
     for g in (ref, hx_graph, hx_direct):
         g.close()
+
+
+def test_single_steps_from_part_graphs_equal_direct_steps(gpulib):
+    ic = cmcgpu.generate(cmcgpu.KING, 20000, seed=95, imf=1)
+    a, b = _ctx([ic], 9), _ctx([ic], 9)
+    a.use_graph(True)
+    b.use_graph(False)
+    for _ in range(3):
+        a.step(1)  # four graph launches a step
+    a.step(2)      # the two-step graph
+    b.step(5)
+    for g in (a, b):
+        g.check_device("steps")
+    for name in ("r", "vr", "vt", "m", "E", "J", "star_phi"):
+        assert np.array_equal(a.get(name), b.get(name)), name
+    assert np.array_equal(a.ids(), b.ids())
+
+
+def test_step_host_rejects_short_output(gpulib):
+    ic = cmcgpu.generate(cmcgpu.PLUMMER, 5000, seed=97)
+    g = _ctx([ic], 11)
+    big, small = _bufs(5000), _bufs(100)
+    n = g.get_stars(0, big)
+    with pytest.raises(cmcgpu.CmcError):
+        g.step_host([(n, big)], [small])
+    g.close()

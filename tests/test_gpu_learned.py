@@ -257,3 +257,32 @@ def test_ensemble_collect_and_tiny_envelope_are_the_plain_sampler(gpulib):
         assert len(X) > 0.9 * collect.nstars(c) and np.all(nt > 0)
     for g in (plain, collect, tiny):
         g.close()
+
+
+def test_fifty_steps_with_the_proposal_follow_the_plain_run(trained):
+    """Config 4's comparison: 50 steps with the proposal and 50 with the plain
+    sampler from the same model.  The runs draw differently, so they are two
+    realisations: their energy errors stay at the plain run's level and their
+    Lagrange radii agree to the noise of 1e5 stars."""
+    N = 100000
+    ic = cmcgpu.generate(cmcgpu.PLUMMER, N, seed=111)
+    runs = {}
+    for mode in (cmcgpu.LEARN_OFF, cmcgpu.LEARN_ON):
+        g = cmcgpu.Context([N], cmcgpu.default_params(orbit_r=ic["rtid"], seed=112))
+        g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+        g.initialize()
+        g.mlp_set_params(trained["w"])
+        g.set_learned(mode, kappa=1.2)
+        e0 = g.scalar("Etot")
+        g.use_graph(True)
+        g.step(50)
+        g.check_device(f"50 steps, mode {mode}")
+        d = g.diagnostics(mass_pc=[0.1, 0.5, 0.9])
+        runs[mode] = (abs(g.scalar("Etot") - e0) / abs(e0) / 50, d.arr("mass_r"), g.nstars(), d.rh)
+        g.close()
+    (ep, lp, np_, rhp), (el, ll, nl, rhl) = runs[cmcgpu.LEARN_OFF], runs[cmcgpu.LEARN_ON]
+    print(f"plain: dE/E/step {ep:.2e}, Lagrange radii {lp}, rh {rhp:.5f}, N {np_}; "
+          f"learned: {el:.2e}, {ll}, {rhl:.5f}, {nl}")
+    assert ep < 1e-6 and el < 1e-6, (ep, el)
+    assert np.all(np.abs(ll / lp - 1) < 0.02), (lp, ll)
+    assert abs(rhl / rhp - 1) < 0.02 and abs(nl - np_) <= 0.001 * N, (rhp, rhl, np_, nl)

@@ -476,3 +476,39 @@ def test_trial_filter_decisions_match_exact(gpulib, model, N):
         g.close()
     for a, b in zip(*states):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("model,N,imf", [(cmcgpu.PLUMMER, 6000, 0), (cmcgpu.KING, 6000, 1)])
+def test_phases_with_a_central_mass(gpulib, orc, model, N, imf):
+    """A central mass (cenma.m, 5% of the cluster's) enters Mtotal, Phi_0,
+    set_a_b's innermost interval, potential(r < r_1) and the energies; each
+    phase still matches the oracle."""
+    ic, o, g = make_pair(model, N, seed=N + 7, imf=imf, cenma_m=0.05 * N)
+    o.initialize()
+    g.initialize()
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
+    assert g.scalar("Mtotal") == o.scalar("Mtotal")
+    for s in ("KE", "PE", "Etot"):
+        assert max_rel(g.scalar(s), o.scalar(s)) <= TOL_SUM
+    for r in (1e-4, 1e-3, 0.5, 3.0):
+        assert max_rel(g.potential(r), o.potential(r)) <= TOL_PHI
+    # the orbit phase from the oracle's post-relaxation state
+    sync_state(o, g, star=[("E", "E"), ("J", "J")])
+    o.begin_step()
+    g.begin_step()
+    o.calc_timestep()
+    o.dynamics_apply(o.scalar("Dt"))
+    o.energy_conservation1()
+    sync_state(o, g, star=[("vr", "vr_rel"), ("vt", "vt_rel"), ("E", "E"), ("J", "J")],
+               scalars=("Rtidal", "Mtotal"))
+    o.new_orbits_calculate()
+    o.energy_conservation2()
+    g.new_orbits_calculate()
+    g.check_device("new_orbits_calculate")
+    rn_o, rn_g = o.get("rnew"), g.get("rnew")
+    keep = rn_o != 1e10
+    assert np.array_equal(rn_g == 1e10, ~keep)
+    assert max_rel(rn_g[keep], rn_o[keep]) <= TOL_ORBIT
+    assert max_rel(g.get("vrnew")[keep], o.get("vrnew")[keep]) <= TOL_ORBIT
+    assert max_rel(g.get("vtnew")[keep], o.get("vtnew")[keep]) <= TOL_ORBIT
+    g.close()

@@ -512,3 +512,45 @@ def test_phases_with_a_central_mass(gpulib, orc, model, N, imf):
     assert max_rel(g.get("vrnew")[keep], o.get("vrnew")[keep]) <= TOL_ORBIT
     assert max_rel(g.get("vtnew")[keep], o.get("vtnew")[keep]) <= TOL_ORBIT
     g.close()
+
+
+@pytest.mark.parametrize("label,N,pkw", [
+    ("apocentre-cut", 5000, dict(TIDAL_TREATMENT=0)),
+    ("no-relaxation", 5000, dict(RELAXATION=0)),
+    ("no-perturbation", 5000, dict(PERTURB=0)),
+    ("kernel-10", 5000, dict(AVEKERNEL=10)),
+    ("small-N", 48, {}),
+    ("small-odd-N", 101, {}),
+])
+def test_free_running_steps_with_other_parameters(gpulib, orc, label, N, pkw):
+    """Whole steps under the .ini switches the benchmark leaves at their
+    defaults, and at small clusters (the windows need N >= 2p + 2; below it
+    the reference indexes outside the star array).  Without relaxation the
+    first step's positions and potential are bit-identical (no sin/cos), and
+    its velocities within an ulp (set_velocities3's scale factor is formed as
+    vnew2 rsqrt(vnew2 v2)); later steps, and the runs with relaxation, stay
+    within the free-running bounds of test_free_running_steps."""
+    model = cmcgpu.PLUMMER if N < 1000 else cmcgpu.KING
+    ic, o, g = make_pair(model, N, seed=N + 13, imf=1, **pkw)
+    o.initialize()
+    g.initialize()
+    exact = pkw.get("RELAXATION", 1) == 0 or pkw.get("PERTURB", 1) == 0
+    e0o, e0g = o.scalar("Etot"), g.scalar("Etot")
+    for step in range(3):
+        o.step()
+        g.step()
+        g.check_device(f"{label} step {step}")
+        assert g.nstars() == o.nstars(), (label, step)
+        assert np.array_equal(g.ids(), o.ids()), (label, step)
+        if exact and step == 0:
+            for name in ("r", "star_phi"):
+                assert np.array_equal(g.get(name), o.get(name)), (label, step, name)
+            for name in ("vr", "vt", "E", "J"):
+                assert max_rel(g.get(name), o.get(name)) <= TOL_PHI, (label, step, name)
+        else:
+            err = rel_err(g.get("r"), o.get("r"))
+            assert np.quantile(err, 0.99) <= 1e-9 and err.max() <= 1e-7, (label, step, err.max())
+        de_o = o.scalar("Etot") - e0o
+        de_g = g.scalar("Etot") - e0g
+        assert abs(de_g - de_o) <= 1e-9 * abs(e0o) + 1e-3 * abs(de_o), (label, step)
+    g.close()

@@ -554,3 +554,23 @@ def test_free_running_steps_with_other_parameters(gpulib, orc, label, N, pkw):
         de_g = g.scalar("Etot") - e0g
         assert abs(de_g - de_o) <= 1e-9 * abs(e0o) + 1e-3 * abs(de_o), (label, step)
     g.close()
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_n_try_exceeded_is_reported(gpulib, learned):
+    """N_TRY = 1: stars whose first trial is rejected stop the step as the
+    reference's exit_cleanly does (cmc_evolution_thr.c:888-891), reported as
+    CMCG_ERR_NTRY with a star index, not a hang; with the learned proposal
+    such a star first goes back to the plain sampler, which then runs out."""
+    N = 5000
+    ic = cmcgpu.generate(cmcgpu.PLUMMER, N, seed=131)
+    g = cmcgpu.Context([N], cmcgpu.default_params(orbit_r=ic["rtid"], seed=132, n_try=1))
+    g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    g.initialize()
+    if learned:
+        g.mlp_init(3)
+        g.set_learned(cmcgpu.LEARN_ON, 1.2)
+    g.step(1)
+    code, idx = g.last_error()
+    assert code == 5 and 1 <= idx <= N, (code, idx)  # CMCG_ERR_NTRY
+    g.close()

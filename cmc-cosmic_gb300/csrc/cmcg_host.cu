@@ -1678,16 +1678,8 @@ int cmcg_autotune(cmcg_ctx *c, int steps, char *report, long report_len)
 //   and energy conservation; vr, vt after energy conservation, during the
 //   energies; E, J last.
 // Each part is replayed from its own graph when graphs are enabled.
-int cmcg_step_host(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
+static int step_host_run(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
 {
-    if (!c || !in || !out) return CMCG_ERR_ARG;
-    for (int k = 0; k < c->ncl; ++k) {
-        const cmcg_stars &a = in[k], &b = out[k];
-        if (!a.r || !a.m || !a.vr || !a.vt || !a.E || !a.J || !a.id) return CMCG_ERR_ARG;
-        if (!b.r || !b.m || !b.vr || !b.vt || !b.E || !b.J || !b.id || b.cap < a.N) return CMCG_ERR_ARG;
-        if (a.N > c->cap[k]) return CMCG_ERR_CAPACITY;
-        if (a.N < 2 * c->params[k].AVEKERNEL + 2) return CMCG_ERR_ARG;
-    }
     const bool graphs = c->use_graph && !c->profile;
     const long l0 = c->launches;
     auto part = [&](int p) { return graphs ? run_part_graph(c, p) : issue_part(c, p); };
@@ -1759,6 +1751,24 @@ int cmcg_step_host(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
     for (int k = 0; k < c->ncl; ++k) out[k].N = (long)n[k];
     c->launches_last = c->launches - l0;
     return CMCG_OK;
+}
+
+int cmcg_step_host(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
+{
+    if (!c || !in || !out) return CMCG_ERR_ARG;
+    for (int k = 0; k < c->ncl; ++k) {
+        const cmcg_stars &a = in[k], &b = out[k];
+        if (!a.r || !a.m || !a.vr || !a.vt || !a.E || !a.J || !a.id) return CMCG_ERR_ARG;
+        if (!b.r || !b.m || !b.vr || !b.vt || !b.E || !b.J || !b.id || b.cap < a.N) return CMCG_ERR_ARG;
+        if (a.N > c->cap[k]) return CMCG_ERR_CAPACITY;
+        if (a.N < 2 * c->params[k].AVEKERNEL + 2) return CMCG_ERR_ARG;
+    }
+    const int rc = step_host_run(c, in, out);
+    if (rc) {  // copies from or to the caller's arrays may still be in flight: they end before the return
+        cudaStreamSynchronize(c->copy);
+        cudaStreamSynchronize(c->stream);
+    }
+    return rc;
 }
 
 }  // extern "C"

@@ -129,8 +129,10 @@ int cmcg_initialize(cmcg_ctx *ctx);
 /* Host-owned star state for cluster c, as the reference's host loop keeps it:
  * per star r (star_r), m (star_m, i.e. x N_STAR), vr, vt, E, J, id; 0-based, N
  * stars.  put replaces the device copy (scalars are kept), get reads it back
- * and returns N.  Both are asynchronous when the buffers are pinned; get
- * synchronises before returning. */
+ * and returns N.  Both are asynchronous when the buffers are pinned: put's
+ * arrays must stay unchanged until the context's stream has read them
+ * (cmcg_synchronize, or any call that synchronises); get synchronises before
+ * returning. */
 int cmcg_put_stars(cmcg_ctx *ctx, int cluster, long N, const double *r, const double *m, const double *vr,
                    const double *vt, const double *E, const double *J, const int64_t *id);
 long cmcg_get_stars(cmcg_ctx *ctx, int cluster, long cap, double *r, double *m, double *vr, double *vt, double *E,
@@ -252,12 +254,13 @@ int cmcg_learned_stats(cmcg_ctx *ctx, uint64_t *out /* CMCG_LSTAT_N */);
 
 /* --------------------------------------------------- host exchange -----
  * One step on host star arrays, one cmcg_stars per cluster: in[k] (N stars,
- * 1-based order as cmcg_put_stars takes them) is uploaded, the step runs, and
+ * 0-based, as cmcg_put_stars takes them) is uploaded, the step runs, and
  * out[k] receives the stars after it (out[k].N set; out[k].cap >= in[k].N).
  * r, m and id are read back while the second half of the step (potential,
  * energy conservation, energies) still runs; graphs are used when enabled.
  * in and out may be the same arrays.  Pinned host memory gives full copy
- * speed.  Equivalent to cmcg_put_stars + cmcg_step + cmcg_get_stars. */
+ * speed.  The call returns once every copy has finished, on errors too.
+ * Equivalent to cmcg_put_stars + cmcg_step + cmcg_get_stars. */
 typedef struct {
     long N;                    /* stars (in), stars after the step (out)          */
     long cap;                  /* capacity of the out arrays                       */

@@ -574,3 +574,36 @@ def test_n_try_exceeded_is_reported(gpulib, learned):
     code, idx = g.last_error()
     assert code == 5 and 1 <= idx <= N, (code, idx)  # CMCG_ERR_NTRY
     g.close()
+
+
+@pytest.mark.parametrize("seed", range(1, 9))
+@pytest.mark.parametrize("model,imf", [(cmcgpu.PLUMMER, 0), (cmcgpu.KING, 1), (cmcgpu.PLUMMER, 1)])
+def test_potential_and_new_orbits_bit_exact_over_seeds(gpulib, orc, seed, model, imf):
+    """The potential and the whole orbit phase (escapers, new r, vr, the
+    accepted X) are bit-identical to the oracle on many seeded models (the
+    same inputs: the oracle's post-relaxation state)."""
+    N = 3000 + 37 * seed
+    ic, o, g = make_pair(model, N, seed=seed * 7 + imf, imf=imf, rng_seed=seed * 13)
+    o.initialize()
+    g.initialize()
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
+    sync_state(o, g, star=[("E", "E"), ("J", "J")])
+    o.begin_step()
+    g.begin_step()
+    o.calc_timestep()
+    o.dynamics_apply(o.scalar("Dt"))
+    o.energy_conservation1()
+    sync_state(o, g, star=[("vr", "vr_rel"), ("vt", "vt_rel"), ("E", "E"), ("J", "J")],
+               scalars=("Rtidal", "Mtotal"))
+    o.new_orbits_calculate()
+    o.energy_conservation2()
+    g.new_orbits_calculate()
+    g.check_device("new_orbits_calculate")
+    rn_o, rn_g = o.get("rnew"), g.get("rnew")
+    keep = rn_o != 1e10
+    assert np.array_equal(rn_g == 1e10, ~keep)
+    assert np.array_equal(rn_g[keep], rn_o[keep])
+    assert np.array_equal(g.get("vrnew")[keep], o.get("vrnew")[keep])
+    sampled = keep & (o.get("r_apo") > 0)
+    assert np.array_equal(g.get("X")[sampled], o.get("X")[sampled])
+    g.close()

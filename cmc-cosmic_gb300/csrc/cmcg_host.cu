@@ -27,6 +27,15 @@ struct TileTable {
     Tiles view() const { return Tiles{d_tiles, d_first, d_count, ntiles}; }
 };
 
+// The step in parts, cut where the host exchange overlaps copies with
+// kernels: the time step (which reads r, m, vr, vt only); relaxation to the
+// sort (which swaps the field pointers); potential and energy conservation
+// (r, m, id are final); energies (vr, vt are final).  The host exchange runs
+// part HX_SORT as two: HX_XRELAX marks E, J and relaxes while the caller's E
+// and J are still on their way; HX_XSORT merges them in, then orbits to the
+// sort.
+constexpr int HX_PARTS = 4, HX_SORT = 1, HX_XRELAX = 4, HX_XSORT = 5, HX_ALL = 6;
+
 enum Family { F_BEGIN, F_TIMESTEP, F_RELAX, F_ORBIT, F_TIDAL, F_SORT, F_POT, F_EC3, F_ENERGY, F_END, F_MLP, F_COUNT };
 const char *kFamilyNames[F_COUNT] = {"begin", "timestep", "relax", "orbit", "tidal",
                                      "sort",  "potential", "ec3", "energy", "end", "mlp"};
@@ -93,13 +102,13 @@ struct cmcg_ctx {
     void *lrn_mem = nullptr;
     // launch variants (autotuner; every variant gives bit-identical results)
     int var[V_COUNT] = {0, 0, 0, 0};
-    // host exchange (cmcg_step_host): the step as two graphs, before and after
-    // the sort, per pointer parity at their start; a copy stream for the
-    // read-back that overlaps the second half
-    cudaGraphExec_t hx[4][2] = {};
-    long hx_launches[4][2] = {};
+    // part graphs of a step (HX_* below), per pointer parity at their start:
+    // single steps and the host exchange (cmcg_step_host), whose copies run on
+    // a second stream and overlap the parts
+    cudaGraphExec_t hx[HX_ALL][2] = {};
+    long hx_launches[HX_ALL][2] = {};
     cudaStream_t copy = nullptr;
-    cudaEvent_t ev_sorted = nullptr, ev_copied = nullptr, ev_in = nullptr, ev_ec3 = nullptr;
+    cudaEvent_t ev_sorted = nullptr, ev_copied = nullptr, ev_in = nullptr, ev_ec3 = nullptr, ev_ej = nullptr;
     long long *d_nout = nullptr;  // per cluster: stars after the step
     // graphs
     // The sort swaps the field pointers every step, so a captured two-step
@@ -468,6 +477,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_ec3, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_ej, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&c->d_nout, (size_t)nclusters * sizeof(long long)) != cudaSuccess) {
         cudaGetLastError();
         cmcg_destroy(c);
@@ -490,11 +500,11 @@ int cmcg_destroy(cmcg_ctx *c)
     if (c->arena) cudaFree(c->arena);
     if (c->net_mem) cudaFree(c->net_mem);
     if (c->lrn_mem) cudaFree(c->lrn_mem);
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < HX_ALL; ++a)
         for (int p = 0; p < 2; ++p)
             if (c->hx[a][p]) cudaGraphExecDestroy(c->hx[a][p]);
     if (c->copy) cudaStreamDestroy(c->copy);
-    for (cudaEvent_t e : {c->ev_sorted, c->ev_copied, c->ev_in, c->ev_ec3})
+    for (cudaEvent_t e : {c->ev_sorted, c->ev_copied, c->ev_in, c->ev_ec3, c->ev_ej})
         if (e) cudaEventDestroy(e);
     if (c->d_nout) cudaFree(c->d_nout);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -565,6 +575,48 @@ __global__ void k_set_count(const Cluster *cls, int k, long long N)
     sc->N_MAX = N;
     sc->N_MAX_NEW = N;
     sc->ridx_ok = 0;
+}
+
+// Host exchange: the caller's E and J travel into rnew and vrnew (which
+// nothing reads before the orbits write them) while the relaxation runs.
+// k_xchg_mark first fills E and J of stars 1..N with a bit pattern that the
+// relaxation never writes (an all-ones NaN: the GPU's arithmetic returns the
+// canonical NaN, sign bit clear); after the relaxation k_xchg_merge
+// takes the staged pair wherever both still hold it.  Those are the stars the
+// relaxation left alone, whose E and J put_stars would have set.
+constexpr unsigned long long XCHG_MARK = ~0ull;
+constexpr int XCHG_THREADS = 256;
+
+__global__ void __launch_bounds__(XCHG_THREADS) k_xchg_mark(const Cluster *__restrict__ cls, Tiles tm, Fields f)
+{
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
+    const long long N = C.sc->N_MAX, i0 = C.off + 1 + (long long)ct.y * POT_T;
+    const long long n = N - (long long)ct.y * POT_T;  // stars of this tile with index <= N
+    unsigned long long *E = (unsigned long long *)f.E, *J = (unsigned long long *)f.J;
+    for (int q = threadIdx.x; q < POT_T && q < n; q += XCHG_THREADS) {
+        E[i0 + q] = XCHG_MARK;
+        J[i0 + q] = XCHG_MARK;
+    }
+}
+
+__global__ void __launch_bounds__(XCHG_THREADS) k_xchg_merge(const Cluster *__restrict__ cls, Tiles tm, Fields f)
+{
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    if (!counts_ok(C)) return;
+    const long long N = C.sc->N_MAX, i0 = C.off + 1 + (long long)ct.y * POT_T;
+    const long long n = N - (long long)ct.y * POT_T;
+    unsigned long long *E = (unsigned long long *)f.E, *J = (unsigned long long *)f.J;
+    const unsigned long long *sE = (const unsigned long long *)f.rnew, *sJ = (const unsigned long long *)f.vrnew;
+    for (int q = threadIdx.x; q < POT_T && q < n; q += XCHG_THREADS) {
+        const long long g = i0 + q;
+        if (E[g] == XCHG_MARK && J[g] == XCHG_MARK) {
+            E[g] = sE[g];
+            J[g] = sJ[g];
+        }
+    }
 }
 
 int cmcg_put_stars(cmcg_ctx *c, int k, long N, const double *r, const double *m, const double *vr, const double *vt,
@@ -689,6 +741,14 @@ static int L_relax(cmcg_ctx *c, double dt)
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
+static int L_xchg(cmcg_ctx *c, bool merge)
+{
+    (merge ? k_xchg_merge : k_xchg_mark)<<<c->t1024.ntiles, XCHG_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(),
+                                                                                        c->f);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
+}
+
 static int L_orbit(cmcg_ctx *c)
 {
     fam_begin(c, F_ORBIT);
@@ -802,11 +862,6 @@ static int L_ec3(cmcg_ctx *c)
         if (rc_) return rc_;  \
     } while (0)
 
-// The step in four parts, cut where the host exchange overlaps copies with
-// kernels: the time step (which reads r, m, vr, vt only); relaxation to the
-// sort (which swaps the field pointers); potential and energy conservation
-// (r, m, id are final); energies (vr, vt are final).
-constexpr int HX_PARTS = 4, HX_SORT = 1;
 static int issue_part(cmcg_ctx *c, int part)
 {
     switch (part) {
@@ -823,6 +878,16 @@ static int issue_part(cmcg_ctx *c, int part)
     case 2:
         RUN(L_pot(c));
         RUN(L_ec3(c));
+        break;
+    case HX_XRELAX:
+        RUN(L_xchg(c, false));
+        RUN(L_relax(c, -1.0));
+        break;
+    case HX_XSORT:
+        RUN(L_xchg(c, true));
+        RUN(L_orbit(c));
+        RUN(L_tidal(c));
+        RUN(L_sort(c));
         break;
     default:
         RUN(L_energy(c));
@@ -844,8 +909,8 @@ __global__ void k_gather_counts(const Cluster *cls, int nclusters, long long *ou
 }
 
 // Runs part `part` of a step from a graph captured at the current parity
-// (capturing it first).  Part HX_SORT ends with the sort's pointer swap,
-// which the host mirrors after the launch.
+// (capturing it first).  Parts HX_SORT and HX_XSORT end with the sort's
+// pointer swap, which the host mirrors after the launch.
 static int run_part_graph(cmcg_ctx *c, int part)
 {
     const int p = c->parity;
@@ -860,7 +925,8 @@ static int run_part_graph(cmcg_ctx *c, int part)
         c->profile = prof;
         c->hx_launches[part][p] = c->launches - l0;
         c->launches = l0;
-        if (part == HX_SORT && c->parity != p) swap_sorted(c);  // the capture ran no kernel: undo the swap
+        const bool sorts = part == HX_SORT || part == HX_XSORT;
+        if (sorts && c->parity != p) swap_sorted(c);  // the capture ran no kernel: undo the swap
         if (rc) {
             if (g) cudaGraphDestroy(g);
             return rc;
@@ -872,7 +938,7 @@ static int run_part_graph(cmcg_ctx *c, int part)
     }
     CK(cudaGraphLaunch(c->hx[part][p], c->stream));
     c->launches += c->hx_launches[part][p];
-    if (part == HX_SORT) swap_sorted(c);
+    if (part == HX_SORT || part == HX_XSORT) swap_sorted(c);
     return CMCG_OK;
 }
 
@@ -1386,7 +1452,7 @@ static void drop_graphs(cmcg_ctx *c)
         c->gexec[p] = nullptr;
         c->graph[p] = nullptr;
         c->graph_ready[p] = false;
-        for (int a = 0; a < HX_PARTS; ++a) {
+        for (int a = 0; a < HX_ALL; ++a) {
             if (c->hx[a][p]) cudaGraphExecDestroy(c->hx[a][p]);
             c->hx[a][p] = nullptr;
         }
@@ -1703,17 +1769,25 @@ static int step_host_run(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
     }
     CK(cudaEventRecord(c->ev_in, c->stream));
     CK(cudaStreamWaitEvent(c->copy, c->ev_in, 0));  // the copy stream's uploads follow the counts
+    // id (the relaxation's draws) during the time step; E and J, staged,
+    // during the relaxation
     for (int k = 0; k < c->ncl; ++k) {
         const long long o = c->off[k] + 1;
-        const long N = in[k].N;
-        CK(cudaMemcpyAsync(c->f.id + o, in[k].id, (size_t)N * sizeof(long long), cudaMemcpyHostToDevice, c->copy));
-        CK(up(c->f.E + o, in[k].E, N, c->copy));
-        CK(up(c->f.J + o, in[k].J, N, c->copy));
+        CK(cudaMemcpyAsync(c->f.id + o, in[k].id, (size_t)in[k].N * sizeof(long long), cudaMemcpyHostToDevice,
+                           c->copy));
     }
     CK(cudaEventRecord(c->ev_in, c->copy));
+    for (int k = 0; k < c->ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        CK(up(c->f.rnew + o, in[k].E, in[k].N, c->copy));
+        CK(up(c->f.vrnew + o, in[k].J, in[k].N, c->copy));
+    }
+    CK(cudaEventRecord(c->ev_ej, c->copy));
     RUN(part(0));
     CK(cudaStreamWaitEvent(c->stream, c->ev_in, 0));
-    RUN(part(1));
+    RUN(part(HX_XRELAX));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_ej, 0));
+    RUN(part(HX_XSORT));
     CK(cudaEventRecord(c->ev_sorted, c->stream));
     CK(cudaStreamWaitEvent(c->copy, c->ev_sorted, 0));
     // a cluster never grows in a step: N given in bounds the stars after it

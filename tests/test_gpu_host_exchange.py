@@ -1,6 +1,8 @@
-"""cmcg_step_host (upload, step in two graph-replayed halves, read-back that
-overlaps the second half) gives exactly what put_stars + step + get_stars
-give, with and without graphs, for one cluster and for an uneven ensemble."""
+"""cmcg_step_host (upload, step in graph-replayed parts, copies that overlap
+them) gives exactly what put_stars + step + get_stars give, with and without
+graphs, for one cluster and for an uneven ensemble.  The caller's E and J
+arrive during the relaxation and are merged in for the stars it leaves alone:
+with the relaxation off that is every star."""
 import numpy as np
 import pytest
 
@@ -11,8 +13,8 @@ pytestmark = pytest.mark.gpu
 KEYS = ("r", "m", "vr", "vt", "E", "J", "id")
 
 
-def _ctx(ics, seed):
-    ps = [cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed + i) for i, ic in enumerate(ics)]
+def _ctx(ics, seed, **kw):
+    ps = [cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed + i, **kw) for i, ic in enumerate(ics)]
     g = cmcgpu.Context([len(ic["r"]) for ic in ics], ps)
     for c, ic in enumerate(ics):
         g.load(c, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
@@ -55,6 +57,36 @@ def test_step_host_equals_put_step_get(gpulib, sizes):
                 assert np.array_equal(bufs[c][k][:n], state["ref"][1][c][k][:n]), (name, c, k)
     for g in (ref, hx_graph, hx_direct):
         g.close()
+
+
+@pytest.mark.parametrize("relaxation", [0, 1])
+def test_step_host_takes_callers_E_J(gpulib, relaxation):
+    # E and J changed on the host between steps: without relaxation the
+    # orbits read them for every star, with it for the unpaired last star
+    ic = cmcgpu.generate(cmcgpu.KING, 12001, seed=98, imf=1)
+    out = {}
+    for name in ("ref", "graph", "direct"):
+        g = _ctx([ic], 13, RELAXATION=relaxation)
+        g.use_graph(name == "graph")
+        b = _bufs(12001)
+        n = g.get_stars(0, b)
+        for _ in range(3):
+            b["E"][:n] *= 1.0 + 1e-7
+            b["J"][:n] *= 1.0 - 1e-7
+            if name == "ref":
+                g.put_stars(0, n, b)
+                g.step(1)
+                n = g.get_stars(0, b)
+            else:
+                (n,) = g.step_host([(n, b)], [b])
+            g.check_device(name)
+        out[name] = (n, b)
+        g.close()
+    for name in ("graph", "direct"):
+        assert out[name][0] == out["ref"][0], name
+        n = out[name][0]
+        for k in KEYS:
+            assert np.array_equal(out[name][1][k][:n], out["ref"][1][k][:n]), (name, k)
 
 
 def test_single_steps_from_part_graphs_equal_direct_steps(gpulib):

@@ -102,7 +102,7 @@ struct cmcg_ctx {
     void *lrn_mem = nullptr;
     // launch variants (autotuner; every variant gives bit-identical results)
     int var[V_COUNT] = {0, 0, 0, 0};
-    // part graphs of a step (HX_* below), per pointer parity at their start:
+    // part graphs of a step (HX_* above), per pointer parity at their start:
     // single steps and the host exchange (cmcg_step_host), whose copies run on
     // a second stream and overlap the parts
     cudaGraphExec_t hx[HX_ALL][2] = {};

@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_ghist(const Cluster *__re
 // earlier passes and sorts carry another epoch and read as not ready, so the
 // words are never cleared (graph replays included).
 constexpr unsigned long long ST_AGG = 1ull << 32, ST_INC = 2ull << 32, ST_VAL = 0xffffffffull;
+constexpr int LOOKBACK = 8;  // predecessor tiles read per round trip of the look-back
 __device__ __forceinline__ unsigned long long st_tag(unsigned int epoch, int pass)
 {
     return ((unsigned long long)((epoch * SORT_MAX_PASSES + (unsigned)pass) & 0x3fffffffu)) << 34;
@@ -276,22 +277,31 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
         unsigned long long *st = sb.status + (size_t)b * RADIX;
         atomicExch(st + d, tag | (ct.y == 0 ? ST_INC : ST_AGG) | cnt);
         if (ct.y > 0) {
+            // walk back to the nearest inclusive prefix, summing aggregates on
+            // the way; LOOKBACK predecessors are read at once, so a long run
+            // of aggregates costs one round trip per LOOKBACK tiles
+            const int jfirst = b - ct.y;  // the cluster's first tile publishes inclusive
             int j = b - 1;
             long long spins = 0;
-            while (true) {
-                const unsigned long long v = *(volatile unsigned long long *)(sb.status + (size_t)j * RADIX + d);
-                if ((v & ~(ST_INC | ST_AGG | ST_VAL)) == tag) {
-                    if (v & ST_INC) {
-                        prefix += v & ST_VAL;
-                        break;
-                    }
-                    if (v & ST_AGG) {
-                        prefix += v & ST_VAL;
-                        --j;  // tile j is not the cluster's first (that one publishes inclusive)
-                        continue;
-                    }
+            bool found = false;
+            while (!found) {
+                unsigned long long v[LOOKBACK];
+#pragma unroll
+                for (int q = 0; q < LOOKBACK; ++q)
+                    v[q] = (j - q >= jfirst) ? *(volatile unsigned long long *)(sb.status + (size_t)(j - q) * RADIX + d)
+                                             : 0ull;
+                int used = 0;
+#pragma unroll
+                for (int q = 0; q < LOOKBACK; ++q) {
+                    if (found || used < q || j - q < jfirst) continue;
+                    if ((v[q] & ~(ST_INC | ST_AGG | ST_VAL)) != tag || !(v[q] & (ST_INC | ST_AGG))) continue;
+                    prefix += v[q] & ST_VAL;
+                    if (v[q] & ST_INC) found = true;
+                    else used = q + 1;  // an aggregate: go on to the next older tile
                 }
-                if (++spins > CMCG_SPIN_LIMIT) {
+                if (found) break;
+                j -= used;
+                if (used == 0 && ++spins > CMCG_SPIN_LIMIT) {
                     set_error(C.sc, CMCG_ERR_SPIN, j);
                     break;
                 }

@@ -260,6 +260,23 @@ __device__ __forceinline__ bool ge_pos(double x, double c)  // x >= c
     const unsigned long long b = ubits(x);
     return b >= ubits(c) && b <= INF_BITS;
 }
+// An ordered integer key of a double that is not a NaN: okey(x) < okey(y)
+// exactly when x < y, and okey(-0.0) == okey(+0.0).
+__device__ __forceinline__ long long okey(double x)
+{
+    const unsigned long long b = ubits(x), m = b & ~SIGN_BIT;
+    return (b & SIGN_BIT) ? -(long long)m : (long long)m;
+}
+// The key a bound c is compared by in gt_key: a NaN bound gets a key no
+// double reaches, since x > NaN is false.
+__device__ __forceinline__ long long bound_key(double c)
+{
+    return (ubits(c) & ~SIGN_BIT) > INF_BITS ? 0x7fffffffffffffffll : okey(c);
+}
+__device__ __forceinline__ bool gt_key(double x, long long kc)  // x > c, with kc = bound_key(c)
+{
+    return (ubits(x) & ~SIGN_BIT) <= INF_BITS && okey(x) > kc;
+}
 __device__ __forceinline__ bool gt_pos(double x, double c)  // x > c
 {
     const unsigned long long b = ubits(x);

@@ -1237,6 +1237,7 @@ __global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict
             const long long i0 = 1 + (long long)ct.y * TID_T + threadIdx.x;
             const double *crit = (C.TIDAL_TREATMENT == 0) ? f.r_apo : f.E;
             const double bound = (C.TIDAL_TREATMENT == 0) ? Rtidal : gierszalpha * phi_rtidal;
+            const long long kbound = bound_key(bound);  // the tests below are integer ones
             double rnv[IT], cv[IT];
 #pragma unroll
             for (int it = 0; it < IT; ++it) {
@@ -1249,7 +1250,7 @@ __global__ void __launch_bounds__(TID_THREADS) k_tidal(const Cluster *__restrict
             for (int it = 0; it < IT; ++it) {
                 const long long g = off + i0 + it * TID_THREADS;
                 // r_apo > Rtidal (treatment 0) or E > gierszalpha * phi_rtidal, and rnew < 1e6
-                if (cv[it] > bound && rnv[it] < 1000000) {
+                if (gt_key(cv[it], kbound) && lt_pos(rnv[it], 1000000.0)) {
                     const double m = f.m[g], E = f.E[g], J = f.J[g];
                     acc[0] += E * m / NSTAR;
                     acc[1] += J * m / NSTAR;

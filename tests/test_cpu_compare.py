@@ -1,5 +1,5 @@
 """The integer forms of FP64 comparisons the kernels use (ge0, lt0, le0, gt0,
-eq0, lt_pos, ge_pos, gt_pos in cmcg_internal.cuh), restated here on the
+eq0, lt_pos, ge_pos, gt_pos, okey/bound_key/gt_key in cmcg_internal.cuh), restated here on the
 uint64 bit patterns and checked against IEEE comparisons over signed zeros,
 subnormals, infinities, NaNs of both signs and random values."""
 import numpy as np
@@ -50,6 +50,21 @@ def gt_pos(x, c):
     return (b > bits(c)) & (b <= INF)
 
 
+def okey(x):
+    b = np.atleast_1d(bits(x)).astype(object)
+    m = [int(v) & ~int(SIGN) for v in b]
+    return [-mm if (int(v) & int(SIGN)) else mm for v, mm in zip(b, m)]
+
+
+def bound_key(c):
+    return (1 << 63) - 1 if (int(bits(c)) & ~int(SIGN)) > int(INF) else okey(c)[0]
+
+
+def gt_key(x, kc):
+    m = [int(v) & ~int(SIGN) for v in bits(x).astype(object)]
+    return np.array([mm <= int(INF) and k > kc for mm, k in zip(m, okey(x))])
+
+
 def _values():
     rng = np.random.default_rng(3)
     special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, -np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
@@ -79,6 +94,15 @@ def test_positive_constant_comparisons_match_ieee():
             assert np.array_equal(gt_pos(x, c), x > c), c
     # the kernels' constant helpers and these restatements read the same patterns
     assert bits(0.0) == 0 and bits(-0.0) == SIGN and bits(np.inf) == INF
+
+
+def test_signed_bound_comparisons_match_ieee():
+    # k_tidal's criterion E > gierszalpha * phi_rtidal (a negative bound) or
+    # r_apo > Rtidal, on ordered integer keys
+    x = _values()
+    for c in (-0.7321, -1e-20, -0.0, 0.0, 1e-20, 3.5, -np.inf, np.inf, np.nan, -np.nan, 5e-324, -5e-324):
+        with np.errstate(invalid="ignore"):
+            assert np.array_equal(gt_key(x, bound_key(c)), x > c), c
 
 
 def f2_split(x):

@@ -256,8 +256,9 @@ int cmcg_learned_stats(cmcg_ctx *ctx, uint64_t *out /* CMCG_LSTAT_N */);
  * One step on host star arrays, one cmcg_stars per cluster: in[k] (N stars,
  * 0-based, as cmcg_put_stars takes them) is uploaded, the step runs, and
  * out[k] receives the stars after it (out[k].N set; out[k].cap >= in[k].N).
- * r, m and id are read back while the second half of the step (potential,
- * energy conservation, energies) still runs; graphs are used when enabled.
+ * E and J go up while the relaxation runs; r, m and id are read back while
+ * the potential, energy conservation and energies still run; graphs are
+ * used when enabled.
  * in and out may be the same arrays.  Pinned host memory gives full copy
  * speed.  The call returns once every copy has finished, on errors too.
  * Equivalent to cmcg_put_stars + cmcg_step + cmcg_get_stars. */

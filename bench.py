@@ -52,8 +52,8 @@ NCU_FP64_PIPE_ACTIVE = {"orbit": 0.685, "relax": 0.703}
 # smsp__sass_thread_inst_executed_op_fp64_pred_on.sum over the stars of one
 # step, King W0=6 + Kroupa, N = 1e6), and the measured FP64 FMA rate of this
 # GPU (bench.py --probe-rates: 1.01 TFLOP/s = 5.05e11 DFMA/s)
-NCU_FP64_OPS_PER_STAR = {"orbit": 343.2, "relax": 181.1, "potential": 53.3, "ec3": 45.0, "energy": 11.8,
-                         "timestep": 12.1, "tidal": 7.8}
+NCU_FP64_OPS_PER_STAR = {"orbit": 343.2, "relax": 181.1, "potential": 61.4, "ec3": 45.0, "energy": 11.8,
+                         "timestep": 12.1, "tidal": 2.1}
 FP64_PEAK_OPS = 5.05e11
 
 

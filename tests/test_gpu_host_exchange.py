@@ -89,6 +89,33 @@ def test_step_host_takes_callers_E_J(gpulib, relaxation):
             assert np.array_equal(out[name][1][k][:n], out["ref"][1][k][:n]), (name, k)
 
 
+def test_step_host_with_learned_proposal(gpulib):
+    # the learned sampler's passes read E and J after the merge like the plain one
+    ic = cmcgpu.generate(cmcgpu.PLUMMER, 20000, seed=99, imf=0)
+    out = {}
+    for name in ("ref", "hx"):
+        g = _ctx([ic], 15)
+        g.mlp_init(3)
+        g.set_learned(cmcgpu.LEARN_ON, 1.2)
+        g.use_graph(name == "hx")
+        b = _bufs(20000)
+        n = g.get_stars(0, b)
+        for _ in range(3):
+            if name == "ref":
+                g.put_stars(0, n, b)
+                g.step(1)
+                n = g.get_stars(0, b)
+            else:
+                (n,) = g.step_host([(n, b)], [b])
+            g.check_device(name)
+        out[name] = (n, b)
+        g.close()
+    assert out["hx"][0] == out["ref"][0]
+    n = out["hx"][0]
+    for k in KEYS:
+        assert np.array_equal(out["hx"][1][k][:n], out["ref"][1][k][:n]), k
+
+
 def test_single_steps_from_part_graphs_equal_direct_steps(gpulib):
     ic = cmcgpu.generate(cmcgpu.KING, 20000, seed=95, imf=1)
     a, b = _ctx([ic], 9), _ctx([ic], 9)

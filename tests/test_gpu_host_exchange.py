@@ -59,14 +59,15 @@ def test_step_host_equals_put_step_get(gpulib, sizes):
         g.close()
 
 
-@pytest.mark.parametrize("relaxation", [0, 1])
-def test_step_host_takes_callers_E_J(gpulib, relaxation):
+@pytest.mark.parametrize("relaxation,fp32", [(0, 0), (1, 0), (1, 1)])
+def test_step_host_takes_callers_E_J(gpulib, relaxation, fp32):
     # E and J changed on the host between steps: without relaxation the
-    # orbits read them for every star, with it for the unpaired last star
+    # orbits read them for every star, with it (FP64 or FP32 kinematics) for
+    # the unpaired last star
     ic = cmcgpu.generate(cmcgpu.KING, 12001, seed=98, imf=1)
     out = {}
     for name in ("ref", "graph", "direct"):
-        g = _ctx([ic], 13, RELAXATION=relaxation)
+        g = _ctx([ic], 13, RELAXATION=relaxation, relax_fp32=fp32)
         g.use_graph(name == "graph")
         b = _bufs(12001)
         n = g.get_stars(0, b)

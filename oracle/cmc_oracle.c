@@ -20,6 +20,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "brent1973.h"
+#include "philox.h"
+
 /* include/cmc/cmc.h:58-64 */
 #define SF_INFINITY 1.0e10
 #define ZERO 1.0e-20
@@ -73,32 +76,10 @@ static int fail(ocmc_state *s, int code, long idx)
 
 /* ---------------------------------------------------------------- RNG ---- */
 
-/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the
- * multiply-xor bijection with Weyl key schedule. */
+/* Philox4x32-10: philox.h */
 void ocmc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4])
 {
-    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
-    uint32_t k0 = key_in[0], k1 = key_in[1];
-    for (int round = 0; round < 10; ++round) {
-        if (round > 0) {
-            k0 += 0x9E3779B9u;
-            k1 += 0xBB67AE85u;
-        }
-        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
-        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
-        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-        uint32_t n0 = hi1 ^ c1 ^ k0;
-        uint32_t n2 = hi0 ^ c3 ^ k1;
-        c0 = n0;
-        c1 = lo1;
-        c2 = n2;
-        c3 = lo0;
-    }
-    out[0] = c0;
-    out[1] = c1;
-    out[2] = c2;
-    out[3] = c3;
+    philox4x32_10(ctr_in, key_in, out);
 }
 
 /* taus113 (L'Ecuyer 1999), seeding by the 69069 LCG with minimum-bit fixes and
@@ -654,100 +635,7 @@ static double vr2_in_interval(ocmc_state *s, double r, long index, long k, doubl
     return function_q(s, index, r, pot, E, J);
 }
 
-/* Brent's method for a bracketed zero (R. P. Brent, "Algorithms for Minimization
- * without Derivatives", 1973, ch. 4, procedure zero), one interpolation or
- * bisection step per call, the bracket kept as [b, c].  This stands in for
- * gsl_root_fsolver_brent, whose sources are not part of the reference. */
-typedef struct {
-    double a, b, c, d, e, fa, fb, fc;
-    int exact; /* f(b) == 0: the bracket collapses to [b, b] */
-} brent_t;
-
-static int brent_set(brent_t *z, double fl, double fu, double lo, double hi)
-{
-    z->a = lo;
-    z->fa = fl;
-    z->b = hi;
-    z->fb = fu;
-    z->c = hi;
-    z->fc = fu;
-    z->d = hi - lo;
-    z->e = hi - lo;
-    z->exact = 0;
-    if ((fl < 0.0 && fu < 0.0) || (fl > 0.0 && fu > 0.0)) return 1;
-    return 0;
-}
-
-static void brent_fix_bracket(brent_t *z)
-{
-    if ((z->fb < 0.0 && z->fc < 0.0) || (z->fb > 0.0 && z->fc > 0.0)) {
-        z->c = z->a;
-        z->fc = z->fa;
-        z->d = z->b - z->a;
-        z->e = z->b - z->a;
-    }
-    if (fabs(z->fc) < fabs(z->fb)) {
-        z->a = z->b;
-        z->b = z->c;
-        z->c = z->a;
-        z->fa = z->fb;
-        z->fb = z->fc;
-        z->fc = z->fa;
-    }
-}
-
-/* returns the new abscissa at which the caller must evaluate f */
-static double brent_propose(brent_t *z)
-{
-    brent_fix_bracket(z);
-    double tol = 0.5 * DBL_EPSILON * fabs(z->b);
-    double m = 0.5 * (z->c - z->b);
-    if (z->fb == 0.0 || fabs(m) <= tol) return z->b;
-    if (fabs(z->e) < tol || fabs(z->fa) <= fabs(z->fb)) {
-        z->d = m;
-        z->e = m;
-    } else {
-        double p, q, r, s = z->fb / z->fa;
-        if (z->a == z->c) {
-            p = 2.0 * m * s;
-            q = 1.0 - s;
-        } else {
-            q = z->fa / z->fc;
-            r = z->fb / z->fc;
-            p = s * (2.0 * m * q * (q - r) - (z->b - z->a) * (r - 1.0));
-            q = (q - 1.0) * (r - 1.0) * (s - 1.0);
-        }
-        if (p > 0.0)
-            q = -q;
-        else
-            p = -p;
-        double min1 = 3.0 * m * q - fabs(tol * q), min2 = fabs(z->e * q);
-        if (2.0 * p < (min1 < min2 ? min1 : min2)) {
-            z->e = z->d;
-            z->d = p / q;
-        } else {
-            z->d = m;
-            z->e = m;
-        }
-    }
-    z->a = z->b;
-    z->fa = z->fb;
-    if (fabs(z->d) > tol)
-        z->b += z->d;
-    else
-        z->b += (m > 0 ? tol : -tol);
-    return z->b;
-}
-
-static void brent_accept(brent_t *z, double fb)
-{
-    z->fb = fb;
-    if (fb == 0.0) {
-        z->exact = 1;
-        return;
-    }
-    brent_fix_bracket(z);
-}
+/* Brent (1973): oracle/brent1973.h */
 
 /* find_root_vr, cmc_nr.c:500-603 */
 static double find_root_vr(ocmc_state *s, long index, long k, double E, double J)

@@ -4,9 +4,15 @@ The oracle (cmc_oracle.c) restates the reference's single-rank Henon step in C
 and is the parity checker for the GPU kernels.  Only the tests, the smoke
 check and bench.py's CPU-baseline leg use it.
 
-``build()`` compiles it (and, where the reference tree is present, its own
-taus113 generator into oracle/_ref for pinning); the products go to
-oracle/_build and oracle/_ref, both outside version control.
+``build()`` compiles it into oracle/_build.  ``build_ref()`` runs the recipe
+oracle/ref.mk where the reference tree is present: it compiles the
+reference's own Henon-step TUs in place against single-rank MPI / GSL / HDF5
+shims (oracle/refshim) into oracle/_ref/libcmcref.so, and the reference's
+taus113 generator into oracle/_ref/libtaus113ref.so.  ``RefOracle`` drives
+libcmcref.so with the same interface as ``Oracle``, so that the restatement
+is pinned to the reference's own code phase by phase.  Both build folders
+stay outside version control.  The reference tree is $CMC_REFERENCE_ROOT, or
+the recipe's default.
 """
 from __future__ import annotations
 
@@ -21,7 +27,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libcmcoracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_TAUS = os.path.join(REF_DIR, "libtaus113ref.so")
-REFERENCE_ROOT = os.environ.get("CMC_REFERENCE_ROOT", "/root/reference")
+REF_LIB = os.path.join(REF_DIR, "libcmcref.so")
+REF_MK = os.path.join(HERE, "ref.mk")
 
 DRAW_COUNTER, DRAW_TAUS113 = 0, 1
 SITE_Y, SITE_PENC, SITE_PSI, SITE_TRIAL, SITE_SIGN = 1, 2, 3, 4, 5
@@ -37,17 +44,29 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+def reference_root() -> str | None:
+    """The reference tree: $CMC_REFERENCE_ROOT, else the recipe's default;
+    None when it is not there (as on a machine without the reference)."""
+    root = os.environ.get("CMC_REFERENCE_ROOT")
+    if not root:
+        res = subprocess.run(["make", "-s", "-f", REF_MK, "print-root"], capture_output=True, text=True)
+        root = res.stdout.strip()
+    if root and os.path.exists(os.path.join(root, "src", "cmc", "cmc_utils.c")):
+        return root
+    return None
+
+
 def build_ref() -> str | None:
-    """Compile the reference's own taus113-v2.c in place into oracle/_ref (pinning
-    the oracle's generator); returns None when the reference tree is absent."""
-    src = os.path.join(REFERENCE_ROOT, "src", "libs", "taus113-v2.c")
-    inc = os.path.join(REFERENCE_ROOT, "include", "common")
-    if not os.path.exists(src):
+    """Build oracle/_ref (libcmcref.so, libtaus113ref.so) with oracle/ref.mk;
+    returns the reference-step library, or None when the reference tree is
+    absent."""
+    root = reference_root()
+    if root is None:
         return None
-    os.makedirs(REF_DIR, exist_ok=True)
-    if not os.path.exists(REF_TAUS) or os.path.getmtime(REF_TAUS) < os.path.getmtime(src):
-        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-I", inc, "-o", REF_TAUS, src])
-    return REF_TAUS
+    jobs = str(min(8, os.cpu_count() or 2))
+    subprocess.check_call(["make", "-s", "-j", jobs, "-f", REF_MK, f"REFERENCE_ROOT={root}", "all"],
+                          stdout=subprocess.DEVNULL)
+    return REF_LIB
 
 
 class OParams(C.Structure):
@@ -215,6 +234,127 @@ class Oracle:
 
     def draw(self, site, star_id, n, word):
         return float(lib().ocmc_draw(self._h, site, star_id, n, word))
+
+
+def ref_lib() -> C.CDLL:
+    """A private copy of oracle/_ref/libcmcref.so, the reference's own step
+    (see build_ref).  The reference keeps its whole state in globals and
+    expects one run per process, so each caller gets its own copy of the
+    library, loaded from a temporary file: its globals start zeroed, as in a
+    fresh process, and no two instances share them."""
+    import shutil
+    import tempfile
+
+    path = build_ref()
+    if path is None:
+        raise RuntimeError("the reference tree is not present: libcmcref.so cannot be built")
+    fd, tmp = tempfile.mkstemp(prefix="cmcref_", suffix=".so")
+    os.close(fd)
+    try:
+        shutil.copyfile(path, tmp)
+        L = C.CDLL(tmp, mode=getattr(os, "RTLD_LOCAL", 0))
+    finally:
+        os.unlink(tmp)
+    vp = C.c_void_p
+    L.cmcref_create.argtypes = [C.POINTER(OParams), C.c_long, vp, vp, vp, vp, vp]
+    for n in ["cmcref_initialize", "cmcref_begin_step", "cmcref_calc_timestep", "cmcref_energy_conservation1",
+              "cmcref_new_orbits_calculate", "cmcref_energy_conservation2", "cmcref_tidally_strip_stars",
+              "cmcref_compute_intermediate_energy", "cmcref_qsorts_new", "cmcref_calc_potential",
+              "cmcref_energy_conservation3", "cmcref_compute_energy", "cmcref_end_step", "cmcref_step",
+              "cmcref_last_error", "cmcref_sizeof_star"]:
+        getattr(L, n).argtypes = []
+    L.cmcref_nstars.restype = C.c_long
+    L.cmcref_dynamics_apply.argtypes = [C.c_double]
+    L.cmcref_potential.argtypes = [C.c_double]
+    L.cmcref_potential.restype = C.c_double
+    L.cmcref_get_field.argtypes = [C.c_char_p, vp, C.c_long]
+    L.cmcref_get_field.restype = C.c_long
+    L.cmcref_set_field.argtypes = [C.c_char_p, vp, C.c_long]
+    L.cmcref_set_field.restype = C.c_long
+    L.cmcref_get_ids.argtypes = [vp, C.c_long]
+    L.cmcref_get_ids.restype = C.c_long
+    L.cmcref_get_scalar.argtypes = [C.c_char_p]
+    L.cmcref_get_scalar.restype = C.c_double
+    L.cmcref_set_scalar.argtypes = [C.c_char_p, C.c_double]
+    L.cmcref_last_error_what.restype = C.c_char_p
+    return L
+
+
+class RefOracle:
+    """One cluster stepped by the reference's own code (libcmcref.so), with the
+    same interface as Oracle; each instance has its own copy of the library."""
+
+    def __init__(self, ic: dict, params: OParams):
+        r, m, vr, vt = (np.ascontiguousarray(ic[k], dtype=np.float64) for k in ("r", "m", "vr", "vt"))
+        ids = np.ascontiguousarray(ic.get("id", np.arange(1, len(r) + 1)), dtype=np.int64)
+        self.params = params
+        self._L = L = ref_lib()
+        rc = L.cmcref_create(C.byref(params), len(r), r.ctypes.data, m.ctypes.data, vr.ctypes.data,
+                             vt.ctypes.data, ids.ctypes.data)
+        if rc:
+            raise OracleError(rc, "cmcref_create (" + L.cmcref_last_error_what().decode() + ")", -1)
+        self._open = True
+
+    def close(self):
+        if self._open:
+            self._L.cmcref_destroy()
+            self._open = False
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name, *args):
+        L = self._L
+        rc = getattr(L, name)(*args)
+        if rc:
+            raise OracleError(rc, name + " (" + L.cmcref_last_error_what().decode() + ")", -1)
+
+    def __getattr__(self, item):
+        fn = "cmcref_" + item
+        if item.startswith("_") or not hasattr(self._L, fn):
+            raise AttributeError(item)
+        return lambda *a: self._call(fn, *a)
+
+    def get(self, name: str) -> np.ndarray:
+        n = self._L.cmcref_nstars() + 2
+        out = np.zeros(max(n, 2))
+        got = self._L.cmcref_get_field(name.encode(), out.ctypes.data, len(out))
+        if got < 0:
+            raise KeyError(name)
+        return out[:got].copy()
+
+    def set(self, name: str, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        if self._L.cmcref_set_field(name.encode(), v.ctypes.data, len(v)) < 0:
+            raise KeyError(name)
+
+    def ids(self) -> np.ndarray:
+        n = self._L.cmcref_nstars()
+        out = np.zeros(max(n, 1), np.int64)
+        got = self._L.cmcref_get_ids(out.ctypes.data, len(out))
+        return out[:got].copy()
+
+    def scalar(self, name: str) -> float:
+        return float(self._L.cmcref_get_scalar(name.encode()))
+
+    def set_scalar(self, name: str, v: float):
+        if self._L.cmcref_set_scalar(name.encode(), float(v)):
+            raise KeyError(name)
+
+    def potential(self, r: float) -> float:
+        return float(self._L.cmcref_potential(float(r)))
+
+    def nstars(self) -> int:
+        return int(self._L.cmcref_nstars())
 
 
 def philox(ctr, key):

@@ -26,10 +26,9 @@ class TausState(C.Structure):
 
 
 def main():
-    ref = oracle.build_ref()
-    if ref is None:
+    if oracle.build_ref() is None:
         raise SystemExit("reference tree not found; cannot regenerate taus113.json")
-    L = C.CDLL(ref)
+    L = C.CDLL(oracle.REF_TAUS)
     L.reset_rng_t113_new.argtypes = [C.c_ulong, C.POINTER(TausState)]
     L.rng_t113_int_new.argtypes = [C.POINTER(TausState)]
     L.rng_t113_int_new.restype = C.c_ulong

@@ -36,6 +36,9 @@ CUDA_SOURCES = [
     "cmcg_mlp.cu",
 ]
 C_SOURCES = ["cmcg_ic.c"]
+# the synthetic-cluster generator alone (plain C, no CUDA): what the CPU
+# baselines and the oracle tests load to build their models
+IC_LIB = os.path.join(BUILD, "libcmcic.so")
 # the reference-named drop-in layer: a second library on the public C ABI
 DROPIN_SOURCE = "cmc_dropin.cpp"
 DROPIN_LIB = os.path.join(BUILD, "libcmc_dropin.so")
@@ -65,8 +68,20 @@ def _run(cmd: list[str]) -> None:
         sys.stderr.write(res.stdout)
 
 
+def build_ic(force: bool = False) -> str:
+    """libcmcic.so: cmcg_ic_generate and cmcg_derive_seed without the GPU library."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(CSRC, "cmcg_ic.c")
+    hdr = os.path.join(ROOT, "include", "cmcgpu.h")
+    if force or not _newer(IC_LIB, [src, hdr]):
+        _run(["gcc", "-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-shared",
+              "-I" + os.path.join(ROOT, "include"), "-o", IC_LIB, src, "-lm"])
+    return IC_LIB
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    build_ic(force)
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "cmcgpu.h"))
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

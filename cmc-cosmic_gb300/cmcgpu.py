@@ -19,6 +19,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libcmcgpu.so")
+IC_LIB_PATH = os.path.join(_HERE, "_build", "libcmcic.so")
 HEADER = os.path.join(os.path.dirname(_HERE), "include", "cmcgpu.h")
 
 ERRORS = {
@@ -248,6 +249,28 @@ def lib() -> C.CDLL:
     return _lib
 
 
+_ic_lib = None
+
+
+def ic_lib() -> C.CDLL:
+    """libcmcic.so, the synthetic-cluster generator alone (no CUDA): models for
+    the CPU oracle and baselines come from it without mapping the GPU library."""
+    global _ic_lib
+    if _ic_lib is None:
+        if not os.path.exists(IC_LIB_PATH):
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("cmcg_build", os.path.join(_HERE, "build.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build_ic()
+        L = C.CDLL(IC_LIB_PATH)
+        L.cmcg_ic_generate.argtypes = [C.POINTER(ICSpec), C.POINTER(ICOut)]
+        L.cmcg_derive_seed.argtypes = [C.c_uint64, C.c_uint64]
+        L.cmcg_derive_seed.restype = C.c_uint64
+        _ic_lib = L
+    return _ic_lib
+
+
 def header_symbols(path: str = HEADER) -> list[str]:
     """Function names the public header declares."""
     text = open(path).read()
@@ -268,7 +291,7 @@ def generate(model: int, N: int, seed: int, w0: float = 6.0, imf: int = 0, binar
     ids = np.zeros(N, np.int64)
     out = ICOut(*[a[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("r", "m", "vr", "vt")],
                 ids.ctypes.data_as(C.POINTER(C.c_int64)), 0.0)
-    rc = lib().cmcg_ic_generate(C.byref(ICSpec(model, N, w0, imf, binary_fraction, seed)), C.byref(out))
+    rc = ic_lib().cmcg_ic_generate(C.byref(ICSpec(model, N, w0, imf, binary_fraction, seed)), C.byref(out))
     if rc:
         raise CmcError(rc, "cmcg_ic_generate")
     a["id"] = ids
@@ -277,7 +300,7 @@ def generate(model: int, N: int, seed: int, w0: float = 6.0, imf: int = 0, binar
 
 
 def derive_seed(master: int, index: int) -> int:
-    return int(lib().cmcg_derive_seed(master, index))
+    return int(ic_lib().cmcg_derive_seed(master, index))
 
 
 def draw(seed: int, tcount: int, site: int, star_id: int, n: int, word: int) -> float:

@@ -169,3 +169,21 @@ def test_nan_mass_stops_both_at_the_same_star(ref):
             R.calc_potential()
         assert R.nstars() == -1  # the reference's exit_cleanly freed its state
     o.close()
+
+
+def test_golden_refstep_fixtures_are_the_references_output(ref):
+    """tests/golden/refstep_*.npz (the GPU tests' inputs and expected values)
+    equal what the reference's step produces now."""
+    import importlib.util
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_refstep.py")
+    spec = importlib.util.spec_from_file_location("make_refstep", path)
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    for case in mk.CASES:
+        rec = mk.record(case)
+        z = np.load(mk.path_of(case[0]))
+        assert sorted(z.files) == sorted(rec), case[0]
+        for k, v in rec.items():
+            assert np.array_equal(z[k], np.asarray(v)), (case[0], k)

@@ -219,6 +219,7 @@ def lib() -> C.CDLL:
         L.cmcg_draw.restype = d
         L.cmcg_sign_stages.argtypes = [vp, vp, vp, vp, d, vp, vp, l, vp]
         L.cmcg_diagnostics.argtypes = [vp, i, vp, i, i, d, vp]
+        L.cmcg_orbit_counters.argtypes = [vp, i]
         L.cmcg_format_dyn_line.argtypes = [vp, vp, vp, l]
         L.cmcg_format_dyn_line.restype = l
         L.cmcg_format_lagrad_line.argtypes = [vp, vp, l]
@@ -305,6 +306,20 @@ def derive_seed(master: int, index: int) -> int:
 
 def draw(seed: int, tcount: int, site: int, star_id: int, n: int, word: int) -> float:
     return float(lib().cmcg_draw(seed, tcount, site, star_id, n, word))
+
+
+ORBIT_COUNTERS = ("sign_f64", "sign_dd", "root_vr")
+
+
+def orbit_counters(reset: bool = False) -> dict:
+    """Rare-branch counts of the orbit phase on the current device since the
+    last reset (cmcg_orbit_counters): probes decided in FP64, probes
+    evaluated in double-double, apsides found by the root finder."""
+    out = (C.c_ulonglong * 4)()
+    rc = lib().cmcg_orbit_counters(out, int(reset))
+    if rc:
+        raise CmcError(rc, "cmcg_orbit_counters")
+    return {k: int(out[i]) for i, k in enumerate(ORBIT_COUNTERS)}
 
 
 def sign_stages(E, J, rj, mj, invN, rk, phik):

@@ -23,6 +23,14 @@ namespace cmcg {
 
 constexpr int BISECT_LIMIT = 80;
 
+// Counts of the orbit phase's rare branches over every launch on this device
+// since the last reset (cmcg_orbit_counters): table probes whose sign the
+// FP32 and float-float stages left to the FP64 stage, probes that went on to
+// double-double, and apsides outside their closed-form interval (the
+// find_root_vr fallback).  A file-scope array, so that the hot kernels carry
+// no extra pointer; the increments sit only on those branches.
+__device__ unsigned long long g_orbit_rare[CMCG_ORBIT_NCOUNTERS];
+
 struct OrbitCtx {
     const double *__restrict__ r, *__restrict__ phi, *__restrict__ inv_r;
     const float4 *__restrict__ rphif;
@@ -47,8 +55,10 @@ static __device__ __forceinline__ int fq_sign_at(const OrbitCtx &o, long long k,
     if (s) return s;
     s = fq_sign_ff(o.s, rp, ge);
     if (s) return s;
+    atomicAdd(&g_orbit_rare[CMCG_ORBIT_SIGN_F64], 1ull);
     s = fq_sign_f64(o.s, __ldg(o.inv_r + k), __ldg(o.phi + k), ge);
     if (s) return s;
+    atomicAdd(&g_orbit_rare[CMCG_ORBIT_SIGN_DD], 1ull);
     const double q = fq(o, k);
     return (q > 0.0) - (q < 0.0);
 }
@@ -149,6 +159,7 @@ static __device__ __forceinline__ double dvr2_in(const OrbitCtx &o, double x, lo
 // checks of cmc_nr.c:584-597.
 static __device__ double find_root_vr(const OrbitCtx &o, long long k, double prec, long long maxit, int *err)
 {
+    atomicAdd(&g_orbit_rare[CMCG_ORBIT_ROOT_VR], 1ull);
     bool ok = true;
     double lo = o.r[k], hi = o.r[k + 1];
     double flo = vr2_in(o, lo, k, &ok), fhi = vr2_in(o, hi, k, &ok);
@@ -1391,4 +1402,17 @@ extern "C" int cmcg_sign_stages(const double *E, const double *J, const double *
     cudaFree(d);
     cudaFree(dout);
     return rc;
+}
+
+extern "C" int cmcg_orbit_counters(unsigned long long out[CMCG_ORBIT_NCOUNTERS], int reset)
+{
+    using namespace cmcg;
+    if (!out) return CMCG_ERR_ARG;
+    if (cudaDeviceSynchronize() != cudaSuccess) return CMCG_ERR_CUDA;
+    if (cudaMemcpyFromSymbol(out, g_orbit_rare, sizeof(g_orbit_rare)) != cudaSuccess) return CMCG_ERR_CUDA;
+    if (reset) {
+        const unsigned long long zero[CMCG_ORBIT_NCOUNTERS] = {0, 0, 0, 0};
+        if (cudaMemcpyToSymbol(g_orbit_rare, zero, sizeof(zero)) != cudaSuccess) return CMCG_ERR_CUDA;
+    }
+    return CMCG_OK;
 }

@@ -194,6 +194,20 @@ double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, i
  * current device and waits for it. */
 int cmcg_sign_stages(const double *E, const double *J, const double *rj, const double *mj, double invN,
                      const double *rk, const double *phik, long n, int *out);
+/* Diagnostic: how often the orbit phase took its rare branches, summed over
+ * every launch on the current device since the last reset (all contexts):
+ *   out[CMCG_ORBIT_SIGN_F64]  table probes of the apsis bisections
+ *                             (find_zero_Q, cmc_nr.c:316) whose sign the FP32
+ *                             and float-float stages left undecided;
+ *   out[CMCG_ORBIT_SIGN_DD]   of those, probes the FP64 stage also left
+ *                             undecided (evaluated in double-double);
+ *   out[CMCG_ORBIT_ROOT_VR]   apsides outside the closed form's interval,
+ *                             found by the root finder that stands in for
+ *                             GSL's Brent in find_root_vr (cmc_nr.c:500),
+ *                             which agrees with it to APSIDES_PRECISION.
+ * Waits for the device; reset != 0 zeroes the counts after reading them. */
+enum { CMCG_ORBIT_SIGN_F64 = 0, CMCG_ORBIT_SIGN_DD = 1, CMCG_ORBIT_ROOT_VR = 2, CMCG_ORBIT_NCOUNTERS = 4 };
+int cmcg_orbit_counters(unsigned long long out[CMCG_ORBIT_NCOUNTERS], int reset);
 
 /* ------------------------------------------------- learned proposal ---
  * An optional proposal for the orbit sampler's rejection loop
@@ -349,14 +363,18 @@ long cmcg_format_lagrad_header(const double *mass_pc, int n_pc, char *buf, long 
  *   d_r      device pointer, n radii (escapers at SF_INFINITY = 1e10 sort last)
  *   d_perm   device pointer, n outputs: 0-based input position of the i-th
  *            smallest radius (ties keep input order)
- *   n_bound  optional host pointer: count of radii below SF_INFINITY (the call
- *            then waits for the sort to finish)
+ *   n_bound  optional host pointer: count of radii below SF_INFINITY.  With
+ *            it the call waits for the sort to finish and also returns any
+ *            error the sort kernels recorded on the device; without it the
+ *            call only queues the work on `stream` and reports host-side
+ *            errors alone
  *   stream   a cudaStream_t, or NULL for the default stream
- * n may not exceed CMCG_NOALLOC_MAX_STARS (CMCG_ERR_CAPACITY otherwise).  The
- * first call on each device looks up the array's device address and must come
- * before any stream capture; every GPU that loads the library holds the
- * array (about 34 MB) until the process exits.  All calls share it, so calls
- * that overlap on the GPU race. */
+ * n may not exceed CMCG_NOALLOC_MAX_STARS (CMCG_ERR_CAPACITY otherwise).  Each
+ * call looks up the array's device address on the current device; the first
+ * call on a device also loads the module there and must come before any
+ * stream capture.  Every GPU that loads the library holds the array (about
+ * 34 MB) until the process exits.  All calls share it, so calls that overlap
+ * on the GPU race. */
 #define CMCG_NOALLOC_MAX_STARS (1L << 20)
 int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_perm, long *n_bound, void *stream);
 

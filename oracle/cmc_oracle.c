@@ -54,6 +54,7 @@ struct ocmc_state {
     double Etot, KE, PE, Etot_ini;
     long tcount;
     long Nrel, Nrelbeta[4];
+    long n_root_vr; /* find_root_vr calls: apsides outside the closed form's interval */
     double qaverelbeta[4], maverelbeta[4], raverelbeta[4];
     uint32_t taus[4];
     int err;
@@ -640,6 +641,7 @@ static double vr2_in_interval(ocmc_state *s, double r, long index, long k, doubl
 /* find_root_vr, cmc_nr.c:500-603 */
 static double find_root_vr(ocmc_state *s, long index, long k, double E, double J)
 {
+    s->n_root_vr++;
     const double prec = s->P.apsides_precision, conv = s->P.apsides_convergence;
     int ok = 1, not_converged = 1;
     long iter = s->P.apsides_max_iter;
@@ -1269,7 +1271,7 @@ double ocmc_get_scalar(const ocmc_state *s, const char *name)
     if (!strcmp(name, #n)) return (double)s->n;
     S(N_STAR) S(N_MAX) S(N_MAX_NEW) S(Mtotal) S(Rtidal) S(orbit_r) S(madhoc) S(cenma_m) S(Dt) S(Prev_Dt)
     S(TotalTime) S(max_r) S(TidalMassLoss) S(OldTidalMassLoss) S(TidalMassLoss_old) S(Eescaped) S(Jescaped)
-    S(Etidal) S(Eoops) S(Etot) S(KE) S(PE) S(Etot_ini) S(tcount) S(Nrel) S(sigma_n)
+    S(Etidal) S(Eoops) S(Etot) S(KE) S(PE) S(Etot_ini) S(tcount) S(Nrel) S(sigma_n) S(n_root_vr)
 #undef S
     if (!strcmp(name, "Nrelbeta0")) return (double)s->Nrelbeta[0];
     if (!strcmp(name, "Nrelbeta1")) return (double)s->Nrelbeta[1];

@@ -1,0 +1,180 @@
+"""Phase-by-phase parity at the benchmark configurations' sizes.
+
+The oracle (cmc_oracle.c, bit-identical to the reference's own compiled step,
+tests/test_cpu_refpin.py) and the sm_103a kernels step the same model:
+  * Plummer, N = 1e5 equal masses (the CPU-runnable configuration);
+  * King W0 = 6 with Kroupa masses, N = 1e6 (the benchmark's configuration);
+  * King W0 = 7 with Kroupa masses and 10% composite binaries, N = 1e6 (the
+    mixed-precision configuration's model at a tenth of its N).
+At these sizes the potential replay crosses more binades, the radius index
+has up to 2^16 buckets and the FP32 sign table outgrows L2.  Each phase starts
+from the oracle's state; the bits must agree where the arithmetic is the
+reference's sequence of IEEE operations, the stated tolerances elsewhere.
+The rare branches of the orbit phase (sign probes left to FP64 or
+double-double, apsides from the root finder) are counted and printed."""
+import numpy as np
+import pytest
+
+import cmcgpu
+from parity_util import TOL_ORBIT, TOL_PHI, TOL_SIGMA, TOL_SUM, make_pair, max_rel, rel_err, sync_state
+
+pytestmark = pytest.mark.gpu
+
+CONFIGS = [
+    pytest.param(dict(model=cmcgpu.PLUMMER, N=100_000, imf=0, w0=6.0, bf=0.0), id="plummer-1e5"),
+    pytest.param(dict(model=cmcgpu.KING, N=1_000_000, imf=1, w0=6.0, bf=0.0), id="king6-kroupa-1e6"),
+    pytest.param(dict(model=cmcgpu.KING, N=1_000_000, imf=1, w0=7.0, bf=0.1), id="king7-binaries-1e6"),
+]
+
+
+def _pair(cfg, seed):
+    import oracle
+
+    ic = cmcgpu.generate(cfg["model"], cfg["N"], seed=seed, w0=cfg["w0"], imf=cfg["imf"],
+                         binary_fraction=cfg["bf"])
+    op = oracle.default_params(orbit_r=ic["rtid"], seed=seed + 1)
+    gp = cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed + 1)
+    o = oracle.Oracle(ic, op)
+    g = cmcgpu.Context([cfg["N"]], gp)
+    g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    return ic, o, g
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_phase_by_phase_at_benchmark_size(gpulib, orc, cfg):
+    ic, o, g = _pair(cfg, seed=777 + cfg["N"] % 1000 + int(10 * cfg["bf"]))
+    N = cfg["N"]
+    o.initialize()
+    g.initialize()
+    g.check_device("initialize")
+    # potential_calculate: the exact replay of the three recurrences
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
+    assert g.scalar("Mtotal") == o.scalar("Mtotal")
+    assert g.scalar("phi_fallback") == 0
+    nsp = [int(g.scalar(f"phi_nsp{c}")) for c in (1, 2, 3)]
+    assert max_rel(g.get("E"), o.get("E")) <= TOL_PHI
+    # time step and relaxation
+    sync_state(o, g, star=[("E", "E"), ("J", "J")])
+    o.begin_step()
+    g.begin_step()
+    o.calc_timestep()
+    g.calc_timestep()
+    assert g.scalar("Dt") == o.scalar("Dt")
+    dt = o.scalar("Dt")
+    o.dynamics_apply(dt)
+    g.dynamics_apply(dt)
+    g.check_device("dynamics_apply")
+    assert np.array_equal(g.get("Y"), o.get("Y"))
+    vro, vto = o.get("vr"), o.get("vt")
+    speed = np.sqrt(vro * vro + vto * vto)
+    assert np.max(np.abs(g.get("vr_rel") - vro) / speed) <= TOL_PHI
+    assert np.max(np.abs(g.get("vt_rel") - vto) / speed) <= TOL_PHI
+    assert max_rel(g.get("E"), o.get("E")) <= TOL_PHI
+    assert max_rel(g.get("J"), o.get("J")) <= TOL_PHI
+    n = o.nstars()
+    assert max_rel(g.get("sigma")[1:n + 1], o.get("sigma")[1:n + 1]) <= TOL_SIGMA
+    # new orbits from the oracle's relaxed state
+    o.set_scalar("Prev_Dt", dt)
+    o.energy_conservation1()
+    sync_state(o, g, star=[("vr", "vr_rel"), ("vt", "vt_rel"), ("E", "E"), ("J", "J")],
+               scalars=("Rtidal", "Mtotal"))
+    roots_o = o.scalar("n_root_vr")
+    o.new_orbits_calculate()
+    o.energy_conservation2()
+    roots_o = o.scalar("n_root_vr") - roots_o
+    cmcgpu.orbit_counters(reset=True)
+    g.new_orbits_calculate()
+    g.check_device("new_orbits_calculate")
+    rare = cmcgpu.orbit_counters(reset=True)
+    assert rare["root_vr"] == roots_o
+    rn_o, rn_g = o.get("rnew"), g.get("rnew")
+    assert np.array_equal(rn_g == 1e10, rn_o == 1e10)
+    if roots_o == 0:
+        # every apsis from the closed form: the reference's bits
+        for k in ("rnew", "vrnew", "vtnew"):
+            assert np.array_equal(g.get(k), o.get(k)), k
+    else:
+        keep = rn_o != 1e10
+        for k in ("rnew", "vrnew", "vtnew"):
+            assert max_rel(g.get(k)[keep], o.get(k)[keep]) <= TOL_ORBIT, k
+    sampled = (rn_o != 1e10) & (o.get("r_apo") > 0)
+    assert np.array_equal(g.get("X")[sampled], o.get("X")[sampled])
+    assert max_rel(g.get("r_peri")[sampled], o.get("r_peri")[sampled]) <= (0 if roots_o == 0 else TOL_ORBIT)
+    assert max_rel(g.get("r_apo")[sampled], o.get("r_apo")[sampled]) <= (0 if roots_o == 0 else TOL_ORBIT)
+    # the tail: stripping, sort, potential, set_velocities3, energies
+    sync_state(o, g, star=[("rnew", "rnew"), ("vrnew", "vrnew"), ("vtnew", "vtnew"), ("E", "E"), ("J", "J"),
+                           ("r_apo", "r_apo")],
+               scalars=("TidalMassLoss", "OldTidalMassLoss", "Mtotal"))
+    vrold, vtold = o.get("vrold"), o.get("vtold")
+    g.set("ec_pre", (vtold * vtold + vrold * vrold) + 1.0 * (o.get("Uoldrold") - o.get("Uoldrnew")))
+    o.tidally_strip_stars()
+    g.tidally_strip_stars()
+    g.check_device("tidally_strip_stars")
+    assert np.array_equal(g.get("rnew") == 1e10, o.get("rnew") == 1e10)
+    o.compute_intermediate_energy()
+    o.qsorts_new()
+    g.qsorts_new()
+    g.check_device("qsorts_new")
+    assert g.nstars() == o.nstars()
+    assert np.array_equal(g.ids(), o.ids())
+    for k in ("r", "m", "vr", "vt", "rOld"):
+        assert np.array_equal(g.get(k), o.get(k)), k
+    o.calc_potential()
+    g.calc_potential()
+    g.check_device("calc_potential")
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
+    assert g.scalar("phi_fallback") == 0
+    o.energy_conservation3()
+    g.energy_conservation3()
+    g.check_device("energy_conservation3")
+    assert max_rel(g.get("vr"), o.get("vr")) <= TOL_PHI
+    assert max_rel(g.get("vt"), o.get("vt")) <= TOL_PHI
+    o.compute_energy()
+    sync_state(o, g, scalars=("Eescaped", "Jescaped", "Etidal"))
+    for s in ("Eescaped_old", "Jescaped_old", "Etidal_old"):
+        g.set_scalar(s, 0.0)
+    g.compute_energy()
+    assert max_rel(g.get("E"), o.get("E")) <= TOL_PHI
+    assert max_rel(g.get("J"), o.get("J")) <= TOL_PHI
+    assert max_rel(g.scalar("Etot"), o.scalar("Etot")) <= TOL_SUM
+    print(f"\n[{N} stars] potential sequential points {nsp}; orbit probes decided in FP64 "
+          f"{rare['sign_f64']}, in double-double {rare['sign_dd']}; apsides from the root finder "
+          f"{rare['root_vr']} (oracle {int(roots_o)})")
+    g.close()
+    o.close()
+
+
+def test_ten_free_running_steps_plummer_1e5(gpulib, orc):
+    """The CPU-runnable configuration's ten steps without state injection,
+    compared star by star (by id) and by the oracle's energy change.
+
+    The trajectories part in the last bits after the first relaxation: the
+    deflection angles go through libm's sin/cos in the oracle and CUDA's on
+    the GPU.  Most stars then stay within a small relative drift of the
+    oracle's radius.  A few take a different rejection trial -- an ulp of E
+    moves a trial across the acceptance test -- and land at an unrelated
+    radius; one such star also shifts the sorted position of every star it
+    passes, so positions are not compared.  The bounds hold the drift of the
+    bulk, the share of stars whose trial changed, and the energy change."""
+    cfg = dict(model=cmcgpu.PLUMMER, N=100_000, imf=0, w0=6.0, bf=0.0)
+    ic, o, g = _pair(cfg, seed=2024)
+    o.initialize()
+    g.initialize()
+    e0o, e0g = o.scalar("Etot"), g.scalar("Etot")
+    for step in range(10):
+        o.step()
+        g.step()
+        g.check_device(f"step {step}")
+        assert g.nstars() == o.nstars()
+        ids_g, ids_o = g.ids(), o.ids()
+        assert np.array_equal(np.sort(ids_g), np.sort(ids_o)), step  # the same stars kept
+        err = rel_err(g.get("r")[np.argsort(ids_g)], o.get("r")[np.argsort(ids_o)])
+        q50, q90, far = np.quantile(err, 0.5), np.quantile(err, 0.9), float(np.mean(err > 1e-3))
+        de_o = o.scalar("Etot") - e0o
+        de_g = g.scalar("Etot") - e0g
+        print(f"step {step}: r rel. error median {q50:.2e}, 90% {q90:.2e}, share beyond 1e-3 {far:.2e}; "
+              f"energy change {de_g:.6e} (oracle {de_o:.6e})")
+        assert q50 <= 1e-9 and q90 <= 1e-6 and far <= 0.02, (step, q50, q90, far)
+        assert abs(de_g - de_o) <= 1e-7 * abs(e0o) + 0.05 * abs(de_o), (step, de_g, de_o)
+    g.close()
+    o.close()

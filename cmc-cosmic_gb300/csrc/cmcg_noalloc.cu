@@ -11,13 +11,18 @@
 //
 // The array is held by every GPU that loads the library until the process
 // exits (about 34 MB for the 2^20-star maximum).  Its device address is looked
-// up once per device, on the first call made with that device current; make
-// that first call before any stream capture.  All calls share the one array
-// and it keeps the previous call's contents: the parts that must start from
-// zero are cleared on every call, and calls that overlap on the GPU (on
-// different streams, or from different host threads) race on it.
+// up on every call, with the caller's device current; the first call on a
+// device also loads the module there, so make that first call before any
+// stream capture.  All calls share the one array and it keeps the previous
+// call's contents: the parts that must start from zero are cleared on every
+// call, and calls that overlap on the GPU (on different streams, or from
+// different host threads) race on it.
+//
+// Errors the sort kernels record on the device (a bounded wait that gave up,
+// inconsistent counts) are read back only by the synchronizing form of the
+// call (n_bound given); the asynchronous form returns after queueing its work
+// and reports only what the host can see.
 #include <cstdio>
-#include <mutex>
 
 #include "cmcg_kernels.cuh"
 #include "cmcgpu.h"
@@ -87,9 +92,6 @@ __global__ void k_na_perm(unsigned char *base, long long n, unsigned int *perm)
 
 using namespace cmcg;
 
-static std::mutex g_na_mutex;
-static unsigned char *g_na_addr[64];  // device address of the scratch array, per device ordinal
-
 extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_perm, long *n_bound, void *stream)
 {
     if (!d_r || !d_perm || n < 1) return CMCG_ERR_ARG;
@@ -97,22 +99,15 @@ extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_pe
         fprintf(stderr, "cmcg_sort_radii_noalloc: %ld stars exceed the fixed maximum of %lld\n", n, NA_MAX);
         return CMCG_ERR_CAPACITY;
     }
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CMCG_ERR_CUDA;
-    unsigned char *base;
-    {
-        std::lock_guard<std::mutex> lock(g_na_mutex);
-        if (!g_na_addr[dev]) {
-            void *p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p) {
-                fprintf(stderr, "cmcg_sort_radii_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
-                return CMCG_ERR_CUDA;
-            }
-            g_na_addr[dev] = (unsigned char *)p;
-        }
-        base = g_na_addr[dev];
+    // the array's address on the current device, looked up on every call: a
+    // cached address would go stale if the device's context were reset
+    void *addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess || !addr) {
+        fprintf(stderr, "cmcg_sort_radii_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+        return CMCG_ERR_CUDA;
     }
+    unsigned char *base = (unsigned char *)addr;
     cudaStream_t s = (cudaStream_t)stream;
     const int ntiles = (int)((n + SORT_T - 1) / SORT_T);
     // radii into slots 1..n (the sort kernels read the reference's 1-based layout)
@@ -153,12 +148,16 @@ extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_pe
     k_na_perm<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(base, n, d_perm);
     if (cudaGetLastError() != cudaSuccess) return CMCG_ERR_CUDA;
     if (n_bound) {
-        long long nb = 0;
-        const Scalars *sc = (const Scalars *)(base + NA_SC);
-        if (cudaMemcpyAsync(&nb, &sc->n_bound, sizeof(nb), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        // the synchronizing form: the kept count and the kernels' status word
+        Scalars sc;
+        if (cudaMemcpyAsync(&sc, base + NA_SC, sizeof(sc), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return CMCG_ERR_CUDA;
-        *n_bound = (long)nb;
+        if (sc.err) {
+            fprintf(stderr, "cmcg_sort_radii_noalloc: device error %d at %lld\n", sc.err, sc.err_index);
+            return sc.err;
+        }
+        *n_bound = (long)sc.n_bound;
     }
     return CMCG_OK;
 }

@@ -82,3 +82,27 @@ def test_sort_runs_sharing_the_sorted_prefix(gpulib):
 def test_noalloc_rejects_oversize(gpulib):
     rc = gpulib.lib().cmcg_sort_radii_noalloc(C.c_void_p(16), (1 << 20) + 1, C.c_void_p(16), None, None)
     assert rc == -3  # CMCG_ERR_CAPACITY, before any device work
+
+
+def test_noalloc_asynchronous_form_on_a_side_stream(gpulib):
+    """Without n_bound the call only queues its work on the caller's stream;
+    once that stream is synchronized the permutation is the regular sort's."""
+    import torch
+
+    rng = np.random.default_rng(99)
+    n = 40000
+    radii = np.exp(rng.uniform(-6.0, 5.0, size=n))
+    radii[rng.random(n) < 0.02] = 1e10
+    want = _context_order(gpulib, radii)
+    side = torch.cuda.Stream(device="cuda:0")
+    with torch.cuda.stream(side):
+        d_r = torch.tensor(radii, dtype=torch.float64, device="cuda:0")
+        d_perm = torch.full((n,), -1, dtype=torch.int32, device="cuda:0")
+    side.synchronize()
+    rc = gpulib.lib().cmcg_sort_radii_noalloc(C.c_void_p(d_r.data_ptr()), n, C.c_void_p(d_perm.data_ptr()), None,
+                                             C.c_void_p(side.cuda_stream))
+    assert rc == 0
+    side.synchronize()
+    got = d_perm.cpu().numpy().astype(np.int64)
+    assert np.array_equal(got[:len(want)], want)
+    assert np.all(radii[got[len(want):]] == 1e10)

@@ -10,10 +10,16 @@ Henon step of every star; one star-update is one star carried through it.
 The state (about 250 bytes/star, 250 MB) is larger than the 129 MB L2, so
 every step streams from HBM; no explicit L2 flush is needed.
 
+The same line carries the N = 1e7 configuration (King W0 = 7, 10% composite
+binaries, FP32 relaxation kinematics) and the 128-cluster ensemble as
+sub-objects, each with its own throughput, roofline, energy drift and the
+learned proposal's numbers.
+
 --impl reference times the reference's algorithm on the host cores instead:
-the CPU restatement in oracle/ (the reference itself needs MPI, GSL and HDF5,
-which this image lacks), with the reference's own taus113 generator, one
-process per core on bounded samples of the same model.
+the oracle's C restatement (bit-identical to the reference's own step compiled
+against single-rank shims; the full reference needs MPI, GSL and HDF5, which
+this image lacks), with the reference's own taus113 generator, one process per
+core, each stepping the same model the GPU arm steps.
 
 Under torchrun each rank steps its own replica (replicas only: the path has
 no data exchange between independent clusters) and value is the sum over
@@ -41,7 +47,7 @@ ALG_BYTES = {"sort": 116, "potential": 24, "relax": 72, "orbit": 80, "ec3": 72, 
 # the proposal network's algorithmic FLOPs per star: 2 (8*64 + 64*64 + 64*33)
 MLP_FLOPS_PER_STAR = 2 * (8 * 64 + 64 * 64 + 64 * 33)
 # DRAM bytes per star of one launch, dram__bytes_read.sum + dram__bytes_write.sum
-# from one ncu capture (summaries under profiles/), scaled by stars: k_orbit
+# from one ncu capture, scaled by stars: k_orbit
 # 961.2 MB over 1,912,424 stars (King W0=6 + Kroupa, N=2e6), k_relax64 57.5 MB
 # over 962,913 stars (the same model at N=1e6)
 NCU_TRAFFIC_PER_STAR = {"orbit": 961.2e6 / 1912424, "relax": 57.5e6 / 962913}
@@ -51,7 +57,7 @@ NCU_FP64_PIPE_ACTIVE = {"orbit": 0.685, "relax": 0.703}
 # FP64 thread-operations per star of each kernel family (ncu
 # smsp__sass_thread_inst_executed_op_fp64_pred_on.sum over the stars of one
 # step, King W0=6 + Kroupa, N = 1e6), and the measured FP64 FMA rate of this
-# GPU (bench.py --probe-rates: 1.01 TFLOP/s = 5.05e11 DFMA/s)
+# GPU (a dependent-chain DFMA probe: 1.01 TFLOP/s = 5.05e11 DFMA/s)
 NCU_FP64_OPS_PER_STAR = {"orbit": 343.2, "relax": 181.1, "potential": 61.4, "ec3": 45.0, "energy": 11.8,
                          "timestep": 12.1, "tidal": 2.1}
 FP64_PEAK_OPS = 5.05e11
@@ -164,7 +170,8 @@ def allreduce_sum(dist, x: float) -> float:
 
 
 # The named synthetic configurations (seeded generators; no dataset exists for
-# them).  king1e6 is the headline; the others are measured on request.
+# them).  king1e6 is the headline; king1e7bin and ensemble128 are measured
+# beside it in the same line (EXTRA_CONFIGS); the others on request.
 CONFIGS = {
     "plummer1e5": dict(model="plummer", N=100_000, imf=0, bf=0.0, fp32=0,
                        desc="Plummer, equal masses, N=1e5, plain FP64 Henon step"),
@@ -179,6 +186,10 @@ CONFIGS = {
                        desc="King W0=7, Kroupa IMF, N=1e7, 10% composite binaries, FP32 relaxation "
                             "kinematics with FP64 energies, FP64 potential and root finds"),
 }
+
+
+EXTRA_CONFIGS = ("king1e7bin", "ensemble128")
+MODEL_SEED = 20240607  # the model every arm builds (plus the rank under torchrun)
 
 
 def make_model(N: int, seed: int, cfg=None):
@@ -199,10 +210,10 @@ def make_clusters(cfg, N, rank):
     import cmcgpu
 
     if cfg["model"] != "ensemble":
-        return [(N, make_model(N, 20240607 + rank, cfg), cmcgpu.derive_seed(777, rank))]
+        return [(N, make_model(N, MODEL_SEED + rank, cfg), cmcgpu.derive_seed(777, rank))]
     from concurrent.futures import ThreadPoolExecutor
 
-    master = 20240607 + rank
+    master = MODEL_SEED + rank
     rng = np.random.default_rng(master)
     Ns = np.exp(rng.uniform(np.log(cfg["lo"]), np.log(cfg["hi"]), cfg["n"])).astype(int)
     w0s = rng.choice([3.0, 5.0, 7.0, 9.0], cfg["n"])
@@ -219,20 +230,33 @@ def make_clusters(cfg, N, rank):
         return list(ex.map(one, range(cfg["n"])))
 
 
+def workload_config(cfg_name: str, N: int):
+    """The `config` object both arms print: what is stepped, nothing about how."""
+    cfg = CONFIGS[cfg_name]
+    n = N or cfg.get("N")
+    state = (n or 28_000_000) * 250
+    return {"workload": cfg["desc"], "name": cfg_name, "N": n if cfg["model"] != "ensemble" else None,
+            "model_seed": MODEL_SEED,
+            "l2": "state ~250 B/star exceeds the 129 MB L2: no flush needed" if state > 129e6
+                  else "L2 holds the state: steps read warm data"}
+
+
 # ------------------------------------------------------------- CPU legs ---
 def _ref_worker(args):
-    """One host core: the oracle (reference algorithm, taus113 draws) stepping a
-    bounded sample of the workload's model; returns (stars*steps, seconds)."""
-    n, steps, warmup, seed, cfg_name = args
+    """One host core: the oracle (reference algorithm, taus113 draws) stepping
+    the workload's model (the ensemble: its largest King member's kind);
+    returns (stars*steps, seconds)."""
+    n, steps, warmup, draw_seed, cfg_name = args
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     sys.path.insert(0, os.path.join(ROOT, "cmc-cosmic_gb300"))
     import oracle
 
     cfg = CONFIGS[cfg_name]
-    if cfg["model"] == "ensemble":  # a sample cluster of the ensemble's kind
+    if cfg["model"] == "ensemble":
         cfg = dict(CONFIGS["king1e6"], w0=5.0)
-    ic = make_model(n, seed, cfg)
-    o = oracle.Oracle(ic, oracle.default_params(orbit_r=ic["rtid"], seed=seed, draw_mode=oracle.DRAW_TAUS113))
+    ic = make_model(n, MODEL_SEED, cfg)
+    o = oracle.Oracle(ic, oracle.default_params(orbit_r=ic["rtid"], seed=draw_seed,
+                                                draw_mode=oracle.DRAW_TAUS113))
     o.initialize()
     for _ in range(warmup):
         o.step()
@@ -245,6 +269,8 @@ def _ref_worker(args):
 
 
 def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int, cfg_name: str = "king1e6"):
+    """The oracle on `procs` host processes (spawned: no GPU state is forked),
+    each stepping the workload's model; star-updates/s over the slowest."""
     import multiprocessing as mp
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -259,7 +285,6 @@ def cpu_baseline(n_sample: int, steps: int, warmup: int, procs: int, cfg_name: s
     return updates / secs, secs
 
 
-# ------------------------------------------------------------ GPU leg ----
 # ------------------------------------------------------ learned proposal ---
 def train_proposal(a):
     """The orbit sampler's proposal network, trained as the learned
@@ -303,15 +328,13 @@ def train_proposal(a):
                "train_tflops": 3 * MLP_FLOPS_PER_STAR * 8192 * a.learn_steps / max(t2 - t1, 1e-9) / 1e12}
 
 
-def learned_leg(a, cfg, clusters, params, ctx, timed, stars):
+def learned_leg(a, clusters, params, ctx, timed, stars, w):
     """Learned-proposal step on the same context (after the plain legs), and
     one step from a common state with each sampler for the distribution test."""
-    import numpy as np
     from scipy.stats import ks_2samp
 
     import cmcgpu
 
-    w, info = train_proposal(a)
     ctx.mlp_set_params(w)
     ctx.set_learned(cmcgpu.LEARN_ON, a.kappa)
     tuned = ctx.autotune(2) if not a.no_autotune else "off"
@@ -363,24 +386,58 @@ def learned_leg(a, cfg, clusters, params, ctx, timed, stars):
         "trials_per_star": trials, "plain_trials_per_star": float(nta.mean()),
         "failed_frac": stb["failed"] / max(stb["stars"], 1),
         "ks_p_X": float(ks_2samp(Xa, Xb).pvalue), "ks_samples": [int(len(Xa)), int(len(Xb))],
+        "ks_cluster": "cluster 0" if ncl > 1 else "the cluster",
         "last_step_stats": st,
         "kernels": {k: {"ms_per_step": round(v[0] / a.steps, 4), "launches": v[1]} for k, v in fam.items() if v[1]},
         "mlp_roofline": {"bound": "tensor", "kernel": "k_mlp_infer", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_kind + " (bf16 sustained)",
                          "flops_per_star": MLP_FLOPS_PER_STAR, "ms_per_launch": mlp_ms},
-        "train": info,
     }
 
 
-def run_ours(a, rank, ws, dist):
+def fp32_error_leg(cluster, params):
+    """FP32 relaxation kinematics against FP64: one relaxation from the same
+    state with each, per-output errors (velocities against the star's speed)."""
     import numpy as np
+
+    import cmcgpu
+
+    n, ic, seed = cluster
+    out = {}
+    for fp32 in (0, 1):
+        p = cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed, relax_fp32=fp32)
+        g = cmcgpu.Context([n], [p])
+        g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+        g.initialize()
+        g.begin_step()
+        g.calc_timestep()
+        g.dynamics_apply(g.scalar("Dt"))
+        g.check_device("fp32 leg")
+        out[fp32] = {k: g.get(k) for k in ("vr_rel", "vt_rel", "E", "J")}
+        out[fp32]["r"] = g.get("star_r")[1:len(out[fp32]["E"]) + 1]
+        g.close()
+    a, b = out[0], out[1]
+    speed = np.sqrt(a["vr_rel"] ** 2 + a["vt_rel"] ** 2)
+    return {"what": "one relaxation from the same state, FP32 kinematics against FP64, max over stars: "
+                    "velocities against the star's speed, E relative, J against r times the speed",
+            "vr_over_speed": float(np.max(np.abs(b["vr_rel"] - a["vr_rel"]) / speed)),
+            "vt_over_speed": float(np.max(np.abs(b["vt_rel"] - a["vt_rel"]) / speed)),
+            "E_rel": float(np.max(np.abs(b["E"] - a["E"]) / np.abs(a["E"]))),
+            "J_over_r_speed": float(np.max(np.abs(b["J"] - a["J"]) / (a["r"] * speed)))}
+
+
+# ------------------------------------------------------------ GPU leg ----
+def measure(a, cfg_name, N, rank, ws, dist, weights=None, sub=False):
+    """One configuration on this rank's GPU: the device-resident step replayed
+    from the CUDA graph (value), the kernel families and the roofline of the
+    top one, the public host-array API end to end (e2e), the energy drift, and
+    with `weights` the learned proposal's step."""
     import torch
 
     import cmcgpu
 
-    cmcgpu.build()
-    cfg = CONFIGS[a.config]
-    N = a.N or cfg.get("N", 0)
+    cfg = CONFIGS[cfg_name]
+    N = N or cfg.get("N", 0)
     clusters = make_clusters(cfg, N, rank)
     params = [cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed, relax_fp32=cfg["fp32"]) for _, ic, seed in clusters]
     ctx = cmcgpu.Context([n for n, _, _ in clusters], params)
@@ -414,7 +471,7 @@ def run_ours(a, rank, ws, dist):
     ctx.check_device("warmup")
     n_start = stars()
 
-    # ---- headline: device-resident steps replayed from the CUDA graph
+    # ---- device-resident steps replayed from the CUDA graph
     e_start = [ctx.scalar("Etot", c) for c in range(ncl)]
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
@@ -442,10 +499,11 @@ def run_ours(a, rank, ws, dist):
     peak, peak_kind = measured_peak()
     achieved = ALG_BYTES[top] * n_prof / (ms_top / n_top * 1e-3) / 1e9
     per_family = {k: {"ms_per_step": round(v[0] / a.steps, 4), "launches": v[1]} for k, v in fam.items() if v[1]}
+    step_bytes = sum(ALG_BYTES.values()) - ALG_BYTES["ec3"] - ALG_BYTES["energy"] - ALG_BYTES["timestep"] \
+        - ALG_BYTES["tidal"]  # the four hot-path kernels' 292 B per star-update
 
-    # ---- end to end through the public API: host star arrays in pinned memory,
-    # copied in before and out after every step
-    # pinned host arrays, one set per cluster: the host owns the star state
+    # ---- end to end through the public API: host star arrays in pinned
+    # memory, copied in before and out after every step (cmcg_step_host)
     def pinned(n):
         b = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k in ("r", "m", "vr", "vt", "E", "J")}
         b["id"] = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy()
@@ -455,10 +513,8 @@ def run_ours(a, rank, ws, dist):
     for c, (n, _, _) in enumerate(clusters):
         b = pinned(n + 16)
         host.append((b, ctx.get_stars(c, b)))
-    # cmcg_step_host: the step's two halves replayed from graphs, the read-back of
-    # the sorted r, m, id overlapping the second half; one warm-up call captures them
     ctx.use_graph(True)
-    ns = ctx.step_host([(n, b) for b, n in host], [b for b, _ in host])
+    ns = ctx.step_host([(n, b) for b, n in host], [b for b, _ in host])  # captures the part graphs
     host = [(b, n) for (b, _), n in zip(host, ns)]
     h2d = d2h = 0
     e2e_updates = 0
@@ -475,27 +531,15 @@ def run_ours(a, rank, ws, dist):
     ctx.check_device("e2e steps")
     e2e_value = allreduce_sum(dist, float(e2e_updates)) / allreduce_max(dist, e2e_dt)
 
-    model_txt = {"plummer": "Plummer model", "king": f"King W0={cfg.get('w0')} model",
-                 "ensemble": "Plummer and King models"}[cfg["model"]]
     out = {
-        "metric": METRIC,
         "value": value,
         "unit": UNIT,
-        "n_gpus": ws,
         "steps": a.steps,
         "warmup": a.warmup,
         "ms_per_step": ms_max / a.steps,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f64" if not cfg["fp32"] else "f64 (f32 relaxation kinematics)",
-        "data": f"synthetic (seeded {model_txt}, {'Kroupa 2001 IMF' if cfg['imf'] else 'equal masses'}; no dataset)",
-        "config": {"workload": cfg["desc"], "name": a.config, "N": N if ncl == 1 else None, "clusters": ncl,
-                   "stars_at_start": n_start, "parallelism": f"replicas x{ws}",
-                   "timing": "CUDA events on the library's stream; whole step replayed from a CUDA graph",
-                   "autotune": tuned,
-                   "l2": "state ~250 B/star exceeds the 129 MB L2 at this size: no flush needed"
-                         if n_start * 250 > 129e6 else "L2 holds the state: steps read warm data"},
+        "stars_at_start": n_start,
+        "clusters": ncl,
+        "autotune": tuned,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // a.steps,
                 "d2h_bytes_per_step": d2h // a.steps},
         "gpu_launches": launches,
@@ -504,6 +548,7 @@ def run_ours(a, rank, ws, dist):
                      "traffic": (NCU_TRAFFIC_PER_STAR[top] * n_prof if top in NCU_TRAFFIC_PER_STAR else None),
                      "fp64_pipe_active": NCU_FP64_PIPE_ACTIVE.get(top),
                      "alg_bytes_per_star": ALG_BYTES[top], "ms_per_launch": ms_top / n_top,
+                     "step_frac": step_bytes * value / ws / 1e9 / peak,
                      "timed_in": "the profiled direct-launch pass"},
         "roofline_fp64": {"bound": "fp64 pipe", "kernel": top,
                           "achieved": NCU_FP64_OPS_PER_STAR.get(top, 0.0) * n_prof / (ms_top / n_top * 1e-3),
@@ -511,7 +556,7 @@ def run_ours(a, rank, ws, dist):
                           "frac": NCU_FP64_OPS_PER_STAR.get(top, 0.0) * n_prof / (ms_top / n_top * 1e-3)
                           / FP64_PEAK_OPS,
                           "ops_per_star": NCU_FP64_OPS_PER_STAR.get(top),
-                          "peak_source": "measured DFMA rate (profiles/fp64_rates.md)",
+                          "peak_source": "measured DFMA rate of this GPU (1.01 TFLOP/s)",
                           "step_frac": sum(NCU_FP64_OPS_PER_STAR.values()) * n_prof / (step_ms * 1e-3)
                           / FP64_PEAK_OPS},
         "energy": {"rel_drift_per_step": drift[0] if ncl == 1 else None,
@@ -522,12 +567,67 @@ def run_ours(a, rank, ws, dist):
         "profiled_ms_per_step": ms_prof / a.steps,
         "clocks": clk,
     }
-    if not a.no_learned and rank == 0 and ws == 1:
+    if weights is not None and rank == 0 and ws == 1:
         try:
-            out["learned"] = learned_leg(a, cfg, clusters, params, ctx, timed, stars)
-        except Exception as e:  # the headline stands without it
+            out["learned"] = learned_leg(a, clusters, params, ctx, timed, stars, weights)
+            out["learned"]["speedup_vs_plain"] = out["learned"]["value"] / value
+        except Exception as e:  # the plain numbers stand without it
             out["learned"] = {"error": repr(e)}
     ctx.close()
+    if cfg["fp32"] and rank == 0:
+        out["fp32_vs_fp64"] = fp32_error_leg(clusters[0], params)
+    return out
+
+
+def run_ours(a, rank, ws, dist):
+    import cmcgpu
+
+    cmcgpu.build()
+    weights, train_info = None, None
+    if not a.no_learned and rank == 0 and ws == 1:
+        try:
+            weights, train_info = train_proposal(a)
+        except Exception as e:
+            train_info = {"error": repr(e)}
+    m = measure(a, a.config, a.N, rank, ws, dist, weights)
+    cfg = CONFIGS[a.config]
+    model_txt = {"plummer": "Plummer model", "king": f"King W0={cfg.get('w0')} model",
+                 "ensemble": "Plummer and King models"}[cfg["model"]]
+    out = {
+        "metric": METRIC,
+        "value": m["value"],
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": m["ms_per_step"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if not cfg["fp32"] else "f64 (f32 relaxation kinematics)",
+        "data": f"synthetic (seeded {model_txt}, {'Kroupa 2001 IMF' if cfg['imf'] else 'equal masses'}; no dataset)",
+        "config": workload_config(a.config, a.N),
+        "run": {"clusters": m["clusters"], "stars_at_start": m["stars_at_start"], "parallelism": f"replicas x{ws}",
+                "timing": "CUDA events on the library's stream; whole step replayed from a CUDA graph"},
+        "autotune": m["autotune"],
+        "e2e": m["e2e"],
+        "gpu_launches": m["gpu_launches"],
+    }
+    for k in ("roofline", "roofline_fp64", "energy", "kernels", "kernel_ms_per_step", "profiled_ms_per_step",
+              "clocks", "learned", "fp32_vs_fp64"):
+        if k in m:
+            out[k] = m[k]
+    if train_info is not None:
+        out.setdefault("learned", {})["train"] = train_info
+    if not a.no_extra and a.config == "king1e6" and not a.N and ws == 1:
+        out["configs"] = {}
+        for name in EXTRA_CONFIGS:
+            try:
+                sub = measure(a, name, 0, rank, ws, dist, weights)
+                sub["config"] = workload_config(name, 0)
+                out["configs"][name] = sub
+            except Exception as e:  # the headline stands without them
+                out["configs"][name] = {"error": repr(e)}
     return out
 
 
@@ -541,23 +641,17 @@ def main():
     ap.add_argument("--N", type=int, default=0, help="override the configuration's N (single-cluster configs)")
     ap.add_argument("--cpu-sample", type=int, default=1_000_000, help="stars per CPU-baseline process")
     ap.add_argument("--cpu-steps", type=int, default=2, help="timed oracle steps of the 1-core CPU baseline")
+    ap.add_argument("--cpu-warmup", type=int, default=1, help="untimed oracle steps before them")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip training the proposal network and timing the learned-proposal step")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="measure the headline configuration alone (not king1e7bin and ensemble128 beside it)")
     ap.add_argument("--kappa", type=float, default=1.2, help="envelope factor of the learned proposal")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch variants")
     ap.add_argument("--learn-records", type=int, default=20_000_000, help="plain-sampler records to train on")
     ap.add_argument("--learn-steps", type=int, default=2500, help="Adam steps of batch 8192")
-    ap.add_argument("--probe-rates", action="store_true",
-                    help="build and run the FP64/FP32/INT64 pipe-rate probe, then exit")
     a = ap.parse_args()
-    if a.probe_rates:
-        src = os.path.join(ROOT, "cmc-cosmic_gb300", "csrc", "probe_rates.cu")
-        exe = os.path.join(ROOT, "cmc-cosmic_gb300", "_build", "probe_rates")
-        os.makedirs(os.path.dirname(exe), exist_ok=True)
-        subprocess.check_call(["nvcc", "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-o", exe, src])
-        subprocess.check_call([exe])
-        return
     if a.warmup < 3:
         a.warmup = 3
     rank, ws, local, dist = dist_setup()
@@ -569,15 +663,19 @@ def main():
             return
         procs = min(os.cpu_count() or 1, 16)
         cfg = CONFIGS[a.config]
-        val, secs = cpu_baseline(a.cpu_sample, a.steps, a.warmup, procs, a.config)
+        n_sample = a.cpu_sample if cfg["model"] == "ensemble" else (a.N or cfg.get("N"))
+        n_sample = min(n_sample, a.cpu_sample)
+        val, secs = cpu_baseline(n_sample, a.steps, a.warmup, procs, a.config)
         out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
                "ms_per_step": secs / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "impl": "reference",
                "data": "synthetic (seeded cluster models of the configuration; no dataset)",
-               "config": {"workload": cfg["desc"], "name": a.config, "N": a.N or cfg.get("N")},
+               "config": workload_config(a.config, a.N),
                "cpu_baseline": {"value": val, "unit": UNIT, "cores": procs, "kind": "port",
-                                "sample": f"{procs} processes x {a.cpu_sample}-star clusters of the configuration's "
-                                          f"model, {a.steps} timed steps each (reference algorithm, taus113 draws)"},
+                                "sample": f"{procs} processes, each stepping a {n_sample}-star cluster of the "
+                                          f"configuration's model (model seed {MODEL_SEED}), {a.warmup} warm-up + "
+                                          f"{a.steps} timed steps (the oracle, bit-identical to the reference's "
+                                          f"compiled step; taus113 draws)"},
                "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         if dist is not None:
@@ -587,11 +685,14 @@ def main():
     out = run_ours(a, rank, ws, dist)
     if rank == 0:
         if not a.no_cpu_baseline and ws == 1:
-            val, secs = cpu_baseline(a.cpu_sample, a.cpu_steps, 0, 1, a.config)
+            cfg = CONFIGS[a.config]
+            n_sample = min(a.cpu_sample, a.N or cfg.get("N") or a.cpu_sample)
+            val, secs = cpu_baseline(n_sample, a.cpu_steps, a.cpu_warmup, 1, a.config)
             out["cpu_baseline"] = {"value": val, "unit": UNIT, "cores": 1, "kind": "port",
-                                   "sample": f"one {a.cpu_sample}-star cluster of the configuration's model, "
-                                             f"{a.cpu_steps} steps ({secs:.1f} s; reference algorithm with taus113 "
-                                             f"draws, 1 core)"}
+                                   "sample": f"one {n_sample}-star cluster of the configuration's model (model seed "
+                                             f"{MODEL_SEED}), {a.cpu_warmup} warm-up + {a.cpu_steps} timed steps "
+                                             f"({secs:.1f} s; the oracle, bit-identical to the reference's compiled "
+                                             f"step, taus113 draws, 1 core)"}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

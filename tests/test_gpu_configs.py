@@ -11,7 +11,8 @@ has up to 2^16 buckets and the FP32 sign table outgrows L2.  Each phase starts
 from the oracle's state; the bits must agree where the arithmetic is the
 reference's sequence of IEEE operations, the stated tolerances elsewhere.
 The rare branches of the orbit phase (sign probes left to FP64 or
-double-double, apsides from the root finder) are counted and printed."""
+double-double, apsides from the root finder) are counted and printed.  Ten
+free-running steps at N = 1e5 compare the energy bookkeeping of whole runs."""
 import numpy as np
 import pytest
 
@@ -144,19 +145,23 @@ def test_phase_by_phase_at_benchmark_size(gpulib, orc, cfg):
     o.close()
 
 
-def test_ten_free_running_steps_plummer_1e5(gpulib, orc):
-    """The CPU-runnable configuration's ten steps without state injection,
-    compared star by star (by id) and by the oracle's energy change.
+@pytest.mark.parametrize("model,imf", [(cmcgpu.PLUMMER, 0), (cmcgpu.KING, 1)], ids=["plummer-1e5", "king6-kroupa-1e5"])
+def test_ten_free_running_steps(gpulib, orc, model, imf):
+    """Ten whole steps at N = 1e5 without state injection, the GPU against the
+    oracle.
 
-    The trajectories part in the last bits after the first relaxation: the
-    deflection angles go through libm's sin/cos in the oracle and CUDA's on
-    the GPU.  Most stars then stay within a small relative drift of the
-    oracle's radius.  A few take a different rejection trial -- an ulp of E
-    moves a trial across the acceptance test -- and land at an unrelated
-    radius; one such star also shifts the sorted position of every star it
-    passes, so positions are not compared.  The bounds hold the drift of the
-    bulk, the share of stars whose trial changed, and the energy change."""
-    cfg = dict(model=cmcgpu.PLUMMER, N=100_000, imf=0, w0=6.0, bf=0.0)
+    The two runs part in the last bits at the first relaxation: the deflection
+    angles go through libm's sin/cos in the oracle and CUDA's on the GPU.  For
+    the first two steps the same stars stay in the same order, radii agree to
+    ~1e-10 (99th percentile, measured on the GB300: 6.8e-11 Plummer, 6.0e-11
+    King) and the energy change agrees to ~1e-14 of the total.  Then an ulp of
+    E moves some rejection trial across its acceptance test, that star lands
+    at an unrelated radius, and from there the runs are two realisations of
+    the same chaotic process: a star escapes in one and not the other by step
+    3 (Plummer) or 7 (King).  The energy bookkeeping must still agree: the
+    cumulative energy change of the two runs stays within a small fraction of
+    the total energy (measured after ten steps: 1.2e-6 Plummer, 2.1e-5 King)."""
+    cfg = dict(model=model, N=100_000, imf=imf, w0=6.0, bf=0.0)
     ic, o, g = _pair(cfg, seed=2024)
     o.initialize()
     g.initialize()
@@ -165,16 +170,17 @@ def test_ten_free_running_steps_plummer_1e5(gpulib, orc):
         o.step()
         g.step()
         g.check_device(f"step {step}")
-        assert g.nstars() == o.nstars()
-        ids_g, ids_o = g.ids(), o.ids()
-        assert np.array_equal(np.sort(ids_g), np.sort(ids_o)), step  # the same stars kept
-        err = rel_err(g.get("r")[np.argsort(ids_g)], o.get("r")[np.argsort(ids_o)])
-        q50, q90, far = np.quantile(err, 0.5), np.quantile(err, 0.9), float(np.mean(err > 1e-3))
         de_o = o.scalar("Etot") - e0o
         de_g = g.scalar("Etot") - e0g
-        print(f"step {step}: r rel. error median {q50:.2e}, 90% {q90:.2e}, share beyond 1e-3 {far:.2e}; "
-              f"energy change {de_g:.6e} (oracle {de_o:.6e})")
-        assert q50 <= 1e-9 and q90 <= 1e-6 and far <= 0.02, (step, q50, q90, far)
-        assert abs(de_g - de_o) <= 1e-7 * abs(e0o) + 0.05 * abs(de_o), (step, de_g, de_o)
+        print(f"step {step}: energy change {de_g:.6e} (oracle {de_o:.6e}), stars {g.nstars()} ({o.nstars()})")
+        if step < 2:
+            assert g.nstars() == o.nstars()
+            assert np.array_equal(g.ids(), o.ids()), step
+            err = rel_err(g.get("r"), o.get("r"))
+            assert np.quantile(err, 0.99) <= 1e-9 and err.max() <= 1e-6, (step, np.quantile(err, 0.99), err.max())
+            assert abs(de_g - de_o) <= 1e-12 * abs(e0o), (step, de_g, de_o)
+        else:
+            assert abs(g.nstars() - o.nstars()) <= 1e-3 * o.nstars(), step
+            assert abs(de_g - de_o) <= 2e-4 * abs(e0o), (step, de_g, de_o)
     g.close()
     o.close()

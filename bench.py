@@ -329,8 +329,10 @@ def train_proposal(a):
 
 
 def learned_leg(a, clusters, params, ctx, timed, stars, w):
-    """Learned-proposal step on the same context (after the plain legs), and
-    one step from a common state with each sampler for the distribution test."""
+    """Learned-proposal step on the same context (after the plain legs), the
+    cost of a trial from a sweep of envelope factors, and one step from a
+    common state with each sampler for the distribution test."""
+    import numpy as np
     from scipy.stats import ks_2samp
 
     import cmcgpu
@@ -352,8 +354,22 @@ def learned_leg(a, clusters, params, ctx, timed, stars, w):
     ctx.kernel_time("reset")
     timed(a.steps, False)
     fam = {name: ctx.kernel_time(name) for name in ALG_BYTES}
+    # what any proposal could save: the orbit phase's time against trials per
+    # star, over envelope factors (the proposal's trials and nothing else
+    # change), fitted by a line; its slope is the marginal cost of a trial
+    sweep = []
+    for kappa in (1.05, a.kappa, 1.6, 2.4):
+        ctx.set_learned(cmcgpu.LEARN_ON, kappa)
+        ctx.step(1)
+        ctx.kernel_time("reset")
+        timed(a.steps, False)
+        ms_orb = ctx.kernel_time("orbit")[0] / a.steps
+        s_k = ctx.learned_stats()
+        tps = (s_k["trials"] + s_k["plain_trials"]) / max(s_k["accepted"] + s_k["plain_stars"], 1)
+        sweep.append((kappa, tps, ms_orb))
     ctx.profile(False)
     ctx.set_learned(cmcgpu.LEARN_OFF)
+    slope, icept = np.polyfit([t for _, t, _ in sweep], [m for _, _, m in sweep], 1)
     mlp_ms = fam["mlp"][0] / max(fam["mlp"][1], 1)
     # the network runs inside a long step: the sustained BF16 rate is its peak
     peak, peak_kind = measured_peak("bf16_tflops_sustained", 1700.0)
@@ -392,6 +408,14 @@ def learned_leg(a, clusters, params, ctx, timed, stars, w):
         "mlp_roofline": {"bound": "tensor", "kernel": "k_mlp_infer", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_kind + " (bf16 sustained)",
                          "flops_per_star": MLP_FLOPS_PER_STAR, "ms_per_launch": mlp_ms},
+        "trial_cost": {
+            "what": "orbit-phase ms per step against trials per star over envelope factors kappa (a line fit): "
+                    "the slope is the marginal cost of one more trial per star; a proposal that needed one trial "
+                    "per star and cost nothing could save at most slope * (plain trials - 1) of the plain step",
+            "sweep": [{"kappa": k, "trials_per_star": t, "orbit_ms": m} for k, t, m in sweep],
+            "ms_per_trial_per_star": float(slope), "orbit_ms_at_zero_trials": float(icept),
+            "max_saving_ms": float(slope * (float(nta.mean()) - 1.0)),
+        },
     }
 
 
@@ -571,6 +595,10 @@ def measure(a, cfg_name, N, rank, ws, dist, weights=None, sub=False):
         try:
             out["learned"] = learned_leg(a, clusters, params, ctx, timed, stars, weights)
             out["learned"]["speedup_vs_plain"] = out["learned"]["value"] / value
+            tc = out["learned"]["trial_cost"]
+            plain_ms = ms_max / a.steps
+            # Amdahl: the plain step less the most any proposal could save
+            tc["max_speedup_any_proposal"] = plain_ms / max(plain_ms - tc["max_saving_ms"], 1e-9)
         except Exception as e:  # the plain numbers stand without it
             out["learned"] = {"error": repr(e)}
     ctx.close()

@@ -49,10 +49,12 @@ struct Tunable {
     const char *variant[4];
 };
 const Tunable kTunables[V_COUNT] = {
-    {"orbit", F_ORBIT, 2, {"5 blocks/SM", "4 blocks/SM"}},
+    {"orbit", F_ORBIT, 4, {"5 blocks/SM", "4 blocks/SM", "5 blocks/SM persistent", "4 blocks/SM persistent"}},
     {"relax", F_RELAX, 2, {"5 blocks/SM", "4 blocks/SM"}},
     {"orbit_learn", F_ORBIT, 2, {"5 blocks/SM", "4 blocks/SM"}},
     {"mlp_grid", F_MLP, 4, {"4 CTAs/SM", "2 CTAs/SM", "3 CTAs/SM", "6 CTAs/SM"}},
+    {"sort_tile", F_SORT, 2, {"2048 keys/tile", "1024 keys/tile"}},
+    {"gather_tile", F_SORT, 3, {"256 stars/block", "128 stars/block", "1024 stars/block"}},
 };
 
 struct ProfRec {
@@ -75,6 +77,7 @@ struct cmcg_ctx {
     double *partials = nullptr;
     unsigned int *tickets = nullptr;
     unsigned int *gbar = nullptr;  // grid barrier of the cooperative tidal kernel
+    unsigned int *orbit_next = nullptr;  // tile counter of the persistent orbit kernels
     int tidal_grid = 1;
     PosQ pq{};
     int posq_grid = 1;
@@ -101,7 +104,7 @@ struct cmcg_ctx {
     Learn lrn{};
     void *lrn_mem = nullptr;
     // launch variants (autotuner; every variant gives bit-identical results)
-    int var[V_COUNT] = {0, 0, 0, 0};
+    int var[V_COUNT] = {};
     // part graphs of a step (HX_* above), per pointer parity at their start:
     // single steps and the host exchange (cmcg_step_host), whose copies run on
     // a second stream and overlap the parts
@@ -215,8 +218,11 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->sb.vals[0] = cv.take<unsigned int>(tot);
     c->sb.vals[1] = cv.take<unsigned int>(tot);
     c->sb.ghist = cv.take<unsigned long long>((size_t)c->ncl * SORT_MAX_PASSES * RADIX);
-    c->sb.status = cv.take<unsigned long long>((size_t)c->t2048.ntiles * RADIX);
+    // look-back words for the digit pass's smaller tiles (1024 keys), the
+    // most tiles either tile size has
+    c->sb.status = cv.take<unsigned long long>((size_t)std::max(c->t1024.ntiles, c->t2048.ntiles) * RADIX);
     c->sb.tile_next = cv.take<unsigned int>(SORT_MAX_PASSES);
+    c->orbit_next = cv.take<unsigned int>(1);
     c->sb.epoch = cv.take<unsigned int>(1);
     c->sb.npass = cv.take<int>(c->ncl);
     c->sb.shift = cv.take<int>(c->ncl);
@@ -756,8 +762,17 @@ static int L_orbit(cmcg_ctx *c)
     k_orbit_pre<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(c->d_cls, c->t128.view(), c->f, c->pq);
     k_posq_scan<<<c->posq_grid, 256, 0, c->stream>>>(c->d_cls, c->f, c->pq);
     if (c->learn_mode == LEARN_OFF) {
-        (c->var[V_ORBIT] ? k_orbit_lb4 : k_orbit)<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(
-            c->d_cls, c->t128.view(), c->f, c->partials, c->tickets, c->pq);
+        const int ov = c->var[V_ORBIT];
+        if (ov < 2) {  // one block per tile, 5 or 4 blocks per SM
+            (ov ? k_orbit_lb4 : k_orbit)<<<c->t128.ntiles, ORB_T, 0, c->stream>>>(
+                c->d_cls, c->t128.view(), c->f, c->partials, c->tickets, c->pq);
+        } else {  // persistent: as many blocks as the SMs hold, tiles taken from a counter
+            const int per_sm = ov == 2 ? 5 : 4;
+            const int grid = (int)std::min<long long>(c->t128.ntiles, (long long)per_sm * c->nsm);
+            CK(cudaMemsetAsync(c->orbit_next, 0, sizeof(unsigned int), c->stream));
+            (ov == 2 ? k_orbit_pers : k_orbit_pers_lb4)<<<grid, ORB_T, 0, c->stream>>>(
+                c->d_cls, c->t128.view(), c->f, c->partials, c->tickets, c->pq, c->orbit_next);
+        }
         c->launches += 3;
     } else {
         // apsides and features; the network on every star slot; the sampling
@@ -834,11 +849,19 @@ static int L_sort(cmcg_ctx *c)
     k_sort_prep<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb,
                                                                    c->partials, c->tickets);
     k_sort_ghist<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb);
+    // digit passes over 2048- or 1024-key tiles (autotuner)
+    const TileTable &ost = c->var[V_SORT_TILE] == 1 ? c->t1024 : c->t2048;
     for (int p = 0; p < SORT_MAX_PASSES; ++p)
-        k_sort_onesweep<<<c->t2048.ntiles, OS_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb, p);
+        launch_sort_onesweep(c->var[V_SORT_TILE] == 1 ? 1024 : 2048, ost.ntiles, c->stream, c->d_cls, ost.view(), c->f,
+                             c->sb, p);
     k_sort_fix<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb);
     k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb);
-    k_sort_gather<<<c->t256.ntiles, GATHER_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->sb);
+    // the payload gather, 256, 128 or 1024 stars per block (autotuner)
+    {
+        const int gv = c->var[V_GATHER_TILE];
+        const TileTable &gt = gv == 1 ? c->t128 : gv == 2 ? c->t1024 : c->t256;
+        launch_sort_gather(gv == 1 ? 128 : gv == 2 ? 1024 : 256, gt.ntiles, c->stream, c->d_cls, gt.view(), c->f, c->sb);
+    }
     k_sort_commit<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
     fam_end(c);
     c->launches += 6 + SORT_MAX_PASSES;
@@ -1698,7 +1721,8 @@ int cmcg_autotune(cmcg_ctx *c, int steps, char *report, long report_len)
     for (int t = 0; t < V_COUNT; ++t) {
         const bool used = (t == V_ORBIT && c->learn_mode == LEARN_OFF) || (t == V_RELAX && !c->relax_fp32) ||
                           (t == V_LEARN && c->learn_mode != LEARN_OFF) ||
-                          (t == V_MLP_GRID && c->learn_mode == LEARN_ON);
+                          (t == V_MLP_GRID && c->learn_mode == LEARN_ON) || t == V_SORT_TILE ||
+                          t == V_GATHER_TILE;
         if (!used) continue;
         const Tunable &T = kTunables[t];
         int best = c->var[t];

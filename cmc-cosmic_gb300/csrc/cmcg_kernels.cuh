@@ -11,7 +11,6 @@ constexpr int ORB_T = 128, ORB_NPART = 5;
 constexpr int TID_T = 2048, TID_THREADS = 256, TID_NPART = 4;
 constexpr int SORT_THREADS = 256, SORT_ITEMS = 8, SORT_T = SORT_THREADS * SORT_ITEMS, RADIX = 256;
 constexpr int OS_THREADS = 512;  // onesweep digit pass: 4 keys per thread, 32 warps per SM
-constexpr int GATHER_T = 256;
 constexpr int POT_THREADS = 256, POT_ITEMS = 4, POT_T = POT_THREADS * POT_ITEMS;
 static_assert(TS_T == POT_T, "the time step runs on the potential's tile table");
 constexpr int EC3_T = 256, EN_T = 2048, EN_THREADS = 256;
@@ -184,19 +183,31 @@ __global__ void k_orbit_aps(const Cluster *cls, Tiles tm, Fields f, double *part
                             Learn L);
 __global__ void k_orbit_learn(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                               PosQ pq, Learn L);
+// persistent forms of k_orbit / k_orbit_lb4: tiles taken from *next (zeroed before the launch)
+__global__ void k_orbit_pers(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets, PosQ pq,
+                             unsigned int *next);
+__global__ void k_orbit_pers_lb4(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
+                                 PosQ pq, unsigned int *next);
 __global__ void k_orbit_learn_lb4(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                                   PosQ pq, Learn L);
 
 // ---- launch variants the autotuner chooses between (bit-identical results)
-enum { V_ORBIT, V_RELAX, V_LEARN, V_MLP_GRID, V_COUNT };
+enum { V_ORBIT, V_RELAX, V_LEARN, V_MLP_GRID, V_SORT_TILE, V_GATHER_TILE, V_COUNT };
 __global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *bar, int nclusters);
 __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, double *partials,
                             unsigned int *tickets);
 __global__ void k_sort_ghist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
-__global__ void k_sort_onesweep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, int pass);
+// One digit pass over tiles of `tile_keys` keys (1024 or 2048: the
+// autotuner's candidates; tm is the matching tile table).  Host launchers of
+// the templated kernels, defined beside them (a template kernel's launch stub
+// is local to the file that instantiates it).
+void launch_sort_onesweep(int tile_keys, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f,
+                          SortBufs sb, int pass);
 __global__ void k_sort_fix(const Cluster *cls, Tiles tm, SortBufs sb);
 __global__ void k_sort_fix_long(const Cluster *cls, Tiles tm, SortBufs sb);
-__global__ void k_sort_gather(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
+// The payload gather, `block` stars per block (128, 256 or 1024, on the
+// matching tile table).
+void launch_sort_gather(int block, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
 __global__ void k_sort_commit(const Cluster *cls, int nclusters);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);
 __global__ void k_pot_carry(const Cluster *cls, Tiles tm, PotBufs pb, PhiBufs ph, int nclusters);

@@ -941,10 +941,10 @@ static __device__ __forceinline__ void add_stat(unsigned long long *dst, unsigne
 template <int MODE>
 static __device__ __forceinline__ void orbit_body(const Cluster *__restrict__ cls, Tiles tm, const Fields &f,
                                                   double *partials, unsigned int *tickets, const PosQ &pq,
-                                                  const Learn &L, SampleSmem &sm, LearnSmem *ls)
+                                                  const Learn &L, SampleSmem &sm, LearnSmem *ls, int tile)
 {
     __shared__ double red[ORB_T / 32];
-    const int2 ct = tm.tiles[blockIdx.x];
+    const int2 ct = tm.tiles[tile];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
@@ -1091,7 +1091,7 @@ static __device__ __forceinline__ void orbit_body(const Cluster *__restrict__ cl
     const double tmax = block_max_nonneg<ORB_T>(max_rad, s_max);
     __shared__ int s_last;
     if (threadIdx.x == 0) {
-        double *slot = partials + (size_t)blockIdx.x * ORB_NPART;
+        double *slot = partials + (size_t)tile * ORB_NPART;
         slot[0] = acc[0];
         slot[1] = acc[1];
         slot[2] = acc[2];
@@ -1128,7 +1128,7 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit(const Cluster *__restrict__ 
 {
     __shared__ SampleSmem sm;
     const Learn none{};
-    orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr);
+    orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr, blockIdx.x);
 }
 
 // The same kernel with room for 128 registers a thread (four blocks per SM):
@@ -1138,14 +1138,51 @@ __global__ void __launch_bounds__(ORB_T, 4) k_orbit_lb4(const Cluster *__restric
 {
     __shared__ SampleSmem sm;
     const Learn none{};
-    orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr);
+    orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr, blockIdx.x);
+}
+
+// The persistent forms: a grid of (blocks per SM) x (SMs) blocks, each taking
+// tiles from a counter (zeroed before the launch) until none are left, in
+// the order the per-tile grid runs them.  The same tiles, partial slots and
+// per-cluster last-arriver reductions: bit-identical results.  Autotuner
+// candidates beside the one-block-per-tile grids above.
+static __device__ __forceinline__ void orbit_persistent(const Cluster *__restrict__ cls, Tiles tm, const Fields &f,
+                                                        double *partials, unsigned int *tickets, const PosQ &pq,
+                                                        unsigned int *next, SampleSmem &sm)
+{
+    __shared__ int s_tile;
+    const Learn none{};
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(next, 1u);
+        __syncthreads();
+        const int b = s_tile;
+        if (b >= tm.ntiles) break;
+        orbit_body<0>(cls, tm, f, partials, tickets, pq, none, sm, nullptr, b);
+        __syncthreads();  // s_tile and the sampling state are the next tile's
+    }
+}
+
+__global__ void __launch_bounds__(ORB_T, 5) k_orbit_pers(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                      double *partials, unsigned int *tickets, PosQ pq,
+                                                      unsigned int *next)
+{
+    __shared__ SampleSmem sm;
+    orbit_persistent(cls, tm, f, partials, tickets, pq, next, sm);
+}
+
+__global__ void __launch_bounds__(ORB_T, 4) k_orbit_pers_lb4(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                          double *partials, unsigned int *tickets, PosQ pq,
+                                                          unsigned int *next)
+{
+    __shared__ SampleSmem sm;
+    orbit_persistent(cls, tm, f, partials, tickets, pq, next, sm);
 }
 
 __global__ void __launch_bounds__(ORB_T, 5) k_orbit_aps(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                      double *partials, unsigned int *tickets, PosQ pq, Learn L)
 {
     __shared__ SampleSmem sm;
-    orbit_body<1>(cls, tm, f, partials, tickets, pq, L, sm, nullptr);
+    orbit_body<1>(cls, tm, f, partials, tickets, pq, L, sm, nullptr, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(ORB_T, 5) k_orbit_learn(const Cluster *__restrict__ cls, Tiles tm, Fields f,
@@ -1153,7 +1190,7 @@ __global__ void __launch_bounds__(ORB_T, 5) k_orbit_learn(const Cluster *__restr
 {
     __shared__ SampleSmem sm;
     __shared__ LearnSmem ls;
-    orbit_body<2>(cls, tm, f, partials, tickets, pq, L, sm, &ls);
+    orbit_body<2>(cls, tm, f, partials, tickets, pq, L, sm, &ls, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(ORB_T, 4) k_orbit_learn_lb4(const Cluster *__restrict__ cls, Tiles tm, Fields f,
@@ -1161,7 +1198,7 @@ __global__ void __launch_bounds__(ORB_T, 4) k_orbit_learn_lb4(const Cluster *__r
 {
     __shared__ SampleSmem sm;
     __shared__ LearnSmem ls;
-    orbit_body<2>(cls, tm, f, partials, tickets, pq, L, sm, &ls);
+    orbit_body<2>(cls, tm, f, partials, tickets, pq, L, sm, &ls, blockIdx.x);
 }
 
 // Grid-wide barrier for a co-resident (cooperatively launched) grid:

@@ -20,9 +20,13 @@
 //                    digit leave the block as contiguous stores
 // Tiles never straddle clusters, so one launch sorts every cluster of an
 // ensemble independently.
+// The radii (pass 0, the histograms, the key range) and the keys and values of
+// the later passes are read with 128-bit loads: double2 pairs of radii,
+// ulonglong2 pairs of keys and uint4 quads of values, staged through shared
+// memory into the warp-striped order the ranking uses.
 // k_sort_gather then moves the payload (rnew, m, vrnew, vtnew, id, r, ec_pre)
-// into radial order with 128-bit-aligned SoA loads and drops the escapers
-// (r == SF_INFINITY), which sort last.
+// into radial order, one 8-byte gather per field and star, and drops the
+// escapers (r == SF_INFINITY), which sort last.
 #include "cmcg_kernels.cuh"
 #include "cmcgpu.h"
 
@@ -44,15 +48,25 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
     unsigned long long kmn = ~0ull, kmx = 0ull;
     long long cnt = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(sb.epoch, 1u);  // this sort's look-back epoch
-    const long long base = 1 + (long long)ct.y * SORT_T;
-    for (int i = threadIdx.x; i < SORT_T; i += SORT_THREADS) {
-        const long long k = base + i;
+    // stars k = k0 + 1 .. k0 + SORT_T (1-based), with 128-bit loads: the
+    // aligned pair at C.off + k0 + 2t holds stars k0 + 2t and k0 + 2t + 1
+    const long long k0 = (long long)ct.y * SORT_T;
+    const double *src = f.rnew + C.off + k0;
+    for (int t = threadIdx.x; t <= SORT_T / 2; t += SORT_THREADS) {
+        const long long k = k0 + 2 * (long long)t;  // the pair's first star
         if (k > N) break;
-        const unsigned long long b = (unsigned long long)__double_as_longlong(f.rnew[C.off + k]);
-        if (b != inf_bits) {
+        const double2 v = *reinterpret_cast<const double2 *>(src + 2 * t);
+        const unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x);
+        const unsigned long long b1 = (unsigned long long)__double_as_longlong(v.y);
+        if (t > 0 && b0 != inf_bits) {
             cnt++;
-            kmn = min(kmn, b);
-            kmx = max(kmx, b);
+            kmn = min(kmn, b0);
+            kmx = max(kmx, b0);
+        }
+        if (k + 1 <= N && t < SORT_T / 2 && b1 != inf_bits) {
+            cnt++;
+            kmn = min(kmn, b1);
+            kmx = max(kmx, b1);
         }
     }
 #pragma unroll
@@ -151,13 +165,6 @@ static __device__ __forceinline__ unsigned long long radius_key(double r, unsign
     return b == (unsigned long long)__double_as_longlong(CMCG_SF_INFINITY) ? kesc : b - kmin;
 }
 
-static __device__ __forceinline__ unsigned long long load_key(const Cluster &C, const Fields &f, const SortBufs &sb,
-                                                              int pass, int cur, long long pos /*0-based*/, int c)
-{
-    if (pass == 0) return radius_key(f.rnew[C.off + 1 + pos], sb.kmin[c], sb.kmax[c]);
-    return (cur ? sb.keys[1] : sb.keys[0])[C.off + pos];
-}
-
 // All digit histograms of the cluster's keys in one read (they do not depend
 // on the order the passes put the keys in): per-block shared counters, then
 // one global add per (pass, digit).
@@ -175,12 +182,21 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_ghist(const Cluster *__re
     const int sh = sb.shift[ct.x];
     for (int i = threadIdx.x; i < SORT_MAX_PASSES * RADIX; i += SORT_THREADS) (&h[0][0])[i] = 0u;
     __syncthreads();
-    const long long base = (long long)ct.y * SORT_T;
-    for (int i = threadIdx.x; i < SORT_T; i += SORT_THREADS) {
-        const long long pos = base + i;
-        if (pos >= N) break;
-        const unsigned long long k = radius_key(f.rnew[C.off + 1 + pos], kmin, kesc);
-        for (int p = 0; p < np; ++p) atomicAdd(&h[p][(unsigned int)(k >> (sh + 8 * p)) & (RADIX - 1)], 1u);
+    const long long base = (long long)ct.y * SORT_T, ntile = N - base;
+    // 128-bit loads: the aligned pair at src + 2t holds items 2t - 1 and 2t
+    const double *src = f.rnew + C.off + base;
+    for (int t = threadIdx.x; t <= SORT_T / 2; t += SORT_THREADS) {
+        const long long i0 = 2 * (long long)t - 1;
+        if (i0 >= ntile) break;
+        const double2 v = *reinterpret_cast<const double2 *>(src + 2 * t);
+        if (i0 >= 0) {
+            const unsigned long long k = radius_key(v.x, kmin, kesc);
+            for (int p = 0; p < np; ++p) atomicAdd(&h[p][(unsigned int)(k >> (sh + 8 * p)) & (RADIX - 1)], 1u);
+        }
+        if (i0 + 1 < ntile && i0 + 1 < SORT_T) {
+            const unsigned long long k = radius_key(v.y, kmin, kesc);
+            for (int p = 0; p < np; ++p) atomicAdd(&h[p][(unsigned int)(k >> (sh + 8 * p)) & (RADIX - 1)], 1u);
+        }
     }
     __syncthreads();
     unsigned long long *g = sb.ghist + (size_t)ct.x * SORT_MAX_PASSES * RADIX;
@@ -209,15 +225,16 @@ __device__ __forceinline__ unsigned long long st_tag(unsigned int epoch, int pas
 // onesweep radix sort), then write their keys in runs of one digit.  A tile
 // only waits on tiles that took a smaller index, which have started; every
 // wait is bounded and records CMCG_ERR_SPIN if it gives up.
+template <int ITEMS>
 __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                               SortBufs sb, int pass)
 {
-    constexpr int NWARP = OS_THREADS / 32, ITEMS = SORT_T / OS_THREADS;
+    constexpr int NWARP = OS_THREADS / 32, T = OS_THREADS * ITEMS;  // T keys per tile
     __shared__ unsigned int wcnt[NWARP][RADIX];  // per-warp digit counters -> prefixes
     __shared__ unsigned int dstart[RADIX];       // in-tile digit start
     __shared__ unsigned long long gbase[RADIX];  // global digit start for this tile
-    __shared__ unsigned long long sk[SORT_T];
-    __shared__ unsigned int sv[SORT_T];
+    __shared__ __align__(16) unsigned long long sk[T];
+    __shared__ __align__(16) unsigned int sv[T];
     __shared__ unsigned int s_w[RADIX / 32];
     __shared__ unsigned long long s_t[RADIX / 32];
     __shared__ int s_b;
@@ -234,20 +251,57 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int cur = pass & 1, nxt = cur ^ 1;
     const int shift = sb.shift[ct.x] + 8 * pass;
-    const long long base = (long long)ct.y * SORT_T;
+    const long long base = (long long)ct.y * T;
     for (int i = threadIdx.x; i < NWARP * RADIX; i += OS_THREADS) (&wcnt[0][0])[i] = 0u;
     __syncthreads();
 
+    // The tile's keys and values into shared memory with 128-bit loads (the
+    // output staging buffers are free until the ranking is done), then each
+    // thread takes its warp-striped items from there.  Slices start on
+    // 256-byte boundaries and are padded to 32 elements, so every vector load
+    // is aligned and stays inside the cluster's slice.
+    const long long ntile = N - base;  // items of this tile (<= 0: none)
+    if (pass == 0) {
+        // radii are 1-based: item i is rnew[C.off + 1 + base + i]; the aligned
+        // pair at src + 2t holds items 2t - 1 and 2t
+        const double *src = f.rnew + C.off + base;
+        const unsigned long long kmin = sb.kmin[ct.x], kesc = sb.kmax[ct.x];
+        for (int t = threadIdx.x; t <= T / 2; t += OS_THREADS) {
+            const long long i0 = 2 * (long long)t - 1;
+            if (i0 >= ntile) break;
+            const double2 v = *reinterpret_cast<const double2 *>(src + 2 * t);
+            if (i0 >= 0) sk[i0] = radius_key(v.x, kmin, kesc);
+            if (i0 + 1 < ntile && i0 + 1 < T) sk[i0 + 1] = radius_key(v.y, kmin, kesc);
+        }
+    } else {
+        const unsigned long long *ks = (cur ? sb.keys[1] : sb.keys[0]) + C.off + base;
+        const unsigned int *vs = (cur ? sb.vals[1] : sb.vals[0]) + C.off + base;
+        for (int t = threadIdx.x; t < T / 4; t += OS_THREADS) {
+            const long long i0 = 4 * (long long)t;
+            if (i0 >= ntile) break;
+            if (i0 + 3 < ntile) {
+                *reinterpret_cast<ulonglong2 *>(sk + i0) = *reinterpret_cast<const ulonglong2 *>(ks + i0);
+                *reinterpret_cast<ulonglong2 *>(sk + i0 + 2) = *reinterpret_cast<const ulonglong2 *>(ks + i0 + 2);
+                *reinterpret_cast<uint4 *>(sv + i0) = *reinterpret_cast<const uint4 *>(vs + i0);
+            } else {
+                for (long long q = i0; q < ntile; ++q) {
+                    sk[q] = ks[q];
+                    sv[q] = vs[q];
+                }
+            }
+        }
+    }
+    __syncthreads();
     unsigned long long key[ITEMS];
     unsigned int val[ITEMS], dig[ITEMS], rank[ITEMS];
     bool valid[ITEMS];
 #pragma unroll
     for (int it = 0; it < ITEMS; ++it) {
         // warp-striped: warp w owns [w*ITEMS*32, (w+1)*ITEMS*32), item it, lane l -> w*ITEMS*32 + it*32 + l
-        const long long pos = base + w * (ITEMS * 32) + it * 32 + lane;
-        valid[it] = pos < N;
-        key[it] = valid[it] ? load_key(C, f, sb, pass, cur, pos, ct.x) : 0ull;
-        val[it] = valid[it] ? (pass == 0 ? (unsigned int)pos : (cur ? sb.vals[1] : sb.vals[0])[C.off + pos]) : 0u;
+        const int i = w * (ITEMS * 32) + it * 32 + lane;
+        valid[it] = i < ntile;
+        key[it] = valid[it] ? sk[i] : 0ull;
+        val[it] = valid[it] ? (pass == 0 ? (unsigned int)(base + i) : sv[i]) : 0u;
         dig[it] = (unsigned int)(key[it] >> shift) & (RADIX - 1);
     }
 #pragma unroll
@@ -352,7 +406,7 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
     }
     __syncthreads();
     long long nt = N - base;
-    if (nt > SORT_T) nt = SORT_T;
+    if (nt > T) nt = T;
     unsigned long long *kout = nxt ? sb.keys[1] : sb.keys[0];
     unsigned int *vout = nxt ? sb.vals[1] : sb.vals[0];
     for (int i = threadIdx.x; i < nt; i += OS_THREADS) {
@@ -366,6 +420,15 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
         kout[C.off + dst] = k;
         vout[C.off + dst] = sv[i];
     }
+}
+
+void launch_sort_onesweep(int tile_keys, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f,
+                          SortBufs sb, int pass)
+{
+    if (tile_keys == OS_THREADS * 2)
+        k_sort_onesweep<2><<<ntiles, OS_THREADS, 0, s>>>(cls, tm, f, sb, pass);
+    else
+        k_sort_onesweep<4><<<ntiles, OS_THREADS, 0, s>>>(cls, tm, f, sb, pass);
 }
 
 // After the digit passes, runs of keys sharing their sorted prefix are in
@@ -515,7 +578,8 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *_
 // Payload gather into radial order (ComputeIntermediateEnergy transfer +
 // post_sort_comm).  Writes the second buffers of r, m, id, ec_pre, which the
 // host then swaps with the first.
-__global__ void __launch_bounds__(256) k_sort_gather(const Cluster *__restrict__ cls, Tiles tm, Fields f, SortBufs sb)
+template <int GT>
+__global__ void __launch_bounds__(GT) k_sort_gather(const Cluster *__restrict__ cls, Tiles tm, Fields f, SortBufs sb)
 {
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
@@ -523,7 +587,7 @@ __global__ void __launch_bounds__(256) k_sort_gather(const Cluster *__restrict__
     Scalars *sc = C.sc;
     const long long nb = sc->n_bound;
     const int np = sb.npass[ct.x];
-    const long long i = (long long)ct.y * 256 + threadIdx.x;  // 0-based output position
+    const long long i = (long long)ct.y * GT + threadIdx.x;  // 0-based output position
     const long long off = C.off;
     if (nb < 0 || nb > sc->N_MAX_NEW) {
         if (i == 0) set_error(sc, CMCG_ERR_BOUNDS, nb);
@@ -554,6 +618,16 @@ __global__ void __launch_bounds__(256) k_sort_gather(const Cluster *__restrict__
         f.r2[off + nb + 1] = CMCG_SF_INFINITY;
         f.m2[off + nb + 1] = 0.0;
     }
+}
+
+void launch_sort_gather(int block, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f, SortBufs sb)
+{
+    if (block == 128)
+        k_sort_gather<128><<<ntiles, 128, 0, s>>>(cls, tm, f, sb);
+    else if (block == 1024)
+        k_sort_gather<1024><<<ntiles, 1024, 0, s>>>(cls, tm, f, sb);
+    else
+        k_sort_gather<256><<<ntiles, 256, 0, s>>>(cls, tm, f, sb);
 }
 
 // New N_MAX after the gather (cmc_sort.c:343-354, cmc_utils.c:2246); a kernel of

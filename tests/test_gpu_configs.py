@@ -152,7 +152,8 @@ def test_ten_free_running_steps(gpulib, orc, model, imf):
 
     The two runs part in the last bits at the first relaxation: the deflection
     angles go through libm's sin/cos in the oracle and CUDA's on the GPU.  For
-    the first two steps the same stars stay in the same order, radii agree to
+    the first two steps the same stars stay in order (but for neighbours
+    closer than the drift, which may trade places), radii agree to
     ~1e-10 (99th percentile, measured on the GB300: 6.8e-11 Plummer, 6.0e-11
     King) and the energy change agrees to ~1e-14 of the total.  Then an ulp of
     E moves some rejection trial across its acceptance test, that star lands
@@ -174,9 +175,13 @@ def test_ten_free_running_steps(gpulib, orc, model, imf):
         de_g = g.scalar("Etot") - e0g
         print(f"step {step}: energy change {de_g:.6e} (oracle {de_o:.6e}), stars {g.nstars()} ({o.nstars()})")
         if step < 2:
+            # the same stars, each at the oracle's radius to the drift; two
+            # neighbours closer than the drift may trade places in the order
             assert g.nstars() == o.nstars()
-            assert np.array_equal(g.ids(), o.ids()), step
-            err = rel_err(g.get("r"), o.get("r"))
+            ids_g, ids_o = g.ids(), o.ids()
+            assert np.array_equal(np.sort(ids_g), np.sort(ids_o)), step
+            assert np.mean(ids_g == ids_o) >= 0.999, step
+            err = rel_err(g.get("r")[np.argsort(ids_g)], o.get("r")[np.argsort(ids_o)])
             assert np.quantile(err, 0.99) <= 1e-9 and err.max() <= 1e-6, (step, np.quantile(err, 0.99), err.max())
             assert abs(de_g - de_o) <= 1e-12 * abs(e0o), (step, de_g, de_o)
         else:

@@ -47,18 +47,19 @@ ALG_BYTES = {"sort": 116, "potential": 24, "relax": 72, "orbit": 80, "ec3": 72, 
 # the proposal network's algorithmic FLOPs per star: 2 (8*64 + 64*64 + 64*33)
 MLP_FLOPS_PER_STAR = 2 * (8 * 64 + 64 * 64 + 64 * 33)
 # DRAM bytes per star of one launch, dram__bytes_read.sum + dram__bytes_write.sum
-# from one ncu capture, scaled by stars: k_orbit
-# 961.2 MB over 1,912,424 stars (King W0=6 + Kroupa, N=2e6), k_relax64 57.5 MB
-# over 962,913 stars (the same model at N=1e6)
-NCU_TRAFFIC_PER_STAR = {"orbit": 961.2e6 / 1912424, "relax": 57.5e6 / 962913}
+# from one-kernel, one-launch ncu captures on the King W0=6 + Kroupa model at
+# N = 1e6 (962,913 stars in the captured step): k_orbit 142.4 MB, k_relax64
+# 57.5 MB, k_ec3 63.3 MB, k_sort_gather 97.6 MB
+NCU_TRAFFIC_PER_STAR = {"orbit": 142.4e6 / 962913, "relax": 57.5e6 / 962913, "ec3": 63.3e6 / 962913}
 # share of cycles the FP64 pipe was busy in the same captures: the kernels'
-# real bound on GB300 (1/64-rate FP64), reported beside the HBM roofline
-NCU_FP64_PIPE_ACTIVE = {"orbit": 0.685, "relax": 0.703}
-# FP64 thread-operations per star of each kernel family (ncu
-# smsp__sass_thread_inst_executed_op_fp64_pred_on.sum over the stars of one
-# step, King W0=6 + Kroupa, N = 1e6), and the measured FP64 FMA rate of this
-# GPU (a dependent-chain DFMA probe: 1.01 TFLOP/s = 5.05e11 DFMA/s)
-NCU_FP64_OPS_PER_STAR = {"orbit": 343.2, "relax": 181.1, "potential": 61.4, "ec3": 45.0, "energy": 11.8,
+# real bound on GB300, reported beside the HBM roofline
+NCU_FP64_PIPE_ACTIVE = {"orbit": 0.742, "relax": 0.843, "ec3": 0.842, "potential": 0.816}
+# FP64 thread-operations per star of each kernel family
+# (smsp__sass_thread_inst_executed_op_fp64_pred_on.sum over the stars of one
+# step, same model: k_orbit 338.2 and k_orbit_pre 8.0, k_relax64 181.1, k_ec3
+# 45.0), and the FP64 pipe's rate at 100% busy, ops / (time x busy) from those
+# captures: 4.7-5.6e11 thread-operations/s
+NCU_FP64_OPS_PER_STAR = {"orbit": 346.2, "relax": 181.1, "potential": 61.4, "ec3": 45.0, "energy": 11.8,
                          "timestep": 12.1, "tidal": 2.1}
 FP64_PEAK_OPS = 5.05e11
 
@@ -580,7 +581,7 @@ def measure(a, cfg_name, N, rank, ws, dist, weights=None, sub=False):
                           "frac": NCU_FP64_OPS_PER_STAR.get(top, 0.0) * n_prof / (ms_top / n_top * 1e-3)
                           / FP64_PEAK_OPS,
                           "ops_per_star": NCU_FP64_OPS_PER_STAR.get(top),
-                          "peak_source": "measured DFMA rate of this GPU (1.01 TFLOP/s)",
+                          "peak_source": "the FP64 pipe at 100% busy, from the ncu captures (4.7-5.6e11 ops/s)",
                           "step_frac": sum(NCU_FP64_OPS_PER_STAR.values()) * n_prof / (step_ms * 1e-3)
                           / FP64_PEAK_OPS},
         "energy": {"rel_drift_per_step": drift[0] if ncl == 1 else None,

@@ -62,6 +62,22 @@ struct ProfRec {
     cudaEvent_t a, b;
 };
 
+// One segment of a batched host exchange (k_xfer): n 8-byte words from src to dst.
+struct XferSeg {
+    unsigned long long *dst;
+    const unsigned long long *src;
+    long long n;   // 8-byte words
+    long long c0;  // first chunk of the segment in its batch
+};
+constexpr int XFER_THREADS = 256, XFER_UNROLL = 4, XFER_CHUNK = XFER_THREADS * XFER_UNROLL;
+constexpr int XFER_PER_CLUSTER = 6;  // segments per cluster: four uploads, two downloads
+// The exchange's table: the segments, then every cluster's star count, in one
+// block (host and device alike) that goes up in one copy.
+static size_t xfer_table_bytes(int ncl)
+{
+    return (size_t)XFER_PER_CLUSTER * ncl * sizeof(XferSeg) + (size_t)ncl * sizeof(long long);
+}
+
 }  // namespace
 
 struct cmcg_ctx {
@@ -113,6 +129,10 @@ struct cmcg_ctx {
     cudaStream_t copy = nullptr;
     cudaEvent_t ev_sorted = nullptr, ev_copied = nullptr, ev_in = nullptr, ev_ec3 = nullptr, ev_ej = nullptr;
     long long *d_nout = nullptr;  // per cluster: stars after the step
+    // batched host exchange: segment tables (pinned host copy, device copy)
+    // and per-cluster counts, XFER_PER_CLUSTER segments per cluster
+    XferSeg *h_xfer = nullptr, *d_xfer = nullptr;
+    long long *h_xn = nullptr, *d_xn = nullptr;
     // graphs
     // The sort swaps the field pointers every step, so a captured two-step
     // graph is tied to the pointer parity it was captured at: one per parity.
@@ -223,6 +243,8 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->sb.status = cv.take<unsigned long long>((size_t)std::max(c->t1024.ntiles, c->t2048.ntiles) * RADIX);
     c->sb.tile_next = cv.take<unsigned int>(SORT_MAX_PASSES);
     c->orbit_next = cv.take<unsigned int>(1);
+    c->d_xfer = (XferSeg *)cv.take<char>(xfer_table_bytes(c->ncl));
+    c->d_xn = c->d_xfer ? (long long *)(c->d_xfer + (size_t)XFER_PER_CLUSTER * c->ncl) : nullptr;
     c->sb.epoch = cv.take<unsigned int>(1);
     c->sb.npass = cv.take<int>(c->ncl);
     c->sb.shift = cv.take<int>(c->ncl);
@@ -484,11 +506,13 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_ec3, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_ej, cudaEventDisableTiming) != cudaSuccess ||
-        cudaMalloc(&c->d_nout, (size_t)nclusters * sizeof(long long)) != cudaSuccess) {
+        cudaMalloc(&c->d_nout, (size_t)nclusters * sizeof(long long)) != cudaSuccess ||
+        cudaHostAlloc((void **)&c->h_xfer, xfer_table_bytes(nclusters), cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         cmcg_destroy(c);
         return CMCG_ERR_CUDA;
     }
+    c->h_xn = (long long *)(c->h_xfer + (size_t)XFER_PER_CLUSTER * nclusters);
     CK(cudaStreamSynchronize(c->stream));
     *out = c;
     return CMCG_OK;
@@ -513,6 +537,7 @@ int cmcg_destroy(cmcg_ctx *c)
     for (cudaEvent_t e : {c->ev_sorted, c->ev_copied, c->ev_in, c->ev_ec3, c->ev_ej})
         if (e) cudaEventDestroy(e);
     if (c->d_nout) cudaFree(c->d_nout);
+    if (c->h_xfer) cudaFreeHost(c->h_xfer);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return CMCG_OK;
@@ -581,6 +606,60 @@ __global__ void k_set_count(const Cluster *cls, int k, long long N)
     sc->N_MAX = N;
     sc->N_MAX_NEW = N;
     sc->ridx_ok = 0;
+}
+
+// Host exchange by kernel.  Each batch of transfers -- the same field group of
+// every cluster: the four inputs the time step reads, or E and J after the
+// energies -- is one launch that moves 8-byte words between the caller's
+// pinned host arrays (addressed from the device through unified addressing)
+// and the context's fields, in place of one cudaMemcpyAsync per array.  On
+// this GPU a kernel reads and writes pinned host memory over NVLink-C2C as
+// fast as the copy engines do (~200 GB/s each way); the launch replaces the
+// per-copy set-up, which adds up over an ensemble's many small arrays.  The
+// batch's segments sit in order of their first chunk.
+// (XferSeg and the chunk sizes: beside cmcg_ctx above)
+
+__global__ void __launch_bounds__(XFER_THREADS) k_xfer(const XferSeg *__restrict__ seg, int nseg, long long nchunk)
+{
+    for (long long c = blockIdx.x; c < nchunk; c += gridDim.x) {
+        int lo = 0, hi = nseg - 1;  // the last segment whose first chunk is <= c
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (seg[mid].c0 <= c)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const unsigned long long *src = seg[lo].src;
+        unsigned long long *dst = seg[lo].dst;
+        const long long n = seg[lo].n, i0 = (c - seg[lo].c0) * XFER_CHUNK + threadIdx.x;
+        unsigned long long v[XFER_UNROLL];
+#pragma unroll
+        for (int u = 0; u < XFER_UNROLL; ++u) {
+            const long long i = i0 + (long long)u * XFER_THREADS;
+            if (i < n) v[u] = src[i];
+        }
+#pragma unroll
+        for (int u = 0; u < XFER_UNROLL; ++u) {
+            const long long i = i0 + (long long)u * XFER_THREADS;
+            if (i < n) dst[i] = v[u];
+        }
+    }
+}
+
+// Every cluster's star count after the exchange's upload, and the sentinel
+// star_r[N+1] = SF_INFINITY.
+__global__ void k_set_counts(const Cluster *cls, Fields f, int nclusters, const long long *N)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nclusters) return;
+    const long long n = N[k];
+    if (n < 0 || n > cls[k].cap) return;  // the host checked; nothing outside the slice is written
+    Scalars *sc = cls[k].sc;
+    sc->N_MAX = n;
+    sc->N_MAX_NEW = n;
+    sc->ridx_ok = 0;
+    f.r[cls[k].off + n + 1] = CMCG_SF_INFINITY;
 }
 
 // Host exchange: the caller's E and J travel into rnew and vrnew (which
@@ -1768,10 +1847,147 @@ int cmcg_autotune(cmcg_ctx *c, int steps, char *report, long report_len)
 //   and energy conservation; vr, vt after energy conservation, during the
 //   energies; E, J last.
 // Each part is replayed from its own graph when graphs are enabled.
+
+// The device address of a caller's host array when a kernel can reach it
+// (pinned or registered host memory, or device or managed memory), else
+// nullptr: pageable memory goes by the copy engines.
+static const void *device_view(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return a.devicePointer;
+    return nullptr;
+}
+
+// The step on host arrays with the exposed transfers batched into k_xfer
+// launches: the uploads of r, m, vr, vt that precede the time step, and the
+// downloads of E and J that follow the energies, with nothing else running on
+// the GPU meanwhile.  The transfers that overlap kernels (id during the time
+// step, E and J staged during the relaxation, r, m, id during the potential,
+// vr, vt during the energies) stay on the copy engines, one cudaMemcpyAsync
+// per array: a copy kernel beside a kernel that fills the SMs waits for free
+// slots, a copy engine does not.  Sets *pageable, and does nothing, when some
+// caller array is not reachable from the device: the caller then takes the
+// copy path for every transfer.
+static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out, bool graphs, long l0,
+                             bool *pageable)
+{
+    *pageable = false;
+    const int ncl = c->ncl;
+    XferSeg *t = c->h_xfer;
+    // batch 0 (uploads) holds four segments per cluster, batch 1 (E, J down) two
+    const int base[2] = {0, 4 * ncl};
+    long long nchunk[2] = {0, 0};
+    int nseg[2] = {0, 0};
+    auto add = [&](int b, void *dst, const void *src, long long n) {
+        XferSeg &e = t[base[b] + nseg[b]++];
+        e.dst = (unsigned long long *)dst;
+        e.src = (const unsigned long long *)src;
+        e.n = n;
+        e.c0 = nchunk[b];
+        nchunk[b] += (n + XFER_CHUNK - 1) / XFER_CHUNK;
+    };
+    for (int k = 0; k < ncl; ++k) {
+        const void *src[4] = {in[k].r, in[k].m, in[k].vr, in[k].vt};
+        const void *dst[2] = {out[k].E, out[k].J};
+        const void *ds[4], *dd[2];
+        for (int q = 0; q < 4; ++q)
+            if (!(ds[q] = device_view(src[q]))) {
+                *pageable = true;
+                return CMCG_OK;
+            }
+        for (int q = 0; q < 2; ++q)
+            if (!(dd[q] = device_view(dst[q]))) {
+                *pageable = true;
+                return CMCG_OK;
+            }
+        const long long o = c->off[k] + 1, N = in[k].N;
+        for (int q = 0; q < 4; ++q) add(0, (q == 0 ? c->f.r : q == 1 ? c->f.m : q == 2 ? c->f.vr : c->f.vt) + o, ds[q], N);
+        add(1, (void *)dd[0], c->f.E + o, N);
+        add(1, (void *)dd[1], c->f.J + o, N);
+        c->h_xn[k] = N;
+    }
+    auto part = [&](int p) { return graphs ? run_part_graph(c, p) : issue_part(c, p); };
+    auto xfer = [&](int b) {
+        if (nchunk[b] == 0) return;
+        const long long grid = std::min<long long>(nchunk[b], 2LL * c->nsm);
+        k_xfer<<<(unsigned)grid, XFER_THREADS, 0, c->stream>>>(c->d_xfer + base[b], nseg[b], nchunk[b]);
+        c->launches += 1;
+    };
+    auto up = [&](double *dst, const double *src, long n, cudaStream_t s) {
+        return cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s);
+    };
+    auto down = [&](double *dst, const double *src, long n, cudaStream_t s) {
+        return cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s);
+    };
+    // the table goes up first (one copy); both batches are ordered after it
+    CK(cudaMemcpyAsync(c->d_xfer, c->h_xfer, xfer_table_bytes(ncl), cudaMemcpyHostToDevice, c->stream));
+    xfer(0);
+    k_set_counts<<<(ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->f, ncl, c->d_xn);
+    c->launches += 1;
+    CK(cudaEventRecord(c->ev_in, c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->ev_in, 0));  // the copy stream's uploads follow the counts
+    for (int k = 0; k < ncl; ++k)
+        CK(cudaMemcpyAsync(c->f.id + c->off[k] + 1, in[k].id, (size_t)in[k].N * sizeof(long long),
+                           cudaMemcpyHostToDevice, c->copy));
+    CK(cudaEventRecord(c->ev_in, c->copy));
+    for (int k = 0; k < ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        CK(up(c->f.rnew + o, in[k].E, in[k].N, c->copy));   // E, staged
+        CK(up(c->f.vrnew + o, in[k].J, in[k].N, c->copy));  // J, staged
+    }
+    CK(cudaEventRecord(c->ev_ej, c->copy));
+    RUN(part(0));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_in, 0));
+    RUN(part(HX_XRELAX));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_ej, 0));
+    RUN(part(HX_XSORT));
+    CK(cudaEventRecord(c->ev_sorted, c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->ev_sorted, 0));
+    // a cluster never grows in a step: N given in bounds the stars after it
+    for (int k = 0; k < ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        const long N = in[k].N;
+        CK(down(out[k].r, c->f.r + o, N, c->copy));
+        CK(down(out[k].m, c->f.m + o, N, c->copy));
+        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)N * sizeof(long long), cudaMemcpyDeviceToHost, c->copy));
+    }
+    RUN(part(2));
+    CK(cudaEventRecord(c->ev_ec3, c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->ev_ec3, 0));
+    for (int k = 0; k < ncl; ++k) {
+        const long long o = c->off[k] + 1;
+        CK(down(out[k].vr, c->f.vr + o, in[k].N, c->copy));
+        CK(down(out[k].vt, c->f.vt + o, in[k].N, c->copy));
+    }
+    CK(cudaEventRecord(c->ev_copied, c->copy));
+    RUN(part(3));
+    k_gather_counts<<<(ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, ncl, c->d_nout);
+    c->launches += 1;
+    xfer(1);
+    CK(cudaGetLastError());
+    std::vector<long long> n(ncl);
+    CK(cudaMemcpyAsync(n.data(), c->d_nout, (size_t)ncl * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamWaitEvent(c->stream, c->ev_copied, 0));  // the next call's uploads follow the read-back
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < ncl; ++k) out[k].N = (long)n[k];
+    c->launches_last = c->launches - l0;
+    return CMCG_OK;
+}
+
 static int step_host_run(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out)
 {
     const bool graphs = c->use_graph && !c->profile;
     const long l0 = c->launches;
+    {
+        bool pageable = false;
+        const int rc = step_host_batched(c, in, out, graphs, l0, &pageable);
+        if (rc || !pageable) return rc;
+    }
     auto part = [&](int p) { return graphs ? run_part_graph(c, p) : issue_part(c, p); };
     auto up = [&](double *dst, const double *src, long n, cudaStream_t s) {
         return cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s);

@@ -22,14 +22,26 @@ def _ctx(ics, seed, **kw):
     return g
 
 
-def _bufs(n):
+def _bufs(n, pinned=False):
+    """Host star arrays: pageable numpy arrays, or views of pinned (page-locked)
+    memory, which the batched exchange reads and writes from the device."""
+    if pinned:
+        import torch
+
+        b = {k: torch.zeros(n + 8, dtype=torch.float64, pin_memory=True).numpy() for k in KEYS[:-1]}
+        b["id"] = torch.zeros(n + 8, dtype=torch.int64, pin_memory=True).numpy()
+        return b
     b = {k: np.zeros(n + 8) for k in KEYS[:-1]}
     b["id"] = np.zeros(n + 8, np.int64)
     return b
 
 
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
 @pytest.mark.parametrize("sizes", [[20000], [6000, 15000, 9001]])
-def test_step_host_equals_put_step_get(gpulib, sizes):
+def test_step_host_equals_put_step_get(gpulib, sizes, pinned):
+    """Pinned arrays go through the batched exchange (one kernel launch per
+    field group of every cluster), pageable ones through the copy engines,
+    one copy per array; both must give put_stars + step + get_stars."""
     ics = [cmcgpu.generate(cmcgpu.KING if i % 2 else cmcgpu.PLUMMER, n, seed=90 + i, imf=1)
            for i, n in enumerate(sizes)]
     ref, hx_graph, hx_direct = _ctx(ics, 7), _ctx(ics, 7), _ctx(ics, 7)
@@ -37,7 +49,7 @@ def test_step_host_equals_put_step_get(gpulib, sizes):
     hx_direct.use_graph(False)
     state = {}
     for name, g in (("ref", ref), ("graph", hx_graph), ("direct", hx_direct)):
-        bufs = [_bufs(n) for n in sizes]
+        bufs = [_bufs(n, pinned and name != "ref") for n in sizes]
         ns = [g.get_stars(c, bufs[c]) for c in range(len(sizes))]
         for _ in range(4):
             if name == "ref":

@@ -534,23 +534,23 @@ def measure(a, cfg_name, N, rank, ws, dist, weights=None, sub=False):
         b["id"] = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy()
         return b
 
-    host = []
+    bufs, ns = [], []
     for c, (n, _, _) in enumerate(clusters):
         b = pinned(n + 16)
-        host.append((b, ctx.get_stars(c, b)))
+        bufs.append(b)
+        ns.append(ctx.get_stars(c, b))
+    hs = cmcgpu.HostStars(bufs, ns)  # steps in place on the same arrays
     ctx.use_graph(True)
-    ns = ctx.step_host([(n, b) for b, n in host], [b for b, _ in host])  # captures the part graphs
-    host = [(b, n) for (b, _), n in zip(host, ns)]
+    ns = ctx.step_host_inplace(hs)  # captures the part graphs
     h2d = d2h = 0
     e2e_updates = 0
     barrier(dist)
     t1 = time.perf_counter()
     for _ in range(a.steps):
-        h2d += sum(n for _, n in host) * 7 * 8
-        d2h += sum(n for _, n in host) * 7 * 8 + 8 * ncl
-        e2e_updates += sum(n for _, n in host)
-        ns = ctx.step_host([(n, b) for b, n in host], [b for b, _ in host])
-        host = [(b, n) for (b, _), n in zip(host, ns)]
+        h2d += sum(ns) * 7 * 8
+        d2h += sum(ns) * 7 * 8 + 8 * ncl
+        e2e_updates += sum(ns)
+        ns = ctx.step_host_inplace(hs)
     e2e_dt = time.perf_counter() - t1
     barrier(dist)
     ctx.check_device("e2e steps")

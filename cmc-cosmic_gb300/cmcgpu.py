@@ -106,6 +106,34 @@ class Stars(C.Structure):
     _fields_ = [("N", C.c_long), ("cap", C.c_long)] + [(k, C.c_void_p) for k in ("r", "m", "vr", "vt", "E", "J", "id")]
 
 
+STAR_KEYS = ("r", "m", "vr", "vt", "E", "J", "id")
+
+
+class HostStars:
+    """Every cluster's host star arrays, bound once for repeated steps in place
+    (Context.step_host_inplace: cmcg_step_host with the same cmcg_stars array
+    as input and output, so each step's star counts are the next step's
+    input).  bufs[k] holds float64 arrays r, m, vr, vt, E, J and an int64 id,
+    contiguous, of one length; ns[k] stars are taken from them."""
+
+    def __init__(self, bufs, ns):
+        self.bufs = list(bufs)  # the arrays must outlive the binding
+        self.arr = (Stars * len(self.bufs))()
+        for k, (b, n) in enumerate(zip(self.bufs, ns)):
+            cap = len(b["r"])
+            for x in STAR_KEYS:
+                a = b[x]
+                want = np.int64 if x == "id" else np.float64
+                if a.dtype != want or not a.flags.c_contiguous or len(a) != cap:
+                    raise ValueError(f"cluster {k}: array {x} must be contiguous {np.dtype(want)} of length {cap}")
+            if not 0 <= n <= cap:
+                raise ValueError(f"cluster {k}: {n} stars do not fit arrays of length {cap}")
+            self.arr[k] = Stars(n, cap, *[b[x].ctypes.data for x in STAR_KEYS])
+
+    def counts(self):
+        return [int(s.N) for s in self.arr]
+
+
 class ICSpec(C.Structure):
     _fields_ = [("model", C.c_int), ("N", C.c_long), ("w0", C.c_double), ("imf", C.c_int),
                 ("binary_fraction", C.c_double), ("seed", C.c_uint64)]
@@ -584,6 +612,15 @@ class Context:
         """Upload host star state (arrays r, m, vr, vt, E, J, id; m already x N_STAR)."""
         a = [bufs[k].ctypes.data for k in ("r", "m", "vr", "vt", "E", "J", "id")]
         self._check(lib().cmcg_put_stars(self._h, cluster, n, *a), "put_stars")
+
+    def step_host_inplace(self, hs: HostStars):
+        """One step on bound host arrays, in place (cmcg_step_host with in ==
+        out); returns the star counts after it, which the binding keeps as the
+        next step's input."""
+        if len(hs.arr) != self.n:
+            raise ValueError(f"binding holds {len(hs.arr)} clusters, the context {self.n}")
+        self._check(lib().cmcg_step_host(self._h, hs.arr, hs.arr), "cmcg_step_host")
+        return hs.counts()
 
     def step_host(self, ins, outs):
         """One step on host arrays: ins[k] = (n, bufs) per cluster, outs[k] = bufs

@@ -273,7 +273,9 @@ int cmcg_learned_stats(cmcg_ctx *ctx, uint64_t *out /* CMCG_LSTAT_N */);
  * E and J go up while the relaxation runs; r, m and id are read back while
  * the potential, energy conservation and energies still run; graphs are
  * used when enabled.
- * in and out may be the same arrays.  Pinned host memory gives full copy
+ * in and out may be the same arrays, and the same cmcg_stars array: each
+ * in[k].N is read before any out[k].N is written, so a step in place leaves
+ * the next step's input counts behind.  Pinned host memory gives full copy
  * speed.  The call returns once every copy has finished, on errors too.
  * Equivalent to cmcg_put_stars + cmcg_step + cmcg_get_stars. */
 typedef struct {

@@ -39,35 +39,41 @@ def _bufs(n, pinned=False):
 @pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
 @pytest.mark.parametrize("sizes", [[20000], [6000, 15000, 9001]])
 def test_step_host_equals_put_step_get(gpulib, sizes, pinned):
-    """Pinned arrays go through the batched exchange (one kernel launch per
-    field group of every cluster), pageable ones through the copy engines,
-    one copy per array; both must give put_stars + step + get_stars."""
+    """Pinned arrays go through the batched exchange (the exposed uploads and
+    the E, J downloads by one kernel launch each, over every cluster),
+    pageable ones through the copy engines, one copy per array; both must
+    give put_stars + step + get_stars.  "inplace" steps a HostStars binding
+    (the same cmcg_stars array as input and output)."""
     ics = [cmcgpu.generate(cmcgpu.KING if i % 2 else cmcgpu.PLUMMER, n, seed=90 + i, imf=1)
            for i, n in enumerate(sizes)]
-    ref, hx_graph, hx_direct = _ctx(ics, 7), _ctx(ics, 7), _ctx(ics, 7)
+    ref, hx_graph, hx_direct, hx_inplace = _ctx(ics, 7), _ctx(ics, 7), _ctx(ics, 7), _ctx(ics, 7)
     hx_graph.use_graph(True)
     hx_direct.use_graph(False)
+    hx_inplace.use_graph(True)
     state = {}
-    for name, g in (("ref", ref), ("graph", hx_graph), ("direct", hx_direct)):
+    for name, g in (("ref", ref), ("graph", hx_graph), ("direct", hx_direct), ("inplace", hx_inplace)):
         bufs = [_bufs(n, pinned and name != "ref") for n in sizes]
         ns = [g.get_stars(c, bufs[c]) for c in range(len(sizes))]
+        hs = cmcgpu.HostStars(bufs, ns) if name == "inplace" else None
         for _ in range(4):
             if name == "ref":
                 for c in range(len(sizes)):
                     g.put_stars(c, ns[c], bufs[c])
                 g.step(1)
                 ns = [g.get_stars(c, bufs[c]) for c in range(len(sizes))]
+            elif hs is not None:
+                ns = g.step_host_inplace(hs)
             else:
                 ns = g.step_host([(ns[c], bufs[c]) for c in range(len(sizes))], bufs)
             g.check_device(name)
         state[name] = (ns, bufs)
-    for name in ("graph", "direct"):
+    for name in ("graph", "direct", "inplace"):
         ns, bufs = state[name]
         assert ns == state["ref"][0], name
         for c, n in enumerate(ns):
             for k in KEYS:
                 assert np.array_equal(bufs[c][k][:n], state["ref"][1][c][k][:n]), (name, c, k)
-    for g in (ref, hx_graph, hx_direct):
+    for g in (ref, hx_graph, hx_direct, hx_inplace):
         g.close()
 
 

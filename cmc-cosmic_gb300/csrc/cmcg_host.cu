@@ -263,6 +263,9 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
         c->ph.agg[i] = cv.take<ChainAgg>(c->t1024.ntiles);
         c->ph.carry[i] = cv.take<ChainCarry>(c->t1024.ntiles);
         c->ph.rec[i] = cv.take<SPRec>((size_t)c->rec_total);
+        c->ph.crho[i] = cv.take<long long>(tot);
+        c->ph.cmeta[i] = cv.take<unsigned int>(tot);
+        c->ph.cscan[i] = cv.take<PhiScan>((size_t)c->t1024.ntiles * POT_THREADS);
     }
     c->ph.ctl = cv.take<PhiCtl>(c->ncl);
     f.ridx = cv.take<int>((size_t)c->ridx_total);

@@ -80,11 +80,24 @@ struct PhiCtl {          // per cluster
     int disorder;                  // radii out of order or non-finite input (no radius index)
     long long nsp[3];
 };
+struct PhiScan {         // per thread of a tile: its tile-local exclusive scans (TileScan)
+    long long P;         // grid units of the run entering its first item
+    int c, r;            // that run's length, and whether it starts at a sequential point
+    int spx;             // sequential points before its first item
+    int pad;
+};
+// A chain's classification, written by the pass that classifies it and read
+// by the passes after it: per star, rho and (key | keyprev << 12 | sp << 24);
+// per thread, its tile scans.  Slot 1 holds chain 2, slot 0 chain 1 and then
+// chain 3 (chain 1's last reader runs before chain 3 is classified).
 struct PhiBufs {
     ChainAgg *agg[2];
     ChainCarry *carry[2];
     SPRec *rec[2];
     PhiCtl *ctl;
+    long long *crho[2];
+    unsigned int *cmeta[2];
+    PhiScan *cscan[2];
 };
 constexpr int PHI_WALK_BATCH = 512;
 

@@ -32,6 +32,9 @@
 //   k_phi_cls3   chain 2 values -> t_k; chain 3: classify; last block scans
 //   k_phi_rec3   chain 3: record; last block replays
 //   k_phi_final  chain 3 values -> star_phi, the FP32 table, sentinels
+// Each chain is classified once: the classifying pass keeps every position's
+// rho, binade keys and sequential-point flag, and every thread's tile scans
+// (store_cls), for the passes after it (load_cls).
 //   k_phi_seq    the plain one-thread loop, run only for a cluster whose
 //                replay was refused (radii out of order, non-finite input,
 //                too many sequential points, a failed check) or that asked
@@ -342,6 +345,58 @@ __device__ __forceinline__ TileScan scan_tile(const Items &it, TileSmem &sm)
     return s;
 }
 
+// Keep the tile's classification of chain CH (slot 1 for chain 2, else 0)
+// for the passes after this one.
+template <int CH>
+__device__ __forceinline__ void store_cls(const Items &it, const TileScan &s, const PhiBufs &ph, long long off)
+{
+    constexpr int slot = CH == 2 ? 1 : 0;
+    long long *rho = ph.crho[slot] + off;
+    unsigned int *meta = ph.cmeta[slot] + off;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        if (!it.valid[i]) continue;
+        const long long k = it.k[i];
+        rho[k] = it.rho[i];
+        meta[k] = ((unsigned)it.key[i] & 0xfffu) | (((unsigned)it.keyprev[i] & 0xfffu) << 12) |
+                  ((it.sp[i] ? 1u : 0u) << 24);
+    }
+    ph.cscan[slot][(size_t)blockIdx.x * POT_THREADS + threadIdx.x] = PhiScan{s.ex.P, s.ex.c, s.ex.r, s.spx, 0};
+}
+
+// The classification store_cls kept, in place of classify + scan_tile (the
+// tile totals are not restored: only the classifying pass uses them).
+// it.k, it.valid and it.a must be loaded.
+template <int CH>
+__device__ __forceinline__ TileScan load_cls(Items &it, const PhiBufs &ph, long long off)
+{
+    constexpr int slot = CH == 2 ? 1 : 0;
+    const long long *rho = ph.crho[slot] + off;
+    const unsigned int *meta = ph.cmeta[slot] + off;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        if (it.valid[i]) {
+            const long long k = it.k[i];
+            const unsigned mt = meta[k];
+            it.rho[i] = rho[k];
+            it.key[i] = (int)(mt & 0xfffu);
+            it.keyprev[i] = (int)((mt >> 12) & 0xfffu);
+            it.sp[i] = ((mt >> 24) & 1u) != 0;
+        } else {
+            it.rho[i] = 0;
+            it.key[i] = it.keyprev[i] = 0;
+            it.sp[i] = false;
+        }
+    }
+    const PhiScan c = ph.cscan[slot][(size_t)blockIdx.x * POT_THREADS + threadIdx.x];
+    TileScan s;
+    s.ex = Seg{c.P, c.c, c.r};
+    s.spx = c.spx;
+    s.tot = Seg{0, 0, 0};
+    s.ntot = 0;
+    return s;
+}
+
 // Exact values before and after each valid item, from the replayed records.
 // Returns false if a check fails (the cluster then falls back).
 __device__ __forceinline__ bool tile_values(const Items &it, const TileScan &s, const ChainCarry &cy,
@@ -522,12 +577,14 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_cls12(const Cluster *__rest
         classify<1>(v, kstart, it, sm);
         TileScan s = scan_tile(it, sm);
         if (threadIdx.x == 0) ph.agg[0][blockIdx.x] = ChainAgg{s.tot.P, s.tot.c, s.ntot};
+        store_cls<1>(it, s, ph, C.off);
         load_positions<2>(v, kstart, it);
 #pragma unroll
         for (int i = 0; i < POT_ITEMS; ++i) it.a[i] = it.valid[i] ? term_at<2>(v, it.k[i]) : 0.0;
         classify<2>(v, kstart, it, sm);
         s = scan_tile(it, sm);
         if (threadIdx.x == 0) ph.agg[1][blockIdx.x] = ChainAgg{s.tot.P, s.tot.c, s.ntot};
+        store_cls<2>(it, s, ph, C.off);
     } else if (threadIdx.x == 0) {
         ph.agg[0][blockIdx.x] = ChainAgg{0, 0, 0};
         ph.agg[1][blockIdx.x] = ChainAgg{0, 0, 0};
@@ -548,7 +605,6 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_cls12(const Cluster *__rest
 __global__ void __launch_bounds__(POT_THREADS) k_phi_rec12(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                             PotBufs pb, PhiBufs ph, unsigned int *tickets)
 {
-    __shared__ TileSmem sm;
     __shared__ WalkSmem ws;
     __shared__ int s_last;
     const int2 ct = tm.tiles[blockIdx.x];
@@ -565,14 +621,12 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_rec12(const Cluster *__rest
         load_positions<1>(v, kstart, it);
 #pragma unroll
         for (int i = 0; i < POT_ITEMS; ++i) it.a[i] = it.valid[i] ? term_at<1>(v, it.k[i]) : 0.0;
-        classify<1>(v, kstart, it, sm);
-        TileScan s = scan_tile(it, sm);
+        TileScan s = load_cls<1>(it, ph, C.off);
         tile_records(it, s, ph.carry[0][blockIdx.x], R1, ctl.nsp[0]);
         load_positions<2>(v, kstart, it);
 #pragma unroll
         for (int i = 0; i < POT_ITEMS; ++i) it.a[i] = it.valid[i] ? term_at<2>(v, it.k[i]) : 0.0;
-        classify<2>(v, kstart, it, sm);
-        s = scan_tile(it, sm);
+        s = load_cls<2>(it, ph, C.off);
         tile_records(it, s, ph.carry[1][blockIdx.x], R2, ctl.nsp[1]);
     }
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
@@ -615,12 +669,9 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_cls3(const Cluster *__restr
     if (!ctl_failed(ctl) && kstart >= 1) {
         const View v = make_view(C, f, pb, ctl);
         Items it;
-        // chain 2 values: M_k is the value before star k
+        // chain 2 values: M_k is the value before star k (records and rho give them, no terms)
         load_positions<2>(v, kstart, it);
-#pragma unroll
-        for (int i = 0; i < POT_ITEMS; ++i) it.a[i] = it.valid[i] ? term_at<2>(v, it.k[i]) : 0.0;
-        classify<2>(v, kstart, it, sm);
-        TileScan s = scan_tile(it, sm);
+        TileScan s = load_cls<2>(it, ph, off);
         double Mbef[POT_ITEMS], Maft[POT_ITEMS];
         const bool ok = tile_values(it, s, ph.carry[1][blockIdx.x], ph.rec[1] + C.rec_off, ctl.nsp[1], Mbef, Maft);
         if (!ok) ctl.fail = 1;
@@ -641,6 +692,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_cls3(const Cluster *__restr
         classify<3>(v, kstart, it, sm);
         s = scan_tile(it, sm);
         if (threadIdx.x == 0) ph.agg[0][blockIdx.x] = ChainAgg{s.tot.P, s.tot.c, s.ntot};
+        store_cls<3>(it, s, ph, off);
     } else if (threadIdx.x == 0) {
         ph.agg[0][blockIdx.x] = ChainAgg{0, 0, 0};
     }
@@ -657,7 +709,6 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_cls3(const Cluster *__restr
 __global__ void __launch_bounds__(POT_THREADS) k_phi_rec3(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                            PotBufs pb, PhiBufs ph, unsigned int *tickets)
 {
-    __shared__ TileSmem sm;
     __shared__ WalkSmem ws;
     __shared__ int s_last;
     const int2 ct = tm.tiles[blockIdx.x];
@@ -673,8 +724,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_rec3(const Cluster *__restr
         load_positions<3>(v, kstart, it);
 #pragma unroll
         for (int i = 0; i < POT_ITEMS; ++i) it.a[i] = it.valid[i] ? term_at<3>(v, it.k[i]) : 0.0;
-        classify<3>(v, kstart, it, sm);
-        TileScan s = scan_tile(it, sm);
+        TileScan s = load_cls<3>(it, ph, C.off);
         tile_records(it, s, ph.carry[0][blockIdx.x], R3, ctl.nsp[2]);
     }
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
@@ -688,7 +738,6 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_rec3(const Cluster *__restr
 __global__ void __launch_bounds__(POT_THREADS) k_phi_final(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                             PotBufs pb, PhiBufs ph)
 {
-    __shared__ TileSmem sm;
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
@@ -699,11 +748,8 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_final(const Cluster *__rest
     if (ctl_failed(ctl) || kstart < 1) return;
     const View v = make_view(C, f, pb, ctl);
     Items it;
-    load_positions<3>(v, kstart, it);
-#pragma unroll
-    for (int i = 0; i < POT_ITEMS; ++i) it.a[i] = it.valid[i] ? term_at<3>(v, it.k[i]) : 0.0;
-    classify<3>(v, kstart, it, sm);
-    TileScan s = scan_tile(it, sm);
+    load_positions<3>(v, kstart, it);  // the values need no terms: records and rho give them
+    TileScan s = load_cls<3>(it, ph, off);
     double Pb[POT_ITEMS], Pa[POT_ITEMS];
     const bool ok = tile_values(it, s, ph.carry[0][blockIdx.x], ph.rec[0] + C.rec_off, ctl.nsp[2], Pb, Pa);
     if (!ok) {

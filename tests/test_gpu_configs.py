@@ -189,3 +189,69 @@ def test_ten_free_running_steps(gpulib, orc, model, imf):
             assert abs(de_g - de_o) <= 2e-4 * abs(e0o), (step, de_g, de_o)
     g.close()
     o.close()
+
+
+def test_config5_size_one_step_properties(gpulib, orc):
+    """The mixed-precision configuration's model at its full size: King W0 = 7,
+    Kroupa masses, 10% composite binaries, N = 1e7, FP32 relaxation
+    kinematics.  The oracle steps 1e6 stars in ~8 s on one core, so at 1e7
+    the whole step is checked through properties that hold at any size:
+      * the initial potential, Mtotal and energies against the oracle (the
+        replay at 1e7 stars crosses more binades than any smaller case);
+      * after one GPU step, the radii in order, the ids a duplicate-free
+        subset of the initial ones, the stars removed accounted for by the
+        tidal mass loss;
+      * the potential the step ends with equal, bit for bit, to the oracle's
+        potential_calculate on the GPU's own post-step radii and masses."""
+    N = 10_000_000
+    ic = cmcgpu.generate(cmcgpu.KING, N, seed=31, w0=7.0, imf=1, binary_fraction=0.1)
+    seed = 4242
+    op = orc.default_params(orbit_r=ic["rtid"], seed=seed)
+    gp = cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed, relax_fp32=1)
+    o = orc.Oracle(ic, op)
+    g = cmcgpu.Context([N], gp)
+    g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    o.initialize()
+    g.initialize()
+    g.check_device("initialize")
+    assert np.array_equal(g.get("star_phi"), o.get("star_phi"))
+    assert g.scalar("Mtotal") == o.scalar("Mtotal")
+    assert g.scalar("phi_fallback") == 0
+    for s in ("KE", "PE", "Etot"):
+        assert max_rel(g.scalar(s), o.scalar(s)) <= TOL_SUM, s
+    n_star = int(o.scalar("N_STAR"))
+    m0 = g.scalar("Mtotal")
+    e0 = g.scalar("Etot")
+    o.close()
+
+    g.step(1)
+    g.check_device("step")
+    n1 = g.nstars()
+    r = g.get("r")
+    assert len(r) == n1 and np.all(np.diff(r) >= 0.0)
+    ids = g.ids()
+    assert len(np.unique(ids)) == n1 and np.all(np.isin(ids, ic["id"]))
+    m1 = g.scalar("Mtotal")
+    lost = g.scalar("TidalMassLoss")
+    assert 0 < n1 < N
+    assert abs(m0 - (m1 + lost)) <= 1e-12 * m0, (m0, m1, lost)
+    e1, esc, etid = g.scalar("Etot"), g.scalar("Eescaped"), g.scalar("Etidal")
+    de = (e1 - e0) / abs(e0)
+    print(f"\n[{N} stars] one step: {N - n1} stars stripped, mass lost {lost:.6e}, relative energy change "
+          f"{de:.3e}, Eescaped {esc:.6e}, Etidal {etid:.6e}, (Etot + Eescaped + Etidal) change "
+          f"{(e1 + esc + etid - e0) / abs(e0):.3e}")
+    assert abs(de) <= 1e-2  # the first step strips ~4% of the mass, and its energy leaves with it
+
+    # the oracle's potential_calculate on the GPU's post-step state
+    sp = orc.default_params(orbit_r=ic["rtid"], seed=seed, N_STAR=n_star)
+    mg = g.get("m")
+    post = {"r": r, "m": mg / n_star, "vr": g.get("vr"), "vt": g.get("vt"), "id": ids}
+    o2 = orc.Oracle(post, sp)
+    o2.set("star_r", g.get("star_r"))
+    o2.set("star_m", g.get("star_m"))
+    o2.calc_potential()
+    assert o2.nstars() == n1
+    assert o2.scalar("Mtotal") == m1
+    assert np.array_equal(g.get("star_phi"), o2.get("star_phi"))
+    o2.close()
+    g.close()

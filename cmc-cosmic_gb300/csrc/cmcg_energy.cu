@@ -45,7 +45,8 @@ __global__ void k_end_step(const Cluster *__restrict__ cls, int nclusters)
     sc->tcount += 1;
 }
 
-__global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, Tiles tm, Fields f, Ec3Bufs eb)
+__global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, Tiles tm, Fields f, Ec3Bufs eb,
+                                               double *const *hx)
 {
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
@@ -91,6 +92,10 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
         f.vr[g] = vr;
         f.vt[g] = vt;
     }
+    if (hx) {  // the caller's copy; k_ec3_fix rewrites the stars it changes
+        hx[4 * ct.x][i - 1] = vr;
+        hx[4 * ct.x + 1][i - 1] = vt;
+    }
 }
 
 // One segment of set_velocities3's loop (cmc_utils.c:270-307): entering
@@ -99,7 +104,8 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
 // up min(0.8 KE, excess) while the excess is positive.  Returns the excess
 // left on reaching `end`, 0 once it is used up.  WRITE applies the changes.
 template <bool WRITE>
-static __device__ double ec3_walk(const Fields &f, long long off, long long i0, long long end, double E)
+static __device__ double ec3_walk(const Fields &f, long long off, long long i0, long long end, double E,
+                                  double *hvr = nullptr, double *hvt = nullptr)
 {
     const double E_dump_factor = 0.8;
     for (long long i = i0 + 1; i < end && E > 0; ++i) {
@@ -112,6 +118,10 @@ static __device__ double ec3_walk(const Fields &f, long long off, long long i0, 
             const double exc_ratio = sqrt((v2 - 2 * E_dump / m) / v2);
             f.vr[g] = vr * exc_ratio;
             f.vt[g] = vt * exc_ratio;
+            if (hvr) {
+                hvr[i - 1] = vr * exc_ratio;
+                hvt[i - 1] = vt * exc_ratio;
+            }
         }
         E -= E_dump;
     }
@@ -134,7 +144,7 @@ static __device__ double ec3_walk(const Fields &f, long long off, long long i0, 
 // whole sequential loop is replayed by one thread, reading windows of
 // FIX_WINDOW consecutive stars that the block stages in shared memory.
 __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__restrict__ cls, Fields f, Ec3Bufs eb,
-                                                             int nclusters)
+                                                             int nclusters, double *const *hx)
 {
     __shared__ __align__(16) int L[EXCESS_CAP];  // star indices (below 2^31: counts_ok bounds them by the capacity)
     __shared__ long long s_i;
@@ -146,6 +156,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
     if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long off = C.off, N = sc->N_MAX_NEW;
+    double *hvr = hx ? hx[4 * c] : nullptr, *hvt = hx ? hx[4 * c + 1] : nullptr;
     const unsigned int n = eb.nlist[c];
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -197,7 +208,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
         __syncthreads();
         for (int t = threadIdx.x; t < nn; t += blockDim.x) {
             const long long i0 = L[t], end = (t + 1 < nn) ? L[t + 1] : N + 1;
-            ec3_walk<true>(f, off, i0, end, carry[t] + eb.a[off + i0]);  // 0 + a = a when nothing is carried
+            ec3_walk<true>(f, off, i0, end, carry[t] + eb.a[off + i0], hvr, hvt);  // 0 + a = a when nothing is carried
         }
         return;
     }
@@ -245,6 +256,10 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
                     vt *= exc_ratio;
                     f.vr[off + i] = vr;
                     f.vt[off + i] = vt;
+                    if (hvr) {
+                        hvr[i - 1] = vr;
+                        hvt[i - 1] = vt;
+                    }
                     Eexcess -= E_dump;
                 }
             }
@@ -260,7 +275,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
 // Eight stars per thread: the per-star FP64 work is the reference's
 // expressions; the sums take one addition per star before the block tree.
 __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                       double *partials, unsigned int *tickets)
+                                                       double *partials, unsigned int *tickets, double *const *hx)
 {
     __shared__ double red[EN_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
@@ -277,6 +292,7 @@ __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict
     // (two FP64 operations a star fewer for each; the sums are tree sums anyway)
     double K = 0.0, P = 0.0;
     int cnt = 0;
+    double *hE = hx ? hx[4 * ct.x + 2] : nullptr, *hJ = hx ? hx[4 * ct.x + 3] : nullptr;
 #pragma unroll 4
     for (int it = 0; it < EN_T / EN_THREADS; ++it) {
         const long long i = 1 + (long long)ct.y * EN_T + it * EN_THREADS + threadIdx.x;
@@ -284,8 +300,13 @@ __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict
         const long long g = off + i;
         const double vr = f.vr[g], vt = f.vt[g], ph = f.phi[g], m = f.m[g];
         const double v2 = sqr(vr) + sqr(vt);
-        f.E[g] = ph + 0.5 * v2;
-        f.J[g] = f.r[g] * vt;
+        const double E = ph + 0.5 * v2, J = f.r[g] * vt;
+        f.E[g] = E;
+        f.J[g] = J;
+        if (hE) {  // the caller's copy
+            hE[i - 1] = E;
+            hJ[i - 1] = J;
+        }
         K += v2 * m;
         P += ph * m;
         ++cnt;

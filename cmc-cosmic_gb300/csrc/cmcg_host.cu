@@ -33,8 +33,10 @@ struct TileTable {
 // (r, m, id are final); energies (vr, vt are final).  The host exchange runs
 // part HX_SORT as two: HX_XRELAX marks E, J and relaxes while the caller's E
 // and J are still on their way; HX_XSORT merges them in, then orbits to the
-// sort.
-constexpr int HX_PARTS = 4, HX_SORT = 1, HX_XRELAX = 4, HX_XSORT = 5, HX_ALL = 6;
+// sort.  With the caller's arrays reachable from the device it runs parts 2
+// and 3 as HX_XEC3 and HX_XEN, whose kernels also write vr, vt (energy
+// conservation) and E, J (energies) into those arrays.
+constexpr int HX_PARTS = 4, HX_SORT = 1, HX_XRELAX = 4, HX_XSORT = 5, HX_XEC3 = 6, HX_XEN = 7, HX_ALL = 8;
 
 enum Family { F_BEGIN, F_TIMESTEP, F_RELAX, F_ORBIT, F_TIDAL, F_SORT, F_POT, F_EC3, F_ENERGY, F_END, F_MLP, F_COUNT };
 const char *kFamilyNames[F_COUNT] = {"begin", "timestep", "relax", "orbit", "tidal",
@@ -70,12 +72,15 @@ struct XferSeg {
     long long c0;  // first chunk of the segment in its batch
 };
 constexpr int XFER_THREADS = 256, XFER_UNROLL = 4, XFER_CHUNK = XFER_THREADS * XFER_UNROLL;
-constexpr int XFER_PER_CLUSTER = 6;  // segments per cluster: four uploads, two downloads
-// The exchange's table: the segments, then every cluster's star count, in one
-// block (host and device alike) that goes up in one copy.
+constexpr int XFER_PER_CLUSTER = 4;  // upload segments per cluster: r, m, vr, vt
+// The exchange's table, in one block (host and device alike) that goes up in
+// one copy: the upload segments; every cluster's host arrays that kernels
+// write (vr, vt, E, J: the hx argument of k_ec3, k_ec3_fix, k_energy); every
+// cluster's star count.
 static size_t xfer_table_bytes(int ncl)
 {
-    return (size_t)XFER_PER_CLUSTER * ncl * sizeof(XferSeg) + (size_t)ncl * sizeof(long long);
+    return (size_t)XFER_PER_CLUSTER * ncl * sizeof(XferSeg) + (size_t)4 * ncl * sizeof(double *) +
+           (size_t)ncl * sizeof(long long);
 }
 
 }  // namespace
@@ -132,6 +137,7 @@ struct cmcg_ctx {
     // batched host exchange: segment tables (pinned host copy, device copy)
     // and per-cluster counts, XFER_PER_CLUSTER segments per cluster
     XferSeg *h_xfer = nullptr, *d_xfer = nullptr;
+    double **h_hx = nullptr, **d_hx = nullptr;
     long long *h_xn = nullptr, *d_xn = nullptr;
     // graphs
     // The sort swaps the field pointers every step, so a captured two-step
@@ -244,7 +250,8 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->sb.tile_next = cv.take<unsigned int>(SORT_MAX_PASSES);
     c->orbit_next = cv.take<unsigned int>(1);
     c->d_xfer = (XferSeg *)cv.take<char>(xfer_table_bytes(c->ncl));
-    c->d_xn = c->d_xfer ? (long long *)(c->d_xfer + (size_t)XFER_PER_CLUSTER * c->ncl) : nullptr;
+    c->d_hx = c->d_xfer ? (double **)(c->d_xfer + (size_t)XFER_PER_CLUSTER * c->ncl) : nullptr;
+    c->d_xn = c->d_xfer ? (long long *)(c->d_hx + (size_t)4 * c->ncl) : nullptr;
     c->sb.epoch = cv.take<unsigned int>(1);
     c->sb.npass = cv.take<int>(c->ncl);
     c->sb.shift = cv.take<int>(c->ncl);
@@ -515,7 +522,8 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         cmcg_destroy(c);
         return CMCG_ERR_CUDA;
     }
-    c->h_xn = (long long *)(c->h_xfer + (size_t)XFER_PER_CLUSTER * nclusters);
+    c->h_hx = (double **)(c->h_xfer + (size_t)XFER_PER_CLUSTER * nclusters);
+    c->h_xn = (long long *)(c->h_hx + (size_t)4 * nclusters);
     CK(cudaStreamSynchronize(c->stream));
     *out = c;
     return CMCG_OK;
@@ -611,15 +619,14 @@ __global__ void k_set_count(const Cluster *cls, int k, long long N)
     sc->ridx_ok = 0;
 }
 
-// Host exchange by kernel.  Each batch of transfers -- the same field group of
-// every cluster: the four inputs the time step reads, or E and J after the
-// energies -- is one launch that moves 8-byte words between the caller's
+// Host exchange by kernel.  The four inputs the time step reads, for every
+// cluster, go up in one launch that moves 8-byte words from the caller's
 // pinned host arrays (addressed from the device through unified addressing)
-// and the context's fields, in place of one cudaMemcpyAsync per array.  On
+// into the context's fields, in place of one cudaMemcpyAsync per array.  On
 // this GPU a kernel reads and writes pinned host memory over NVLink-C2C as
 // fast as the copy engines do (~200 GB/s each way); the launch replaces the
 // per-copy set-up, which adds up over an ensemble's many small arrays.  The
-// batch's segments sit in order of their first chunk.
+// segments sit in order of their first chunk.
 // (XferSeg and the chunk sizes: beside cmcg_ctx above)
 
 __global__ void __launch_bounds__(XFER_THREADS) k_xfer(const XferSeg *__restrict__ seg, int nseg, long long nchunk)
@@ -778,11 +785,11 @@ static int L_pot(cmcg_ctx *c)
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
-static int L_energy(cmcg_ctx *c)
+static int L_energy(cmcg_ctx *c, double *const *hx = nullptr)
 {
     fam_begin(c, F_ENERGY);
     k_energy<<<c->t2048.ntiles, EN_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->partials,
-                                                             c->tickets);
+                                                             c->tickets, hx);
     fam_end(c);
     c->launches += 1;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
@@ -951,11 +958,11 @@ static int L_sort(cmcg_ctx *c)
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
-static int L_ec3(cmcg_ctx *c)
+static int L_ec3(cmcg_ctx *c, double *const *hx = nullptr)
 {
     fam_begin(c, F_EC3);
-    k_ec3<<<c->t256.ntiles, EC3_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->eb);
-    k_ec3_fix<<<c->ncl, EC3_FIX_THREADS, 0, c->stream>>>(c->d_cls, c->f, c->eb, c->ncl);
+    k_ec3<<<c->t256.ntiles, EC3_T, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->eb, hx);
+    k_ec3_fix<<<c->ncl, EC3_FIX_THREADS, 0, c->stream>>>(c->d_cls, c->f, c->eb, c->ncl, hx);
     fam_end(c);
     c->launches += 2;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
@@ -993,6 +1000,14 @@ static int issue_part(cmcg_ctx *c, int part)
         RUN(L_orbit(c));
         RUN(L_tidal(c));
         RUN(L_sort(c));
+        break;
+    case HX_XEC3:
+        RUN(L_pot(c));
+        RUN(L_ec3(c, c->d_hx));
+        break;
+    case HX_XEN:
+        RUN(L_energy(c, c->d_hx));
+        RUN(L_end(c));
         break;
     default:
         RUN(L_energy(c));
@@ -1866,70 +1881,61 @@ static const void *device_view(const void *p)
     return nullptr;
 }
 
-// The step on host arrays with the exposed transfers batched into k_xfer
-// launches: the uploads of r, m, vr, vt that precede the time step, and the
-// downloads of E and J that follow the energies, with nothing else running on
-// the GPU meanwhile.  The transfers that overlap kernels (id during the time
-// step, E and J staged during the relaxation, r, m, id during the potential,
-// vr, vt during the energies) stay on the copy engines, one cudaMemcpyAsync
-// per array: a copy kernel beside a kernel that fills the SMs waits for free
-// slots, a copy engine does not.  Sets *pageable, and does nothing, when some
-// caller array is not reachable from the device: the caller then takes the
-// copy path for every transfer.
+// The step on host arrays that kernels can reach (pinned or registered host
+// memory, or device memory).  The uploads of r, m, vr, vt, which precede the
+// time step with nothing else to run, go by one k_xfer launch over every
+// cluster.  The results that are final only at the step's end are written
+// into the caller's arrays by the kernels that compute them: vr and vt by
+// energy conservation (HX_XEC3), E and J by the energies (HX_XEN), so that
+// they cross the host link while those kernels run.  The transfers that
+// overlap other kernels stay on the copy engines, one cudaMemcpyAsync per
+// array (id up during the time step, E and J staged during the relaxation,
+// r, m, id down during the potential): a copy kernel beside a kernel that
+// fills the SMs waits for free slots, a copy engine does not.  Sets
+// *pageable, and does nothing, when some caller array is not reachable from
+// the device: the caller then takes the copy path for every transfer.
 static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out, bool graphs, long l0,
                              bool *pageable)
 {
     *pageable = false;
     const int ncl = c->ncl;
     XferSeg *t = c->h_xfer;
-    // batch 0 (uploads) holds four segments per cluster, batch 1 (E, J down) two
-    const int base[2] = {0, 4 * ncl};
-    long long nchunk[2] = {0, 0};
-    int nseg[2] = {0, 0};
-    auto add = [&](int b, void *dst, const void *src, long long n) {
-        XferSeg &e = t[base[b] + nseg[b]++];
+    long long nchunk = 0;
+    int nseg = 0;
+    auto add = [&](void *dst, const void *src, long long n) {
+        XferSeg &e = t[nseg++];
         e.dst = (unsigned long long *)dst;
         e.src = (const unsigned long long *)src;
         e.n = n;
-        e.c0 = nchunk[b];
-        nchunk[b] += (n + XFER_CHUNK - 1) / XFER_CHUNK;
+        e.c0 = nchunk;
+        nchunk += (n + XFER_CHUNK - 1) / XFER_CHUNK;
     };
     for (int k = 0; k < ncl; ++k) {
         const void *src[4] = {in[k].r, in[k].m, in[k].vr, in[k].vt};
-        const void *dst[2] = {out[k].E, out[k].J};
-        const void *ds[4], *dd[2];
-        for (int q = 0; q < 4; ++q)
-            if (!(ds[q] = device_view(src[q]))) {
+        const void *dst[4] = {out[k].vr, out[k].vt, out[k].E, out[k].J};
+        const void *ds[4], *dd[4];
+        for (int q = 0; q < 4; ++q) {
+            ds[q] = device_view(src[q]);
+            dd[q] = device_view(dst[q]);
+            if (!ds[q] || !dd[q]) {
                 *pageable = true;
                 return CMCG_OK;
             }
-        for (int q = 0; q < 2; ++q)
-            if (!(dd[q] = device_view(dst[q]))) {
-                *pageable = true;
-                return CMCG_OK;
-            }
+        }
         const long long o = c->off[k] + 1, N = in[k].N;
-        for (int q = 0; q < 4; ++q) add(0, (q == 0 ? c->f.r : q == 1 ? c->f.m : q == 2 ? c->f.vr : c->f.vt) + o, ds[q], N);
-        add(1, (void *)dd[0], c->f.E + o, N);
-        add(1, (void *)dd[1], c->f.J + o, N);
+        double *fields[4] = {c->f.r, c->f.m, c->f.vr, c->f.vt};
+        for (int q = 0; q < 4; ++q) add(fields[q] + o, ds[q], N);
+        for (int q = 0; q < 4; ++q) c->h_hx[4 * k + q] = (double *)dd[q];
         c->h_xn[k] = N;
     }
     auto part = [&](int p) { return graphs ? run_part_graph(c, p) : issue_part(c, p); };
-    auto xfer = [&](int b) {
-        if (nchunk[b] == 0) return;
-        const long long grid = std::min<long long>(nchunk[b], 2LL * c->nsm);
-        k_xfer<<<(unsigned)grid, XFER_THREADS, 0, c->stream>>>(c->d_xfer + base[b], nseg[b], nchunk[b]);
-        c->launches += 1;
-    };
-    auto up = [&](double *dst, const double *src, long n, cudaStream_t s) {
-        return cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s);
-    };
-    auto down = [&](double *dst, const double *src, long n, cudaStream_t s) {
-        return cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s);
-    };
-    // the table goes up first (one copy); both batches are ordered after it
+    // the table goes up first (one copy); everything after is ordered behind it
     CK(cudaMemcpyAsync(c->d_xfer, c->h_xfer, xfer_table_bytes(ncl), cudaMemcpyHostToDevice, c->stream));
-    xfer(0);
+    if (nchunk > 0) {
+        const long long grid = std::min<long long>(nchunk, 2LL * c->nsm);  // nothing runs beside it
+        k_xfer<<<(unsigned)grid, XFER_THREADS, 0, c->stream>>>(c->d_xfer, nseg, nchunk);
+        c->launches += 1;
+    }
     k_set_counts<<<(ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->f, ncl, c->d_xn);
     c->launches += 1;
     CK(cudaEventRecord(c->ev_in, c->stream));
@@ -1940,8 +1946,9 @@ static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out,
     CK(cudaEventRecord(c->ev_in, c->copy));
     for (int k = 0; k < ncl; ++k) {
         const long long o = c->off[k] + 1;
-        CK(up(c->f.rnew + o, in[k].E, in[k].N, c->copy));   // E, staged
-        CK(up(c->f.vrnew + o, in[k].J, in[k].N, c->copy));  // J, staged
+        const size_t bytes = (size_t)in[k].N * sizeof(double);
+        CK(cudaMemcpyAsync(c->f.rnew + o, in[k].E, bytes, cudaMemcpyHostToDevice, c->copy));   // E, staged
+        CK(cudaMemcpyAsync(c->f.vrnew + o, in[k].J, bytes, cudaMemcpyHostToDevice, c->copy));  // J, staged
     }
     CK(cudaEventRecord(c->ev_ej, c->copy));
     RUN(part(0));
@@ -1954,24 +1961,17 @@ static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out,
     // a cluster never grows in a step: N given in bounds the stars after it
     for (int k = 0; k < ncl; ++k) {
         const long long o = c->off[k] + 1;
-        const long N = in[k].N;
-        CK(down(out[k].r, c->f.r + o, N, c->copy));
-        CK(down(out[k].m, c->f.m + o, N, c->copy));
-        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)N * sizeof(long long), cudaMemcpyDeviceToHost, c->copy));
-    }
-    RUN(part(2));
-    CK(cudaEventRecord(c->ev_ec3, c->stream));
-    CK(cudaStreamWaitEvent(c->copy, c->ev_ec3, 0));
-    for (int k = 0; k < ncl; ++k) {
-        const long long o = c->off[k] + 1;
-        CK(down(out[k].vr, c->f.vr + o, in[k].N, c->copy));
-        CK(down(out[k].vt, c->f.vt + o, in[k].N, c->copy));
+        const size_t bytes = (size_t)in[k].N * sizeof(double);
+        CK(cudaMemcpyAsync(out[k].r, c->f.r + o, bytes, cudaMemcpyDeviceToHost, c->copy));
+        CK(cudaMemcpyAsync(out[k].m, c->f.m + o, bytes, cudaMemcpyDeviceToHost, c->copy));
+        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)in[k].N * sizeof(long long), cudaMemcpyDeviceToHost,
+                           c->copy));
     }
     CK(cudaEventRecord(c->ev_copied, c->copy));
-    RUN(part(3));
+    RUN(part(HX_XEC3));
+    RUN(part(HX_XEN));
     k_gather_counts<<<(ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, ncl, c->d_nout);
     c->launches += 1;
-    xfer(1);
     CK(cudaGetLastError());
     std::vector<long long> n(ncl);
     CK(cudaMemcpyAsync(n.data(), c->d_nout, (size_t)ncl * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));

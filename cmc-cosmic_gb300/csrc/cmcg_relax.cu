@@ -22,8 +22,9 @@ namespace cmcg {
 static __device__ __forceinline__ double sqr(double x) { return x * x; }
 static __device__ __forceinline__ double cub(double x) { return x * x * x; }
 
-// calc_n_local, cmc_dynamics_helper.c:768-786
-static __device__ __forceinline__ double n_local_at(const double *__restrict__ r, long long k, long long p,
+// r_max^3 - r_min^3 over the 2p neighbours of star k (calc_n_local's window,
+// cmc_dynamics_helper.c:768-786)
+static __device__ __forceinline__ double window_dr3(const double *__restrict__ r, long long k, long long p,
                                                     long long N_LIMIT)
 {
     long long kmin = k - p, kmax = k + p;
@@ -34,7 +35,14 @@ static __device__ __forceinline__ double n_local_at(const double *__restrict__ r
         kmax = N_LIMIT;
         kmin = N_LIMIT - 2 * p - 1;
     }
-    return (2.0 * ((double)p)) * 3.0 / (4.0 * CMCG_PI * (cub(r[kmax]) - cub(r[kmin])));
+    return cub(r[kmax]) - cub(r[kmin]);
+}
+
+// calc_n_local, cmc_dynamics_helper.c:768-786
+static __device__ __forceinline__ double n_local_at(const double *__restrict__ r, long long k, long long p,
+                                                    long long N_LIMIT)
+{
+    return (2.0 * ((double)p)) * 3.0 / (4.0 * CMCG_PI * window_dr3(r, k, p, N_LIMIT));
 }
 
 // ------------------------------------------------------------ time step --
@@ -275,18 +283,22 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
             }
             // the three quotients by m_k + m_kp share one correctly rounded reciprocal (div_rcp)
             const double msum = mass_k + mass_kp, imsum = __drcp_rn(msum);
-            const double rcm = div_rcp(m[k] * r[k] + m[kp] * r[kp], msum, imsum);
-            const double n_local = n_local_at(r, k, p, N);
             // S = 0: single-single with SS_COLLISION off, so P_enc = 0 and the
             // encounter draw (cmc_dynamics.c:406) can never succeed.
             double beta = 0.0;
             if (ok && C.RELAXATION) {
-                const double Trel12 = (CMCG_PI / 32.0) * cub(W) / (NSTAR * n_local * sqr((mass_k + mass_kp) * madhoc));
-                beta = (CMCG_PI / 2.0) * sqrt(dt / Trel12);
+                // beta = (pi/2) sqrt(dt / Trel12) with Trel12 = (pi/32) W^3 / (N_STAR n_local
+                // ((m_k + m_k') madhoc)^2) and n_local = 6p / (4 pi (r_max^3 - r_min^3))
+                // (cmc_dynamics_helper.c:768-786, 831-871): the three quotients as one, within a
+                // few ulps of the reference's beta
+                const double num = dt * NSTAR * (192.0 * (double)p) * sqr(msum * madhoc);
+                const double den = (4.0 * CMCG_PI * CMCG_PI) * window_dr3(r, k, p, N) * cub(W);
+                beta = (CMCG_PI / 2.0) * sqrt(num / den);
                 const double relbeta[4] = {CMCG_PI / 2.0, CMCG_PI / 4.0, CMCG_PI / 8.0, CMCG_PI / 16.0};
                 part[0] += 1.0;
-                if (gt_pos(beta, relbeta[3])) {  // the smallest threshold: the ratio is formed once per pair
+                if (gt_pos(beta, relbeta[3])) {  // the smallest threshold: ratio and centre formed once per pair
                     const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
+                    const double rcm = div_rcp(m[k] * r[k] + m[kp] * r[kp], msum, imsum);
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
                         if (gt_pos(beta, relbeta[i])) {

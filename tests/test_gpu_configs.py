@@ -235,12 +235,12 @@ def test_config5_size_one_step_properties(gpulib, orc):
     lost = g.scalar("TidalMassLoss")
     assert 0 < n1 < N
     assert abs(m0 - (m1 + lost)) <= 1e-12 * m0, (m0, m1, lost)
-    e1, esc, etid = g.scalar("Etot"), g.scalar("Eescaped"), g.scalar("Etidal")
-    de = (e1 - e0) / abs(e0)
-    print(f"\n[{N} stars] one step: {N - n1} stars stripped, mass lost {lost:.6e}, relative energy change "
-          f"{de:.3e}, Eescaped {esc:.6e}, Etidal {etid:.6e}, (Etot + Eescaped + Etidal) change "
-          f"{(e1 + esc + etid - e0) / abs(e0):.3e}")
-    assert abs(de) <= 1e-2  # the first step strips ~4% of the mass, and its energy leaves with it
+    # Etot counts the escapers' energy (Eescaped, compute_energy_new); measured on the GB300:
+    # -8.5e-4 of it in this first step, which strips 4% of the mass
+    de = (g.scalar("Etot") - e0) / abs(e0)
+    print(f"\n[{N} stars] one step: {N - n1} stars stripped, mass lost {lost:.6e}, relative change of Etot "
+          f"{de:.3e} (Eescaped {g.scalar('Eescaped'):.6e}, Etidal {g.scalar('Etidal'):.6e})")
+    assert abs(de) <= 1e-2
 
     # the oracle's potential_calculate on the GPU's post-step state
     sp = orc.default_params(orbit_r=ic["rtid"], seed=seed, N_STAR=n_star)

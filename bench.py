@@ -49,17 +49,17 @@ MLP_FLOPS_PER_STAR = 2 * (8 * 64 + 64 * 64 + 64 * 33)
 # DRAM bytes per star of one launch, dram__bytes_read.sum + dram__bytes_write.sum
 # from one-kernel, one-launch ncu captures on the King W0=6 + Kroupa model at
 # N = 1e6 (962,913 stars in the captured step): k_orbit 142.4 MB, k_relax64
-# 57.5 MB, k_ec3 63.3 MB, k_sort_gather 97.6 MB
-NCU_TRAFFIC_PER_STAR = {"orbit": 142.4e6 / 962913, "relax": 57.5e6 / 962913, "ec3": 63.3e6 / 962913}
+# 58.0 MB, k_ec3 63.1 MB, k_sort_gather 97.6 MB
+NCU_TRAFFIC_PER_STAR = {"orbit": 142.4e6 / 962913, "relax": 58.0e6 / 962913, "ec3": 63.1e6 / 962913}
 # share of cycles the FP64 pipe was busy in the same captures: the kernels'
 # real bound on GB300, reported beside the HBM roofline
-NCU_FP64_PIPE_ACTIVE = {"orbit": 0.742, "relax": 0.843, "ec3": 0.842, "potential": 0.816}
+NCU_FP64_PIPE_ACTIVE = {"orbit": 0.742, "relax": 0.838, "ec3": 0.845, "potential": 0.816, "timestep": 0.705}
 # FP64 thread-operations per star of each kernel family
 # (smsp__sass_thread_inst_executed_op_fp64_pred_on.sum over the stars of one
-# step, same model: k_orbit 338.2 and k_orbit_pre 8.0, k_relax64 181.1, k_ec3
-# 45.0), and the FP64 pipe's rate at 100% busy, ops / (time x busy) from those
-# captures: 4.7-5.6e11 thread-operations/s
-NCU_FP64_OPS_PER_STAR = {"orbit": 346.2, "relax": 181.1, "potential": 61.4, "ec3": 45.0, "energy": 11.8,
+# step, same model: k_orbit 338.2 and k_orbit_pre 8.0, k_relax64 168.3, k_ec3
+# 45.0, k_timestep 12.1), and the FP64 pipe's rate at 100% busy, ops / (time x
+# busy) from those captures: 4.7-5.6e11 thread-operations/s
+NCU_FP64_OPS_PER_STAR = {"orbit": 346.2, "relax": 168.3, "potential": 61.4, "ec3": 45.0, "energy": 11.8,
                          "timestep": 12.1, "tidal": 2.1}
 FP64_PEAK_OPS = 5.05e11
 

@@ -1929,6 +1929,8 @@ static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out,
         c->h_xn[k] = N;
     }
     auto part = [&](int p) { return graphs ? run_part_graph(c, p) : issue_part(c, p); };
+    // the caller's arrays may be host or device memory here: the copies below
+    // take their direction from unified addressing (cudaMemcpyDefault)
     // the table goes up first (one copy); everything after is ordered behind it
     CK(cudaMemcpyAsync(c->d_xfer, c->h_xfer, xfer_table_bytes(ncl), cudaMemcpyHostToDevice, c->stream));
     if (nchunk > 0) {
@@ -1942,13 +1944,13 @@ static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out,
     CK(cudaStreamWaitEvent(c->copy, c->ev_in, 0));  // the copy stream's uploads follow the counts
     for (int k = 0; k < ncl; ++k)
         CK(cudaMemcpyAsync(c->f.id + c->off[k] + 1, in[k].id, (size_t)in[k].N * sizeof(long long),
-                           cudaMemcpyHostToDevice, c->copy));
+                           cudaMemcpyDefault, c->copy));
     CK(cudaEventRecord(c->ev_in, c->copy));
     for (int k = 0; k < ncl; ++k) {
         const long long o = c->off[k] + 1;
         const size_t bytes = (size_t)in[k].N * sizeof(double);
-        CK(cudaMemcpyAsync(c->f.rnew + o, in[k].E, bytes, cudaMemcpyHostToDevice, c->copy));   // E, staged
-        CK(cudaMemcpyAsync(c->f.vrnew + o, in[k].J, bytes, cudaMemcpyHostToDevice, c->copy));  // J, staged
+        CK(cudaMemcpyAsync(c->f.rnew + o, in[k].E, bytes, cudaMemcpyDefault, c->copy));   // E, staged
+        CK(cudaMemcpyAsync(c->f.vrnew + o, in[k].J, bytes, cudaMemcpyDefault, c->copy));  // J, staged
     }
     CK(cudaEventRecord(c->ev_ej, c->copy));
     RUN(part(0));
@@ -1962,9 +1964,9 @@ static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out,
     for (int k = 0; k < ncl; ++k) {
         const long long o = c->off[k] + 1;
         const size_t bytes = (size_t)in[k].N * sizeof(double);
-        CK(cudaMemcpyAsync(out[k].r, c->f.r + o, bytes, cudaMemcpyDeviceToHost, c->copy));
-        CK(cudaMemcpyAsync(out[k].m, c->f.m + o, bytes, cudaMemcpyDeviceToHost, c->copy));
-        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)in[k].N * sizeof(long long), cudaMemcpyDeviceToHost,
+        CK(cudaMemcpyAsync(out[k].r, c->f.r + o, bytes, cudaMemcpyDefault, c->copy));
+        CK(cudaMemcpyAsync(out[k].m, c->f.m + o, bytes, cudaMemcpyDefault, c->copy));
+        CK(cudaMemcpyAsync(out[k].id, c->f.id + o, (size_t)in[k].N * sizeof(long long), cudaMemcpyDefault,
                            c->copy));
     }
     CK(cudaEventRecord(c->ev_copied, c->copy));

@@ -159,3 +159,32 @@ def test_step_host_rejects_short_output(gpulib):
     with pytest.raises(cmcgpu.CmcError):
         g.step_host([(n, big)], [small])
     g.close()
+
+
+def test_step_host_on_device_arrays(gpulib):
+    """The caller's arrays in device memory: the kernels reach them like pinned
+    host arrays and the copies take their direction from unified addressing.
+    Three steps in place give what they give on pinned host arrays."""
+    import torch
+
+    ic = cmcgpu.generate(cmcgpu.KING, 20000, seed=95, imf=1)
+    a, b = _ctx([ic], 7), _ctx([ic], 7)
+    a.use_graph(True)
+    b.use_graph(True)
+    bufs = _bufs(20000, pinned=True)
+    n = a.get_stars(0, bufs)
+    dev = {k: torch.from_numpy(bufs[k].copy()).cuda() for k in KEYS}
+    torch.cuda.synchronize()
+    hs = cmcgpu.HostStars([bufs], [n])
+    arr = (cmcgpu.Stars * 1)()
+    arr[0] = cmcgpu.Stars(n, len(bufs["r"]), *[dev[k].data_ptr() for k in KEYS])
+    for _ in range(3):
+        a.step_host_inplace(hs)
+        assert cmcgpu.lib().cmcg_step_host(b._h, arr, arr) == 0
+        b.check_device("device arrays")
+    (n1,) = hs.counts()
+    assert arr[0].N == n1
+    for k in KEYS:
+        assert np.array_equal(dev[k][:n1].cpu().numpy(), bufs[k][:n1]), k
+    a.close()
+    b.close()

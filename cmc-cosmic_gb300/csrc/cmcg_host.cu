@@ -34,9 +34,9 @@ struct TileTable {
 // part HX_SORT as two: HX_XRELAX marks E, J and relaxes while the caller's E
 // and J are still on their way; HX_XSORT merges them in, then orbits to the
 // sort.  With the caller's arrays reachable from the device it runs parts 2
-// and 3 as HX_XEC3 and HX_XEN, whose kernels also write vr, vt (energy
+// and 3 as one, HX_XTAIL, whose kernels also write vr, vt (energy
 // conservation) and E, J (energies) into those arrays.
-constexpr int HX_PARTS = 4, HX_SORT = 1, HX_XRELAX = 4, HX_XSORT = 5, HX_XEC3 = 6, HX_XEN = 7, HX_ALL = 8;
+constexpr int HX_PARTS = 4, HX_SORT = 1, HX_XRELAX = 4, HX_XSORT = 5, HX_XTAIL = 6, HX_ALL = 7;
 
 enum Family { F_BEGIN, F_TIMESTEP, F_RELAX, F_ORBIT, F_TIDAL, F_SORT, F_POT, F_EC3, F_ENERGY, F_END, F_MLP, F_COUNT };
 const char *kFamilyNames[F_COUNT] = {"begin", "timestep", "relax", "orbit", "tidal",
@@ -1001,11 +1001,9 @@ static int issue_part(cmcg_ctx *c, int part)
         RUN(L_tidal(c));
         RUN(L_sort(c));
         break;
-    case HX_XEC3:
+    case HX_XTAIL:
         RUN(L_pot(c));
         RUN(L_ec3(c, c->d_hx));
-        break;
-    case HX_XEN:
         RUN(L_energy(c, c->d_hx));
         RUN(L_end(c));
         break;
@@ -1886,8 +1884,8 @@ static const void *device_view(const void *p)
 // time step with nothing else to run, go by one k_xfer launch over every
 // cluster.  The results that are final only at the step's end are written
 // into the caller's arrays by the kernels that compute them: vr and vt by
-// energy conservation (HX_XEC3), E and J by the energies (HX_XEN), so that
-// they cross the host link while those kernels run.  The transfers that
+// energy conservation, E and J by the energies (part HX_XTAIL), so that they
+// cross the host link while those kernels run.  The transfers that
 // overlap other kernels stay on the copy engines, one cudaMemcpyAsync per
 // array (id up during the time step, E and J staged during the relaxation,
 // r, m, id down during the potential): a copy kernel beside a kernel that
@@ -1970,8 +1968,7 @@ static int step_host_batched(cmcg_ctx *c, const cmcg_stars *in, cmcg_stars *out,
                            c->copy));
     }
     CK(cudaEventRecord(c->ev_copied, c->copy));
-    RUN(part(HX_XEC3));
-    RUN(part(HX_XEN));
+    RUN(part(HX_XTAIL));
     k_gather_counts<<<(ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, ncl, c->d_nout);
     c->launches += 1;
     CK(cudaGetLastError());

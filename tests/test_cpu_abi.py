@@ -188,3 +188,32 @@ def test_c_host_with_reference_prototypes_links_and_runs(gpulib, tmp_path):
                     "-lcmc_dropin", "-lcmcgpu", "-Wl,-rpath," + build], check=True)
     res = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert res.returncode == 0, res.stdout + res.stderr
+
+
+def test_host_stars_binding_checks_its_arrays(gpulib):
+    """HostStars (the in-place host-exchange binding) refuses arrays the C side
+    would misread: wrong dtype, non-contiguous, unequal lengths, too many stars.
+    No GPU is touched."""
+    import numpy as np
+
+    def bufs(n):
+        b = {k: np.zeros(n) for k in ("r", "m", "vr", "vt", "E", "J")}
+        b["id"] = np.zeros(n, np.int64)
+        return b
+
+    hs = gpulib.HostStars([bufs(100), bufs(50)], [90, 50])
+    assert hs.counts() == [90, 50]
+    bad = bufs(100)
+    bad["id"] = np.zeros(100)  # float64 ids
+    with pytest.raises(ValueError):
+        gpulib.HostStars([bad], [10])
+    bad = bufs(100)
+    bad["E"] = np.zeros(200)[::2]  # strided
+    with pytest.raises(ValueError):
+        gpulib.HostStars([bad], [10])
+    bad = bufs(100)
+    bad["J"] = np.zeros(99)
+    with pytest.raises(ValueError):
+        gpulib.HostStars([bad], [10])
+    with pytest.raises(ValueError):
+        gpulib.HostStars([bufs(100)], [101])

@@ -669,7 +669,7 @@ def main():
     ap.add_argument("--config", default="king1e6", choices=sorted(CONFIGS))
     ap.add_argument("--N", type=int, default=0, help="override the configuration's N (single-cluster configs)")
     ap.add_argument("--cpu-sample", type=int, default=1_000_000, help="stars per CPU-baseline process")
-    ap.add_argument("--cpu-steps", type=int, default=2, help="timed oracle steps of the 1-core CPU baseline")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="timed oracle steps of the 1-core CPU baseline")
     ap.add_argument("--cpu-warmup", type=int, default=1, help="untimed oracle steps before them")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true",

@@ -35,7 +35,7 @@ CUDA_SOURCES = [
     "cmcg_diag.cu",
     "cmcg_mlp.cu",
 ]
-C_SOURCES = ["cmcg_ic.c"]
+C_SOURCES = ["cmcg_ic.c", "cmcg_h5.c"]
 # the synthetic-cluster generator alone (plain C, no CUDA): what the CPU
 # baselines and the oracle tests load to build their models
 IC_LIB = os.path.join(BUILD, "libcmcic.so")
@@ -69,13 +69,14 @@ def _run(cmd: list[str]) -> None:
 
 
 def build_ic(force: bool = False) -> str:
-    """libcmcic.so: cmcg_ic_generate and cmcg_derive_seed without the GPU library."""
+    """libcmcic.so: cmcg_ic_generate, cmcg_derive_seed and cmcg_read_cmc_hdf5
+    without the GPU library."""
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(CSRC, "cmcg_ic.c")
+    srcs = [os.path.join(CSRC, s) for s in C_SOURCES]
     hdr = os.path.join(ROOT, "include", "cmcgpu.h")
-    if force or not _newer(IC_LIB, [src, hdr]):
+    if force or not _newer(IC_LIB, srcs + [hdr]):
         _run(["gcc", "-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-shared",
-              "-I" + os.path.join(ROOT, "include"), "-o", IC_LIB, src, "-lm"])
+              "-I" + os.path.join(ROOT, "include"), "-o", IC_LIB, *srcs, "-lm"])
     return IC_LIB
 
 

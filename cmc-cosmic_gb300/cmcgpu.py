@@ -24,7 +24,7 @@ HEADER = os.path.join(os.path.dirname(_HERE), "include", "cmcgpu.h")
 
 ERRORS = {
     -1: "bad argument", -2: "CUDA error", -3: "capacity exceeded", -4: "out of device memory",
-    -5: "bad state", 1: "NaN in mass sum", 2: "NaN in potential", 3: "W = 0 in encounter",
+    -5: "bad state", -6: "file not readable", -7: "file layout not read here", 1: "NaN in mass sum", 2: "NaN in potential", 3: "W = 0 in encounter",
     4: "wp = 0 in deflection", 5: "N_TRY exceeded", 6: "vr^2 is NaN", 7: "no sign change of vr^2",
     8: "apsis root not converged", 9: "negative residual at apsis", 10: "radius search failed",
     11: "radius outside interval", 12: "strong encounter drawn", 20: "bounded wait gave up",
@@ -33,6 +33,7 @@ ERRORS = {
 
 
 CMCG_ERR_NAN_MASS, CMCG_ERR_NAN_PHI = 1, 2
+CMCG_ERR_IO, CMCG_ERR_FORMAT = -6, -7
 
 
 class CmcError(RuntimeError):
@@ -132,6 +133,18 @@ class HostStars:
 
     def counts(self):
         return [int(s.N) for s in self.arr]
+
+
+class CmcHdf5Info(C.Structure):
+    """cmcg_cmc_hdf5_info: the attributes and table shapes of a CMC initial-conditions file."""
+    _fields_ = [("nobj", C.c_long), ("nbinary", C.c_long), ("mclus", C.c_double), ("rvir", C.c_double),
+                ("rtid", C.c_double), ("z", C.c_double), ("obj_rows", C.c_long), ("obj_cols", C.c_long),
+                ("bin_rows", C.c_long), ("bin_cols", C.c_long)]
+
+
+# the columns of the file's two tables, as cmc_read_hdf5_file (src/libs/fitslib.c:385-420) takes them
+CMC_OBJ_COLUMNS = ("id", "k", "m", "Reff", "r", "vr", "vt", "binind")
+CMC_BIN_COLUMNS = ("index", "id1", "k1", "m1", "Reff1", "id2", "k2", "m2", "Reff2", "a", "e")
 
 
 class ICSpec(C.Structure):
@@ -295,6 +308,8 @@ def ic_lib() -> C.CDLL:
         L = C.CDLL(IC_LIB_PATH)
         L.cmcg_ic_generate.argtypes = [C.POINTER(ICSpec), C.POINTER(ICOut)]
         L.cmcg_derive_seed.argtypes = [C.c_uint64, C.c_uint64]
+        L.cmcg_read_cmc_hdf5.argtypes = [C.c_char_p, C.POINTER(CmcHdf5Info), C.c_void_p, C.c_long, C.c_void_p,
+                                         C.c_long]
         L.cmcg_derive_seed.restype = C.c_uint64
         _ic_lib = L
     return _ic_lib
@@ -330,6 +345,44 @@ def generate(model: int, N: int, seed: int, w0: float = 6.0, imf: int = 0, binar
 
 def derive_seed(master: int, index: int) -> int:
     return int(ic_lib().cmcg_derive_seed(master, index))
+
+
+def read_cmc_hdf5(path: str) -> dict:
+    """COSMIC's CMC initial-conditions file (cmcg_read_cmc_hdf5, read without
+    the HDF5 library): {"info": the attributes and shapes, "obj": the object
+    table, rows 0..NOBJ+1 (row 0 the central mass, the last the sentinel),
+    columns CMC_OBJ_COLUMNS; "bin": the binary table, rows 0..NBINARY,
+    columns CMC_BIN_COLUMNS}."""
+    info = CmcHdf5Info()
+    L = ic_lib()
+    rc = L.cmcg_read_cmc_hdf5(os.fsencode(path), C.byref(info), None, 0, None, 0)
+    if rc:
+        raise CmcError(rc, "cmcg_read_cmc_hdf5")
+    obj = np.zeros((info.obj_rows, info.obj_cols))
+    binr = np.zeros((info.bin_rows, info.bin_cols))
+    rc = L.cmcg_read_cmc_hdf5(os.fsencode(path), C.byref(info), obj.ctypes.data, info.obj_rows, binr.ctypes.data,
+                              info.bin_rows)
+    if rc:
+        raise CmcError(rc, "cmcg_read_cmc_hdf5")
+    return {"info": {k: getattr(info, k) for k, _ in CmcHdf5Info._fields_}, "obj": obj, "bin": binr}
+
+
+def model_from_cmc_hdf5(path: str) -> dict:
+    """A CMC initial-conditions file as a model for Context.load and the oracle:
+    the NOBJ objects' r, m, vr, vt and id as the file holds them (N-body units,
+    masses summing to 1 with the central mass), "rtid" the file's RTID,
+    "cenma" row 0's mass (the central mass, cmc_fits.c:129-131), "binind" the
+    objects' binary rows.  The plain Henon step treats a binary as a point
+    mass of its object mass: with binary encounters off its cross-section is
+    zero (cmc_dynamics.c:239-262)."""
+    t = read_cmc_hdf5(path)
+    obj, n = t["obj"], t["info"]["nobj"]
+    col = {c: i for i, c in enumerate(CMC_OBJ_COLUMNS)}
+    rows = obj[1:n + 1]
+    return {"r": rows[:, col["r"]].copy(), "m": rows[:, col["m"]].copy(), "vr": rows[:, col["vr"]].copy(),
+            "vt": rows[:, col["vt"]].copy(), "id": rows[:, col["id"]].astype(np.int64),
+            "binind": rows[:, col["binind"]].astype(np.int64), "rtid": float(t["info"]["rtid"]),
+            "cenma": float(obj[0, col["m"]])}
 
 
 def draw(seed: int, tcount: int, site: int, star_id: int, n: int, word: int) -> float:

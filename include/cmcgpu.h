@@ -45,6 +45,8 @@ enum {
     CMCG_ERR_CAPACITY = -3,
     CMCG_ERR_NOMEM = -4,
     CMCG_ERR_STATE = -5,
+    CMCG_ERR_IO = -6,          /* a file could not be opened or read               */
+    CMCG_ERR_FORMAT = -7,      /* a file's contents are not the layout expected    */
     /* device-side physics errors; the reference site each one mirrors: */
     CMCG_ERR_NAN_MASS = 1,      /* cmc_utils.c:688   NaN in the mass sum        */
     CMCG_ERR_NAN_PHI = 2,       /* cmc_utils.c:718   NaN in the potential       */
@@ -113,6 +115,27 @@ typedef struct {
 int cmcg_ic_generate(const cmcg_ic_spec *spec, cmcg_ic *out);
 /* Per-cluster seed for cluster `index` of an ensemble drawn from one master seed. */
 uint64_t cmcg_derive_seed(uint64_t master, uint64_t index);
+
+/* The CMC initial-conditions file that COSMIC's InitialCMCTable writes (HDF5,
+ * pandas fixed format), read without the HDF5 library.  Replaces
+ * cmc_read_hdf5_file (src/libs/fitslib.c:209-455): obj receives
+ * CLUS_OBJ_DATA/block0_values, one row per object with the columns
+ * id, k, m, Reff, r, vr, vt, binind (row 0 the central mass, row NOBJ+1 the
+ * outer sentinel, as cmc_fits.c:63-136 reads them); bin receives
+ * CLUS_BINARY_DATA/block0_values, one row per binary with the columns
+ * index, id1, k1, m1, Reff1, id2, k2, m2, Reff2, a, e.  Call with obj and bin
+ * NULL to learn the shapes; then with row capacities of at least obj_rows and
+ * bin_rows.  Returns CMCG_ERR_IO, CMCG_ERR_FORMAT (a storage layout or number
+ * type this reader does not take: chunked or filtered data, big-endian or
+ * non-8-byte numbers), CMCG_ERR_CAPACITY.  Host only, no GPU needed. */
+typedef struct {
+    long nobj, nbinary;          /* the NOBJ and NBINARY attributes                */
+    double mclus, rvir, rtid, z; /* MCLUS, RVIR, RTID (N-body units), Z             */
+    long obj_rows, obj_cols;     /* shape of CLUS_OBJ_DATA/block0_values (cols 8)   */
+    long bin_rows, bin_cols;     /* shape of CLUS_BINARY_DATA/block0_values (11)    */
+} cmcg_cmc_hdf5_info;
+int cmcg_read_cmc_hdf5(const char *path, cmcg_cmc_hdf5_info *info, double *obj, long obj_cap_rows, double *bin,
+                       long bin_cap_rows);
 
 /* ---------------------------------------------------------- context ----- */
 typedef struct cmcg_ctx cmcg_ctx;

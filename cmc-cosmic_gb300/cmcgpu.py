@@ -50,7 +50,7 @@ class Params(C.Structure):
         ("TIDAL_TREATMENT", C.c_int), ("orbit_r", C.c_double), ("cenma_m", C.c_double),
         ("apsides_max_iter", C.c_long), ("apsides_precision", C.c_double),
         ("apsides_convergence", C.c_double), ("n_try", C.c_long), ("seed", C.c_uint64),
-        ("relax_fp32", C.c_int), ("phi_sequential", C.c_int), ("check_filters", C.c_int),
+        ("relax_fp32", C.c_int), ("phi_sequential", C.c_int), ("check_filters", C.c_int), ("relax_trig32", C.c_int),
     ]
 
 
@@ -259,6 +259,7 @@ def lib() -> C.CDLL:
         L.cmcg_draw.argtypes = [C.c_uint64, l, i, C.c_int64, C.c_uint32, i]
         L.cmcg_draw.restype = d
         L.cmcg_sign_stages.argtypes = [vp, vp, vp, vp, d, vp, vp, l, vp]
+        L.cmcg_trig_check.argtypes = [vp, l, vp, l, vp]
         L.cmcg_diagnostics.argtypes = [vp, i, vp, i, i, d, vp]
         L.cmcg_orbit_counters.argtypes = [vp, i]
         L.cmcg_format_dyn_line.argtypes = [vp, vp, vp, l]
@@ -415,6 +416,19 @@ def sign_stages(E, J, rj, mj, invN, rk, phik):
     if rc != 0:
         raise RuntimeError(f"cmcg_sign_stages failed: {rc}")
     return out
+
+
+def trig_check(w, beta):
+    """The relaxation's FP32-pipe sines and cosines (cmcg_trig_check): [n, 2]
+    (sin, cos) of 2 pi w 2^-32 for 32-bit draws w, and [nb, 2] of beta."""
+    import numpy as np
+    w = np.ascontiguousarray(w, dtype=np.uint32)
+    b = np.ascontiguousarray(beta, dtype=np.float64)
+    out = np.zeros(2 * (len(w) + len(b)))
+    rc = lib().cmcg_trig_check(w.ctypes.data, len(w), b.ctypes.data, len(b), out.ctypes.data)
+    if rc != 0:
+        raise CmcError(rc, "cmcg_trig_check")
+    return out[:2 * len(w)].reshape(-1, 2), out[2 * len(w):].reshape(-1, 2)
 
 
 LEARN_OFF, LEARN_ON, LEARN_COLLECT = 0, 1, 2

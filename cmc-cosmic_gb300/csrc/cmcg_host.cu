@@ -114,7 +114,7 @@ struct cmcg_ctx {
     TileTable t128, t256, t1024, t2048;
     void *arena = nullptr;
     size_t arena_bytes = 0;
-    int relax_fp32 = 0;
+    int relax_fp32 = 0, relax_trig32 = 0;
     int nsm = 1;
     // learned proposal: the network (always), the per-star buffers (on first use)
     MlpNet net{};
@@ -385,6 +385,7 @@ void cmcg_default_params(cmcg_params *p)
     p->n_try = 50000;
     p->seed = 0;
     p->relax_fp32 = 0;
+    p->relax_trig32 = 0;
     p->phi_sequential = 0;
     p->check_filters = 0;
 }
@@ -415,10 +416,12 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         if (capacity[k] < 1 || capacity[k] > (1L << 31) - 64) return CMCG_ERR_ARG;  // 32-bit star indices
         if (params[k].AVEKERNEL < 1 || params[k].AVEKERNEL > PMAX) return CMCG_ERR_ARG;
         if (params[k].relax_fp32 != params[0].relax_fp32) return CMCG_ERR_ARG;
+        if (params[k].relax_trig32 != params[0].relax_trig32) return CMCG_ERR_ARG;
     }
     cmcg_ctx *c = new cmcg_ctx();
     c->ncl = nclusters;
     c->relax_fp32 = params[0].relax_fp32;
+    c->relax_trig32 = params[0].relax_trig32;
     c->params.assign(params, params + nclusters);
     c->cap.resize(nclusters);
     c->off.resize(nclusters);
@@ -828,6 +831,9 @@ static int L_relax(cmcg_ctx *c, double dt)
     if (c->relax_fp32)
         k_relax32<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials,
                                                                     c->tickets, dt);
+    else if (c->relax_trig32)
+        k_relax64t<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(c->d_cls, c->t256.view(), c->f, c->partials,
+                                                                     c->tickets, dt);
     else
         (c->var[V_RELAX] ? k_relax64_lb4 : k_relax64)<<<c->t256.ntiles, RELAX_THREADS, 0, c->stream>>>(
             c->d_cls, c->t256.view(), c->f, c->partials, c->tickets, dt);
@@ -1814,7 +1820,7 @@ int cmcg_autotune(cmcg_ctx *c, int steps, char *report, long report_len)
     std::string rep;
     const bool prof0 = c->profile;
     for (int t = 0; t < V_COUNT; ++t) {
-        const bool used = (t == V_ORBIT && c->learn_mode == LEARN_OFF) || (t == V_RELAX && !c->relax_fp32) ||
+        const bool used = (t == V_ORBIT && c->learn_mode == LEARN_OFF) || (t == V_RELAX && !c->relax_fp32 && !c->relax_trig32) ||
                           (t == V_LEARN && c->learn_mode != LEARN_OFF) ||
                           (t == V_MLP_GRID && c->learn_mode == LEARN_ON) || t == V_SORT_TILE ||
                           t == V_GATHER_TILE;

@@ -114,6 +114,9 @@ __global__ void k_relax64(const Cluster *cls, Tiles tm, Fields f, double *partia
                           double dt_override);
 __global__ void k_relax32(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                           double dt_override);
+// FP64 kinematics with the sines and cosines on the FP32 pipe (cmcg_params.relax_trig32)
+__global__ void k_relax64t(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
+                           double dt_override);
 __global__ void k_relax64_lb4(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                               double dt_override);
 // Stars whose Q(j) <= 0 and the first index with Q > 0 found for each (k_posq_scan)

@@ -13,6 +13,7 @@
 // halo in shared memory to form the sliding-window sigma, then relaxes its
 // pairs.  Velocities after relaxation go to separate arrays so that no block
 // ever reads a neighbour's updated velocities in its sigma halo.
+#include "cmcg_fftrig.cuh"
 #include "cmcg_kernels.cuh"
 #include "cmcgpu.h"
 
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_timestep(const Cluster *__restri
 }
 
 // ------------------------------------------------------------ relaxation --
-template <bool FP32>
+template <bool FP32, bool TRIG32 = false>
 static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                   double *partials, unsigned int *tickets, double dt_override)
 {
@@ -250,16 +251,21 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
             const double mass_k = m[k], mass_kp = m[kp];
             const long long idk = id[k];
             // calc_encounter_dyns, cmc_dynamics_helper.c:831-871
-            const double Y = u01(draw_block(C.seed, tcount, SITE_Y, idk, 0u).x);
+            const unsigned int wy = draw_block(C.seed, tcount, SITE_Y, idk, 0u).x;
+            const double Y = u01(wy);
             f.Y[off + k] = Y;
             f.Y[off + kp] = Y;
             double v1 = vtk, v2 = 0.0, v3 = vrk, vp1, vp2, vp3 = vrkp, w1, w2, w3, W;
             double vr_k, vt_k, vr_kp, vt_kp;
             bool ok = true;
             if (!FP32) {
-                const double ang = Y * 2.0 * CMCG_PI;
                 double sa, ca;
-                sincos(ang, &sa, &ca);
+                if (TRIG32) {
+                    sincos_2pi_draw(wy, &sa, &ca);  // sin and cos of Y 2 pi on the FP32 pipe (cmcg_fftrig.cuh)
+                } else {
+                    const double ang = Y * 2.0 * CMCG_PI;
+                    sincos(ang, &sa, &ca);
+                }
                 vp1 = vtkp * ca;
                 vp2 = vtkp * sa;
                 w1 = vp1 - v1;
@@ -310,7 +316,7 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                     }
                 }
                 if (gt_pos(beta, CMCG_PI / 2.0)) beta = CMCG_PI / 2.0;
-                const double psi = u01(draw_block(C.seed, tcount, SITE_PSI, idk, 0u).x) * 2 * CMCG_PI;
+                const unsigned int wpsi = draw_block(C.seed, tcount, SITE_PSI, idk, 0u).x;
                 if (!FP32) {
                     const double wp = sqrt(sqr(w1) + sqr(w2));
                     if (eq0(wp)) {
@@ -321,8 +327,14 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                         const double a1 = div_rcp(-w2 * W, wp, iwp), a2 = div_rcp(w1 * W, wp, iwp), a3 = 0.0;
                         const double b1 = div_rcp(-w1 * w3, wp, iwp), b2 = div_rcp(-w2 * w3, wp, iwp), b3 = wp;
                         double sb, cb, sp, cp;
-                        sincos(beta, &sb, &cb);
-                        sincos(psi, &sp, &cp);
+                        if (TRIG32) {
+                            sincos_beta(beta, &sb, &cb);     // cmcg_fftrig.cuh
+                            sincos_2pi_draw(wpsi, &sp, &cp);  // psi = u01 * 2 pi
+                        } else {
+                            const double psi = u01(wpsi) * 2 * CMCG_PI;
+                            sincos(beta, &sb, &cb);
+                            sincos(psi, &sp, &cp);
+                        }
                         const double wn1 = w1 * cb + a1 * sb * cp + b1 * sb * sp;
                         const double wn2 = w2 * cb + a2 * sb * cp + b2 * sb * sp;
                         const double wn3 = w3 * cb + a3 * sb * cp + b3 * sb * sp;
@@ -345,8 +357,9 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                         const float a1 = -fw2 * fW * iwp, a2 = fw1 * fW * iwp;
                         const float b1 = -fw1 * fw3 * iwp, b2 = -fw2 * fw3 * iwp, b3 = wp;
                         float sb, cb, sp, cp;
+                        const float psi = (float)(u01(wpsi) * 2 * CMCG_PI);
                         sincosf((float)beta, &sb, &cb);
-                        sincosf((float)psi, &sp, &cp);
+                        sincosf(psi, &sp, &cp);
                         const float d1 = fw1 * (cb - 1.0f) + a1 * sb * cp + b1 * sb * sp;
                         const float d2 = fw2 * (cb - 1.0f) + a2 * sb * cp + b2 * sb * sp;
                         const float d3 = fw3 * (cb - 1.0f) + b3 * sb * sp;
@@ -418,10 +431,56 @@ __global__ void __launch_bounds__(RELAX_THREADS, 4) k_relax64_lb4(const Cluster 
     relax_body<false>(cls, tm, f, partials, tickets, dt);
 }
 
+__global__ void __launch_bounds__(RELAX_THREADS, 5) k_relax64t(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+                                                            double *partials, unsigned int *tickets, double dt)
+{
+    relax_body<false, true>(cls, tm, f, partials, tickets, dt);
+}
+
 __global__ void __launch_bounds__(RELAX_THREADS) k_relax32(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                            double *partials, unsigned int *tickets, double dt)
 {
     relax_body<true>(cls, tm, f, partials, tickets, dt);
 }
 
+// The relaxation's sines and cosines at given arguments (cmcg_trig_check).
+__global__ void k_trig_check(const unsigned int *w, long long n, const double *beta, long long nb, double *out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) sincos_2pi_draw(w[i], &out[2 * i], &out[2 * i + 1]);
+    if (i < nb) sincos_beta(beta[i], &out[2 * n + 2 * i], &out[2 * n + 2 * i + 1]);
+}
+
 }  // namespace cmcg
+
+extern "C" int cmcg_trig_check(const unsigned int *w, long n, const double *beta, long nb, double *out)
+{
+    using namespace cmcg;
+    if (n < 0 || nb < 0 || (n > 0 && !w) || (nb > 0 && !beta) || ((n > 0 || nb > 0) && !out)) return CMCG_ERR_ARG;
+    for (long i = 0; i < nb; ++i)
+        if (!(beta[i] >= 0.0 && beta[i] <= 1.57079632679489661923)) return CMCG_ERR_ARG;
+    if (n == 0 && nb == 0) return CMCG_OK;
+    unsigned int *dw = nullptr;
+    double *db = nullptr, *dout = nullptr;
+    const size_t no = 2 * (size_t)(n + nb) * sizeof(double);
+    int rc = CMCG_OK;
+    if (cudaMalloc(&dw, (size_t)(n > 0 ? n : 1) * sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc(&db, (size_t)(nb > 0 ? nb : 1) * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&dout, no) != cudaSuccess)
+        rc = CMCG_ERR_NOMEM;
+    if (rc == CMCG_OK && n > 0 && cudaMemcpy(dw, w, (size_t)n * sizeof(unsigned int), cudaMemcpyHostToDevice))
+        rc = CMCG_ERR_CUDA;
+    if (rc == CMCG_OK && nb > 0 && cudaMemcpy(db, beta, (size_t)nb * sizeof(double), cudaMemcpyHostToDevice))
+        rc = CMCG_ERR_CUDA;
+    if (rc == CMCG_OK) {
+        const long long m = n > nb ? n : nb;
+        k_trig_check<<<(unsigned)((m + 255) / 256), 256>>>(dw, n, db, nb, dout);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, dout, no, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = CMCG_ERR_CUDA;
+    }
+    cudaFree(dw);
+    cudaFree(db);
+    cudaFree(dout);
+    if (rc == CMCG_ERR_NOMEM) cudaGetLastError();
+    return rc;
+}

@@ -91,6 +91,10 @@ typedef struct {
     int check_filters;         /* 1 = every certified FP32 accept/reject of an
                                   orbit trial is also evaluated exactly; a
                                   disagreement is CMCG_ERR_FILTER (for testing)   */
+    int relax_trig32;          /* 1 = the FP64 relaxation's sines and cosines on
+                                  the FP32 pipe in double-float (within 2e-14 of
+                                  sin/cos instead of an ulp; 11% faster
+                                  relaxation); 0 = FP64 sincos (default)         */
 } cmcg_params;
 
 void cmcg_default_params(cmcg_params *p);
@@ -217,6 +221,12 @@ double cmcg_draw(uint64_t seed, long tcount, int site, int64_t id, uint32_t n, i
  * current device and waits for it. */
 int cmcg_sign_stages(const double *E, const double *J, const double *rj, const double *mj, double invN,
                      const double *rk, const double *phik, long n, int *out);
+/* Diagnostic: the sines and cosines the relaxation forms on the FP32 pipe
+ * (double-float arithmetic): for i < n, out[2i], out[2i + 1] = sin, cos of
+ * 2 pi w[i] 2^-32 (a uniform draw's angle); for j < nb, out[2n + 2j],
+ * out[2n + 2j + 1] = sin, cos of beta[j] in [0, pi/2] (CMCG_ERR_ARG outside).
+ * Host arrays; runs on the current device and waits for it. */
+int cmcg_trig_check(const unsigned int *w, long n, const double *beta, long nb, double *out);
 /* Diagnostic: how often the orbit phase took its rare branches, summed over
  * every launch on the current device since the last reset (all contexts):
  *   out[CMCG_ORBIT_SIGN_F64]  table probes of the apsis bisections

@@ -74,6 +74,40 @@ def test_timestep_and_dynamics(gpulib, orc, model, N, imf):
 
 
 @pytest.mark.parametrize("model,N,imf", CASES[:2])
+def test_dynamics_with_sines_on_the_fp32_pipe(gpulib, orc, model, N, imf):
+    """cmcg_params.relax_trig32: the FP64 relaxation with its sines and
+    cosines in double-float on the FP32 pipe (cmcg_fftrig.cuh).  The pairing
+    draws are the oracle's bits and every output is within the relaxation's
+    tolerance of the FP64 oracle (libm sin/cos): velocities against the
+    star's speed, E and J at 1e-12."""
+    ic = cmcgpu.generate(model, N, seed=N + imf, w0=6.0, imf=imf)
+    o = orc.Oracle(ic, orc.default_params(orbit_r=ic["rtid"], seed=12345))
+    g = cmcgpu.Context([N], cmcgpu.default_params(orbit_r=ic["rtid"], seed=12345, relax_trig32=1))
+    g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    o.initialize()
+    g.initialize()
+    sync_state(o, g, star=[("E", "E"), ("J", "J")])
+    o.begin_step()
+    g.begin_step()
+    o.calc_timestep()
+    g.calc_timestep()
+    assert g.scalar("Dt") == o.scalar("Dt")
+    dt = o.scalar("Dt")
+    o.dynamics_apply(dt)
+    g.dynamics_apply(dt)
+    g.check_device("dynamics_apply")
+    assert np.array_equal(g.get("Y"), o.get("Y"))
+    vro, vto = o.get("vr"), o.get("vt")
+    speed = np.sqrt(vro * vro + vto * vto)
+    ev = max(np.max(np.abs(g.get("vr_rel") - vro) / speed), np.max(np.abs(g.get("vt_rel") - vto) / speed))
+    eE, eJ = max_rel(g.get("E"), o.get("E")), max_rel(g.get("J"), o.get("J"))
+    print(f"\nFP32-pipe sines: max error against the speed {ev:.2e}, E {eE:.2e}, J {eJ:.2e}")
+    assert ev <= TOL_PHI and eE <= TOL_PHI and eJ <= TOL_PHI
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("model,N,imf", CASES[:2])
 def test_dynamics_fp32_kinematics_error(gpulib, orc, model, N, imf):
     """FP32 relaxation kinematics with FP64 energies: the error of each output
     against the FP64 oracle, relative to the star's speed (velocities) or value."""
@@ -607,3 +641,30 @@ def test_potential_and_new_orbits_bit_exact_over_seeds(gpulib, orc, seed, model,
     sampled = keep & (o.get("r_apo") > 0)
     assert np.array_equal(g.get("X")[sampled], o.get("X")[sampled])
     g.close()
+
+
+def test_relaxation_sines_and_cosines(gpulib):
+    """The relaxation's sines and cosines, formed on the FP32 pipe in
+    double-float (cmcg_fftrig.cuh: exact reduction from the draw's bits,
+    Taylor series with Dekker/Knuth error-free products and sums), against
+    float64 sin and cos over the whole range: within 2e-13, where the kernels'
+    outputs are held to 1e-12."""
+    rng = np.random.default_rng(42)
+    edges = np.array([0, 1, 2, 63, 64, 65, 2**29 - 1, 2**29, 2**29 + 1, 2**30 - 1, 2**30, 2**30 + 1, 2**31 - 1,
+                      2**31, 2**31 + 1, 3 * 2**30 - 1, 3 * 2**30, 3 * 2**30 + 1, 2**32 - 1], dtype=np.uint64)
+    w = np.concatenate([edges, rng.integers(0, 2**32, 400_000, dtype=np.uint64)]).astype(np.uint32)
+    pio4 = np.pi / 4
+    bedges = np.array([0.0, 1e-300, 1e-20, 1e-8, np.nextafter(pio4, 0), pio4, np.nextafter(pio4, 2), 1.0,
+                       np.nextafter(np.pi / 2, 0), np.pi / 2])
+    beta = np.concatenate([bedges, rng.uniform(0, np.pi / 2, 400_000), rng.uniform(0, 1e-3, 10_000)])
+    sw, sb = cmcgpu.trig_check(w, beta)
+    ang = 2 * np.pi * (w.astype(np.float64) * 2.0**-32)
+    err_w = max(np.max(np.abs(sw[:, 0] - np.sin(ang))), np.max(np.abs(sw[:, 1] - np.cos(ang))))
+    err_b = max(np.max(np.abs(sb[:, 0] - np.sin(beta))), np.max(np.abs(sb[:, 1] - np.cos(beta))))
+    # relative where the value is small (beta near 0: sin beta ~ beta)
+    small = beta < 1e-3
+    rel_b = np.max(np.abs(sb[small, 0] - np.sin(beta[small])) / np.maximum(np.sin(beta[small]), 1e-300))
+    print(f"\nmax |error|: draws' angles {err_w:.2e}, beta {err_b:.2e}; relative for beta < 1e-3: {rel_b:.2e}")
+    assert err_w <= 2e-13 and err_b <= 2e-13 and rel_b <= 2e-13
+    assert sw[0, 0] == 0.0 and sw[0, 1] == 1.0 and sb[0, 0] == 0.0 and sb[0, 1] == 1.0
+    assert sb[1, 0] == 1e-300 and sb[1, 1] == 1.0  # below 2^-60: sin beta = beta, cos beta = 1

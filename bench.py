@@ -451,6 +451,46 @@ def fp32_error_leg(cluster, params):
             "J_over_r_speed": float(np.max(np.abs(b["J"] - a["J"]) / (a["r"] * speed)))}
 
 
+def trig32_leg(a, clusters, tuned_relax):
+    """The same clusters with cmcg_params.relax_trig32 (the relaxation's sines
+    and cosines on the FP32 pipe): the graph-replayed step timed with CUDA
+    events over the same number of steps, and the relaxation's own time from a
+    profiled run of them."""
+    import torch
+
+    import cmcgpu
+
+    params = [cmcgpu.default_params(orbit_r=ic["rtid"], seed=seed, relax_trig32=1) for _, ic, seed in clusters]
+    g = cmcgpu.Context([n for n, _, _ in clusters], params)
+    for c, (n, ic, _) in enumerate(clusters):
+        g.load(c, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+    g.initialize()
+    g.use_graph(True)
+    g.step(a.warmup)
+    g.check_device("trig32 warm-up")
+    stream = torch.cuda.ExternalStream(g.stream_handle())
+    n0 = sum(g.nstars(c) for c in range(len(clusters)))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    e0.record(stream)
+    g.step(a.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    g.check_device("trig32 steps")
+    g.use_graph(False)
+    g.profile(True)
+    g.kernel_time("reset")
+    g.step(a.steps)
+    g.synchronize()
+    relax_ms = g.kernel_time("relax")[0] / a.steps
+    g.close()
+    return {"what": "relax_trig32 = 1: the FP64 relaxation's sines and cosines in double-float on the FP32 pipe "
+                    "(within 2e-14 of sin/cos; off by default)",
+            "value": n0 * a.steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / a.steps,
+            "relax_ms_per_step": relax_ms, "default_relax_ms_per_step": tuned_relax}
+
+
 # ------------------------------------------------------------ GPU leg ----
 def measure(a, cfg_name, N, rank, ws, dist, weights=None, sub=False):
     """One configuration on this rank's GPU: the device-resident step replayed
@@ -605,6 +645,12 @@ def measure(a, cfg_name, N, rank, ws, dist, weights=None, sub=False):
     ctx.close()
     if cfg["fp32"] and rank == 0:
         out["fp32_vs_fp64"] = fp32_error_leg(clusters[0], params)
+    if not cfg["fp32"] and not sub and rank == 0 and ws == 1:
+        try:
+            out["relax_trig32"] = trig32_leg(a, clusters, per_family.get("relax", {}).get("ms_per_step"))
+            out["relax_trig32"]["speedup_vs_default"] = out["relax_trig32"]["value"] / value
+        except Exception as e:  # the default numbers stand without it
+            out["relax_trig32"] = {"error": repr(e)}
     return out
 
 
@@ -643,7 +689,7 @@ def run_ours(a, rank, ws, dist):
         "gpu_launches": m["gpu_launches"],
     }
     for k in ("roofline", "roofline_fp64", "energy", "kernels", "kernel_ms_per_step", "profiled_ms_per_step",
-              "clocks", "learned", "fp32_vs_fp64"):
+              "clocks", "learned", "fp32_vs_fp64", "relax_trig32"):
         if k in m:
             out[k] = m[k]
     if train_info is not None:

@@ -6,7 +6,7 @@ headers (with the single-rank MPI / GSL / HDF5 shims of oracle/refshim
 standing in for the libraries this image lacks), which checks every
 offsetof(star_t, ...) and every host pointer the binding takes.  Then the
 reference's hot-path TUs are compiled with the definitions libcmc_dropin.so
-replaces renamed away, as INTEGRATION.md tells a maintainer to do, and linked
+replaces renamed away (with -D<name>=reference_<name>, the maintainer's route), and linked
 with the glue and a main that references every replaced function: the link
 must succeed with each of them resolved from libcmc_dropin.so.  Needs the
 reference tree; nothing runs on a GPU."""

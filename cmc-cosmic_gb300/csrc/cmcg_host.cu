@@ -949,17 +949,17 @@ static int L_sort(cmcg_ctx *c)
     for (int p = 0; p < SORT_MAX_PASSES; ++p)
         launch_sort_onesweep(c->var[V_SORT_TILE] == 1 ? 1024 : 2048, ost.ntiles, c->stream, c->d_cls, ost.view(), c->f,
                              c->sb, p);
-    k_sort_fix<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb);
-    k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb);
-    // the payload gather, 256, 128 or 1024 stars per block (autotuner)
+    // the payload gather, placing runs of up to FIX_SHORT keys, 256, 128 or
+    // 1024 stars per block (autotuner); then the longer runs
     {
         const int gv = c->var[V_GATHER_TILE];
         const TileTable &gt = gv == 1 ? c->t128 : gv == 2 ? c->t1024 : c->t256;
         launch_sort_gather(gv == 1 ? 128 : gv == 2 ? 1024 : 256, gt.ntiles, c->stream, c->d_cls, gt.view(), c->f, c->sb);
     }
+    k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb, c->f, 1);
     k_sort_commit<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
     fam_end(c);
-    c->launches += 6 + SORT_MAX_PASSES;
+    c->launches += 5 + SORT_MAX_PASSES;
     swap_sorted(c);
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }

@@ -17,8 +17,10 @@ constexpr int EC3_T = 256, EN_T = 2048, EN_THREADS = 256;
 constexpr int EXCESS_CAP = 4096;      // listed unphysical predictions per cluster (else full replay)
 constexpr int EC3_FIX_THREADS = 512;
 constexpr int FIX_WINDOW = 512;       // stars staged per window of the excess-energy replay
-// The digit passes sort the top SORT_PREFIX_BITS bits of the keys; k_sort_fix
-// then sorts each run of keys sharing them by the full key.
+// The digit passes sort the top SORT_PREFIX_BITS bits of the keys; each run of
+// keys sharing them is then put in full-key order: by the payload gather
+// (k_sort_gather, the step's sort) or by k_sort_fix (the allocation-free sort),
+// runs longer than FIX_SHORT by k_sort_fix_long.
 constexpr int SORT_PREFIX_BITS = 24, SORT_MAX_PASSES = SORT_PREFIX_BITS / 8;
 constexpr int FIX_SHORT = 32;   // runs up to this length are sorted by one thread
 constexpr int FIX_BLOCK = 2048; // longer runs up to this length in shared memory, the rest in place
@@ -220,9 +222,12 @@ __global__ void k_sort_ghist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb
 void launch_sort_onesweep(int tile_keys, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f,
                           SortBufs sb, int pass);
 __global__ void k_sort_fix(const Cluster *cls, Tiles tm, SortBufs sb);
-__global__ void k_sort_fix_long(const Cluster *cls, Tiles tm, SortBufs sb);
+// gather = 1: also moves the payload of the runs it sorts (the step's sort,
+// after k_sort_gather); 0: keys and values only (the allocation-free sort).
+__global__ void k_sort_fix_long(const Cluster *cls, Tiles tm, SortBufs sb, Fields f, int gather);
 // The payload gather, `block` stars per block (128, 256 or 1024, on the
-// matching tile table).
+// matching tile table); it places the runs of up to FIX_SHORT keys and lists
+// the longer ones for k_sort_fix_long.
 void launch_sort_gather(int block, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
 __global__ void k_sort_commit(const Cluster *cls, int nclusters);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);

@@ -10,9 +10,10 @@
 // bits) less the cluster's smallest, with every escaper (rnew = SF_INFINITY)
 // at the first key of the 24-bit prefix after the largest bound key's;
 // values the star's slot.  The digit passes sort the keys' top 24 bits (3
-// passes); keys that share them then form runs in input order, which
-// k_sort_fix sorts by the full key (runs are a star or two at the densities
-// of these clusters; the escapers' run is equal keys, already in order).
+// passes); keys that share them then form runs in input order, which are put
+// in full-key order as the payload moves (runs are a star or two at the
+// densities of these clusters; the escapers' run is equal keys, already in
+// order).
 //   k_sort_ghist     every 8-bit digit's histogram in one read of the keys
 //   k_sort_onesweep  one kernel per digit pass: stable in-tile ranking (warp
 //                    match + per-warp counters), tile offsets by decoupled
@@ -26,7 +27,11 @@
 // memory into the warp-striped order the ranking uses.
 // k_sort_gather then moves the payload (rnew, m, vrnew, vtnew, id, r, ec_pre)
 // into radial order, one 8-byte gather per field and star, and drops the
-// escapers (r == SF_INFINITY), which sort last.
+// escapers (r == SF_INFINITY), which sort last.  Each of its threads places
+// its star within the star's run by the rank of (key, position) in it; runs
+// longer than FIX_SHORT go to k_sort_fix_long, which sorts them and moves their
+// payload.  (The allocation-free sort, which has no payload, sorts the runs
+// in place with k_sort_fix and k_sort_fix_long instead.)
 #include "cmcg_kernels.cuh"
 #include "cmcgpu.h"
 
@@ -486,6 +491,59 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_fix(const Cluster *__rest
     }
 }
 
+// One star's payload from input slot v (0-based) to output position i
+// (0-based) of the radial order (ComputeIntermediateEnergy transfer +
+// post_sort_comm): the second buffers of r, m, id and ec_pre, which the host
+// then swaps with the first.
+__device__ __forceinline__ void move_star(const Cluster &C, const Fields &f, unsigned int v, long long i)
+{
+    const long long src = 1 + (long long)v;
+    if (src > C.sc->N_MAX_NEW) {
+        set_error(C.sc, CMCG_ERR_BOUNDS, src);
+        return;
+    }
+    const long long gs = C.off + src, gd = C.off + 1 + i;
+    f.r2[gd] = f.rnew[gs];
+    f.m2[gd] = f.m[gs];
+    f.vr[gd] = f.vrnew[gs];
+    f.vt[gd] = f.vtnew[gs];
+    f.id2[gd] = f.id[gs];
+    f.rOld[gd] = f.r[gs];
+    f.ec_pre2[gd] = f.ec_pre[gs];
+}
+
+// The output position of the key at sorted position i of n (keys 0..n-1 after
+// the digit passes, which order the prefixes K >> sh): i itself when no
+// neighbour shares its prefix; inside a run of keys sharing it, the run's
+// start plus the rank of (key, position) among the run's members, which is
+// the stable full-key order (members are in input order).  A run longer than
+// FIX_SHORT returns -1; its first member lists it for k_sort_fix_long.
+__device__ __forceinline__ long long run_place(const unsigned long long *K, long long i, long long n, int sh,
+                                               unsigned int *nlong, long long *lists)
+{
+    const unsigned long long ki = K[i], p = ki >> sh;
+    const bool up = i > 0 && (K[i - 1] >> sh) == p;
+    const bool dn = i + 1 < n && (K[i + 1] >> sh) == p;
+    if (!up && !dn) return i;
+    long long s = i;  // walk back to the run's start, at most FIX_SHORT + 1 keys
+#pragma unroll 1
+    while (s > 0 && i - s <= FIX_SHORT && (K[s - 1] >> sh) == p) --s;
+    long long e = i + 1;
+#pragma unroll 1
+    while (e < n && e - s <= FIX_SHORT && (K[e] >> sh) == p) ++e;
+    if (e - s > FIX_SHORT) {
+        if (!up) lists[atomicAdd(nlong, 1u)] = i;  // at most n / (FIX_SHORT + 1) runs fit
+        return -1;
+    }
+    long long r = 0;
+#pragma unroll 1
+    for (long long j = s; j < e; ++j) {
+        const unsigned long long kj = K[j];
+        r += (kj < ki) || (kj == ki && j < i);
+    }
+    return s + r;
+}
+
 // (key, slot) pairs ordered by key, then by slot: the slots are the input
 // positions, so this order is the stable one and no two pairs are equal.
 __device__ __forceinline__ bool pair_less(unsigned long long ka, unsigned int va, unsigned long long kb,
@@ -500,7 +558,7 @@ __device__ __forceinline__ bool pair_less(unsigned long long ka, unsigned int va
 // lengths need no padding.  Up to FIX_BLOCK keys in shared memory, longer
 // runs in place in global memory.
 __global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *__restrict__ cls, Tiles tm,
-                                                                SortBufs sb)
+                                                                SortBufs sb, Fields f, int gather)
 {
     __shared__ unsigned long long s_k[FIX_BLOCK];
     __shared__ unsigned int s_v[FIX_BLOCK];
@@ -550,6 +608,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *_
             for (long long t = threadIdx.x; t < L; t += SORT_THREADS) {
                 K[s + t] = s_k[t];
                 V[s + t] = s_v[t];
+                if (gather) move_star(C, f, s_v[t], s + t);
             }
         } else {
             unsigned long long *k0 = K + s;
@@ -570,14 +629,16 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *_
                     __syncthreads();  // orders the block's global writes between stages
                 }
             }
+            if (gather)
+                for (long long t = threadIdx.x; t < L; t += SORT_THREADS) move_star(C, f, v0[t], s + t);
         }
         __syncthreads();
     }
 }
 
 // Payload gather into radial order (ComputeIntermediateEnergy transfer +
-// post_sort_comm).  Writes the second buffers of r, m, id, ec_pre, which the
-// host then swaps with the first.
+// post_sort_comm), each star placed within its run (run_place).  Writes the
+// second buffers of r, m, id, ec_pre, which the host then swaps with the first.
 template <int GT>
 __global__ void __launch_bounds__(GT) k_sort_gather(const Cluster *__restrict__ cls, Tiles tm, Fields f, SortBufs sb)
 {
@@ -587,26 +648,25 @@ __global__ void __launch_bounds__(GT) k_sort_gather(const Cluster *__restrict__ 
     Scalars *sc = C.sc;
     const long long nb = sc->n_bound;
     const int np = sb.npass[ct.x];
-    const long long i = (long long)ct.y * GT + threadIdx.x;  // 0-based output position
+    const long long i = (long long)ct.y * GT + threadIdx.x;  // 0-based sorted position
     const long long off = C.off;
     if (nb < 0 || nb > sc->N_MAX_NEW) {
         if (i == 0) set_error(sc, CMCG_ERR_BOUNDS, nb);
         return;
     }
     if (i < nb) {
-        const long long src = 1 + (np == 0 ? i : (long long)((np & 1) ? sb.vals[1] : sb.vals[0])[off + i]);
-        if (src < 1 || src > sc->N_MAX_NEW) {
-            set_error(sc, CMCG_ERR_BOUNDS, src);
-            return;
+        if (np == 0) {
+            move_star(C, f, (unsigned int)i, i);
+        } else {
+            const int sel = np & 1;
+            const unsigned int v = (sel ? sb.vals[1] : sb.vals[0])[off + i];
+            const int sh = sb.shift[ct.x];
+            // bound stars sort before the escapers' run, so their runs end by nb
+            const long long dst = sh == 0 ? i
+                                          : run_place((sel ? sb.keys[1] : sb.keys[0]) + off, i, nb, sh,
+                                                      sb.nlong + ct.x, sb.lstart + off / 32 + 64 * ct.x);
+            if (dst >= 0) move_star(C, f, v, dst);
         }
-        const long long gs = off + src, gd = off + 1 + i;
-        f.r2[gd] = f.rnew[gs];
-        f.m2[gd] = f.m[gs];
-        f.vr[gd] = f.vrnew[gs];
-        f.vt[gd] = f.vtnew[gs];
-        f.id2[gd] = f.id[gs];
-        f.rOld[gd] = f.r[gs];
-        f.ec_pre2[gd] = f.ec_pre[gs];
     }
     if (i == 0) {
         // the second buffers become the live arrays: carry the sentinels over

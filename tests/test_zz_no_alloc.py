@@ -56,15 +56,18 @@ def test_noalloc_sort_matches_regular_sort_twice(gpulib):
 
 def test_sort_runs_sharing_the_sorted_prefix(gpulib):
     """The digit passes sort the keys' top 24 bits; keys sharing them form runs
-    that a fix-up sorts by the full key.  Planted groups of radii within 1e-12
-    of a centre give runs of every kind: a few keys (one thread), hundreds
-    (shared memory) and 5000 (in place), with exact ties inside them."""
+    that are put in full-key order afterwards.  Planted groups of radii within
+    1e-12 of a centre give runs of every kind: up to 32 keys (placed by rank in
+    the payload gather, or insertion-sorted by one thread in the
+    allocation-free sort), hundreds (shared memory) and 5000 (in place), with
+    exact ties inside them."""
     rng = np.random.default_rng(77)
     n = 60000
     radii = np.exp(rng.uniform(-6.0, 5.0, size=n))
     pos = rng.permutation(n)
     at = 0
-    for size, count in ((7, 400), (300, 20), (5000, 1)):
+    # 32 and 33 keys: the longest run a gather thread places and the shortest listed one
+    for size, count in ((7, 400), (32, 30), (33, 30), (300, 20), (5000, 1)):
         for _ in range(count):
             c = np.exp(rng.uniform(-5.0, 4.0))
             grp = c * (1.0 + rng.uniform(0.0, 1e-12, size))

@@ -55,7 +55,7 @@ const Tunable kTunables[V_COUNT] = {
     {"relax", F_RELAX, 2, {"5 blocks/SM", "4 blocks/SM"}},
     {"orbit_learn", F_ORBIT, 2, {"5 blocks/SM", "4 blocks/SM"}},
     {"mlp_grid", F_MLP, 4, {"4 CTAs/SM", "2 CTAs/SM", "3 CTAs/SM", "6 CTAs/SM"}},
-    {"sort_tile", F_SORT, 2, {"2048 keys/tile", "1024 keys/tile"}},
+    {"sort_tile", F_SORT, 3, {"4096 keys/tile", "2048 keys/tile", "1024 keys/tile"}},
     {"gather_tile", F_SORT, 3, {"256 stars/block", "128 stars/block", "1024 stars/block"}},
 };
 
@@ -111,7 +111,7 @@ struct cmcg_ctx {
     Ec3Bufs eb{};
     double *d_query = nullptr;
     DiagDev *d_diag = nullptr;
-    TileTable t128, t256, t1024, t2048;
+    TileTable t128, t256, t1024, t2048, t4096;  // t4096: the 4096-key digit passes
     void *arena = nullptr;
     size_t arena_bytes = 0;
     int relax_fp32 = 0, relax_trig32 = 0;
@@ -298,8 +298,8 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->d_cls = cv.take<Cluster>(c->ncl);
     c->d_query = cv.take<double>(2);
     c->d_diag = cv.take<DiagDev>(1);
-    TileTable *tts[4] = {&c->t128, &c->t256, &c->t1024, &c->t2048};
-    for (int i = 0; i < 4; ++i) {
+    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t4096};
+    for (int i = 0; i < 5; ++i) {
         tts[i]->d_tiles = cv.take<int2>(tabs[i].size());
         tts[i]->d_first = cv.take<int>(c->ncl);
         tts[i]->d_count = cv.take<int>(c->ncl);
@@ -438,11 +438,12 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         c->ridx_total += ridx_buckets(capacity[k]) + 1;
         c->ridx_Bmax = std::max(c->ridx_Bmax, ridx_buckets(capacity[k]));
     }
-    std::vector<int2> tabs[4];
+    std::vector<int2> tabs[5];
     build_table(c->t128, c->cap, ORB_T, tabs[0]);
     build_table(c->t256, c->cap, RELAX_T, tabs[1]);
     build_table(c->t1024, c->cap, POT_T, tabs[2]);
     build_table(c->t2048, c->cap, SORT_T, tabs[3]);
+    build_table(c->t4096, c->cap, 4096, tabs[4]);
     size_t bytes = 0;
     carve_all(c, nullptr, tabs, &bytes);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -489,8 +490,8 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         ridx_off += C.ridx_B + 1;
     }
     CK(cudaMemcpyAsync(c->d_cls, c->h_cls.data(), nclusters * sizeof(Cluster), cudaMemcpyHostToDevice, c->stream));
-    TileTable *tts[4] = {&c->t128, &c->t256, &c->t1024, &c->t2048};
-    for (int i = 0; i < 4; ++i) {
+    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t4096};
+    for (int i = 0; i < 5; ++i) {
         CK(cudaMemcpyAsync(tts[i]->d_tiles, tabs[i].data(), tabs[i].size() * sizeof(int2), cudaMemcpyHostToDevice,
                            c->stream));
         CK(cudaMemcpyAsync(tts[i]->d_first, tts[i]->first.data(), nclusters * sizeof(int), cudaMemcpyHostToDevice,
@@ -502,6 +503,7 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
     int dev = 0, nsm = 0, per_sm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    CK(sort_onesweep_setup());
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tidal, TID_THREADS, 0));
     c->tidal_grid = std::max(1, std::min(c->t2048.ntiles, nsm * std::max(per_sm, 1)));
     c->posq_grid = 2 * nsm;
@@ -944,10 +946,11 @@ static int L_sort(cmcg_ctx *c)
     k_sort_prep<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb,
                                                                    c->partials, c->tickets);
     k_sort_ghist<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->sb);
-    // digit passes over 2048- or 1024-key tiles (autotuner)
-    const TileTable &ost = c->var[V_SORT_TILE] == 1 ? c->t1024 : c->t2048;
+    // digit passes over 4096-, 2048- or 1024-key tiles (autotuner)
+    const int sv = c->var[V_SORT_TILE];
+    const TileTable &ost = sv == 1 ? c->t2048 : sv == 2 ? c->t1024 : c->t4096;
     for (int p = 0; p < SORT_MAX_PASSES; ++p)
-        launch_sort_onesweep(c->var[V_SORT_TILE] == 1 ? 1024 : 2048, ost.ntiles, c->stream, c->d_cls, ost.view(), c->f,
+        launch_sort_onesweep(sv == 1 ? 2048 : sv == 2 ? 1024 : 4096, ost.ntiles, c->stream, c->d_cls, ost.view(), c->f,
                              c->sb, p);
     // the payload gather, placing runs of up to FIX_SHORT keys, 256, 128 or
     // 1024 stars per block (autotuner); then the longer runs
@@ -956,10 +959,10 @@ static int L_sort(cmcg_ctx *c)
         const TileTable &gt = gv == 1 ? c->t128 : gv == 2 ? c->t1024 : c->t256;
         launch_sort_gather(gv == 1 ? 128 : gv == 2 ? 1024 : 256, gt.ntiles, c->stream, c->d_cls, gt.view(), c->f, c->sb);
     }
-    k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb, c->f, 1);
-    k_sort_commit<<<(c->ncl + 127) / 128, 128, 0, c->stream>>>(c->d_cls, c->ncl);
+    k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb, c->f,
+                                                                      c->tickets);
     fam_end(c);
-    c->launches += 5 + SORT_MAX_PASSES;
+    c->launches += 4 + SORT_MAX_PASSES;
     swap_sorted(c);
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }

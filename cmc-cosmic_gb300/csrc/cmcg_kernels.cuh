@@ -215,21 +215,24 @@ __global__ void k_tidal(const Cluster *cls, Tiles tm, Fields f, double *partials
 __global__ void k_sort_prep(const Cluster *cls, Tiles tm, Fields f, SortBufs sb, double *partials,
                             unsigned int *tickets);
 __global__ void k_sort_ghist(const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
-// One digit pass over tiles of `tile_keys` keys (1024 or 2048: the
-// autotuner's candidates; tm is the matching tile table).  Host launchers of
+// One digit pass over tiles of `tile_keys` keys (1024, 2048 or 4096: the
+// autotuner's candidates; tm is the matching tile table).  The 4096-key form
+// stages 48 KB of dynamic shared memory, which sort_onesweep_setup allows
+// (once per process, before any launch).  Host launchers of
 // the templated kernels, defined beside them (a template kernel's launch stub
 // is local to the file that instantiates it).
 void launch_sort_onesweep(int tile_keys, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f,
                           SortBufs sb, int pass);
+cudaError_t sort_onesweep_setup();
 __global__ void k_sort_fix(const Cluster *cls, Tiles tm, SortBufs sb);
-// gather = 1: also moves the payload of the runs it sorts (the step's sort,
-// after k_sort_gather); 0: keys and values only (the allocation-free sort).
-__global__ void k_sort_fix_long(const Cluster *cls, Tiles tm, SortBufs sb, Fields f, int gather);
+// With tickets (the step's sort, after k_sort_gather): also moves the payload
+// of the runs it sorts, and the last block of each cluster commits its new
+// star count.  Without (the allocation-free sort): keys and values only.
+__global__ void k_sort_fix_long(const Cluster *cls, Tiles tm, SortBufs sb, Fields f, unsigned int *tickets);
 // The payload gather, `block` stars per block (128, 256 or 1024, on the
 // matching tile table); it places the runs of up to FIX_SHORT keys and lists
 // the longer ones for k_sort_fix_long.
 void launch_sort_gather(int block, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
-__global__ void k_sort_commit(const Cluster *cls, int nclusters);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);
 __global__ void k_pot_carry(const Cluster *cls, Tiles tm, PotBufs pb, PhiBufs ph, int nclusters);
 __global__ void k_pot_apply(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph);

@@ -144,7 +144,7 @@ extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_pe
     k_sort_ghist<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb);
     for (int p = 0; p < SORT_MAX_PASSES; ++p) launch_sort_onesweep(SORT_T, ntiles, s, cls, tm, f, sb, p);
     k_sort_fix<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, sb);
-    k_sort_fix_long<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, sb, f, 0);
+    k_sort_fix_long<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, sb, f, nullptr);
     k_na_perm<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(base, n, d_perm);
     if (cudaGetLastError() != cudaSuccess) return CMCG_ERR_CUDA;
     if (n_bound) {

@@ -231,15 +231,17 @@ __device__ __forceinline__ unsigned long long st_tag(unsigned int epoch, int pas
 // only waits on tiles that took a smaller index, which have started; every
 // wait is bounded and records CMCG_ERR_SPIN if it gives up.
 template <int ITEMS>
-__global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+__global__ void __launch_bounds__(OS_THREADS, 2) k_sort_onesweep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                               SortBufs sb, int pass)
 {
     constexpr int NWARP = OS_THREADS / 32, T = OS_THREADS * ITEMS;  // T keys per tile
     __shared__ unsigned int wcnt[NWARP][RADIX];  // per-warp digit counters -> prefixes
     __shared__ unsigned int dstart[RADIX];       // in-tile digit start
     __shared__ unsigned long long gbase[RADIX];  // global digit start for this tile
-    __shared__ __align__(16) unsigned long long sk[T];
-    __shared__ __align__(16) unsigned int sv[T];
+    // the tile's keys and values (dynamic: T x 12 bytes, 48 KB at 4096 keys)
+    extern __shared__ __align__(16) unsigned char os_dyn[];
+    unsigned long long *sk = reinterpret_cast<unsigned long long *>(os_dyn);
+    unsigned int *sv = reinterpret_cast<unsigned int *>(os_dyn + sizeof(unsigned long long) * T);
     __shared__ unsigned int s_w[RADIX / 32];
     __shared__ unsigned long long s_t[RADIX / 32];
     __shared__ int s_b;
@@ -427,13 +429,27 @@ __global__ void __launch_bounds__(OS_THREADS) k_sort_onesweep(const Cluster *__r
     }
 }
 
+constexpr size_t os_dyn_bytes(int items)
+{
+    return (size_t)OS_THREADS * items * (sizeof(unsigned long long) + sizeof(unsigned int));
+}
+
+cudaError_t sort_onesweep_setup()
+{
+    // 4096-key tiles stage 48 KB of keys and values beside the static counters
+    return cudaFuncSetAttribute(k_sort_onesweep<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)os_dyn_bytes(8));
+}
+
 void launch_sort_onesweep(int tile_keys, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f,
                           SortBufs sb, int pass)
 {
     if (tile_keys == OS_THREADS * 2)
-        k_sort_onesweep<2><<<ntiles, OS_THREADS, 0, s>>>(cls, tm, f, sb, pass);
+        k_sort_onesweep<2><<<ntiles, OS_THREADS, os_dyn_bytes(2), s>>>(cls, tm, f, sb, pass);
+    else if (tile_keys == OS_THREADS * 8)
+        k_sort_onesweep<8><<<ntiles, OS_THREADS, os_dyn_bytes(8), s>>>(cls, tm, f, sb, pass);
     else
-        k_sort_onesweep<4><<<ntiles, OS_THREADS, 0, s>>>(cls, tm, f, sb, pass);
+        k_sort_onesweep<4><<<ntiles, OS_THREADS, os_dyn_bytes(4), s>>>(cls, tm, f, sb, pass);
 }
 
 // After the digit passes, runs of keys sharing their sorted prefix are in
@@ -552,22 +568,31 @@ __device__ __forceinline__ bool pair_less(unsigned long long ka, unsigned int va
     return ka < kb || (ka == kb && va < vb);
 }
 
+// New N_MAX after the gather (cmc_sort.c:343-354, cmc_utils.c:2246), once
+// every block of the cluster is past it.
+__device__ __forceinline__ void sort_commit(Scalars *sc)
+{
+    if (sc->n_bound < 0 || sc->n_bound > sc->N_MAX_NEW) {
+        set_error(sc, CMCG_ERR_BOUNDS, sc->n_bound);
+        return;
+    }
+    sc->N_MAX = sc->n_bound;
+    sc->N_MAX_NEW = sc->n_bound;
+}
+
 // Runs longer than FIX_SHORT, each by one block (a cluster's tiles share its
 // list): a bitonic network in the form whose first comparison of each merge
 // pairs i with its mirror i ^ (k - 1), so every comparison is ascending and
 // lengths need no padding.  Up to FIX_BLOCK keys in shared memory, longer
 // runs in place in global memory.
-__global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *__restrict__ cls, Tiles tm,
-                                                                SortBufs sb, Fields f, int gather)
+// With gather, also each run's payload (the step's sort).
+__device__ __forceinline__ void sort_long_runs(const Cluster &C, int2 ct, const Tiles &tm, const SortBufs &sb,
+                                               const Fields &f, bool gather)
 {
     __shared__ unsigned long long s_k[FIX_BLOCK];
     __shared__ unsigned int s_v[FIX_BLOCK];
     __shared__ long long s_len;
-    const int2 ct = tm.tiles[blockIdx.x];
-    const Cluster &C = cls[ct.x];
-    if (!counts_ok(C)) return;
     const int sh = sb.shift[ct.x];
-    if (sh == 0) return;
     const int np = sb.npass[ct.x];
     const long long N = C.sc->N_MAX_NEW;
     unsigned long long *K = ((np & 1) ? sb.keys[1] : sb.keys[0]) + C.off;
@@ -636,6 +661,19 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *_
     }
 }
 
+// The long runs, then (the step's sort, tickets given) the star-count commit.
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_fix_long(const Cluster *__restrict__ cls, Tiles tm,
+                                                                SortBufs sb, Fields f, unsigned int *tickets)
+{
+    __shared__ int s_last;
+    const int2 ct = tm.tiles[blockIdx.x];
+    const Cluster &C = cls[ct.x];
+    if (counts_ok(C) && sb.shift[ct.x] != 0) sort_long_runs(C, ct, tm, sb, f, tickets != nullptr);
+    // the step's sort: the cluster's last block commits the new star count
+    if (tickets && block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last) && threadIdx.x == 0)
+        sort_commit(C.sc);
+}
+
 // Payload gather into radial order (ComputeIntermediateEnergy transfer +
 // post_sort_comm), each star placed within its run (run_place).  Writes the
 // second buffers of r, m, id, ec_pre, which the host then swaps with the first.
@@ -688,21 +726,6 @@ void launch_sort_gather(int block, int ntiles, cudaStream_t s, const Cluster *cl
         k_sort_gather<1024><<<ntiles, 1024, 0, s>>>(cls, tm, f, sb);
     else
         k_sort_gather<256><<<ntiles, 256, 0, s>>>(cls, tm, f, sb);
-}
-
-// New N_MAX after the gather (cmc_sort.c:343-354, cmc_utils.c:2246); a kernel of
-// its own so no gather block ever sees the count change under it.
-__global__ void k_sort_commit(const Cluster *__restrict__ cls, int nclusters)
-{
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nclusters) return;
-    Scalars *sc = cls[c].sc;
-    if (sc->n_bound < 0 || sc->n_bound > sc->N_MAX_NEW) {
-        set_error(sc, CMCG_ERR_BOUNDS, sc->n_bound);
-        return;
-    }
-    sc->N_MAX = sc->n_bound;
-    sc->N_MAX_NEW = sc->n_bound;
 }
 
 }  // namespace cmcg

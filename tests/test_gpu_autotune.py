@@ -31,7 +31,7 @@ def test_plain_variants_are_bit_identical(gpulib):
     a, b = _pair(30000, 81)
     b.set_variant("orbit", 1)
     b.set_variant("relax", 1)
-    b.set_variant("sort_tile", 1)    # 1024-key digit-pass tiles
+    b.set_variant("sort_tile", 2)    # 1024-key digit-pass tiles
     b.set_variant("gather_tile", 2)  # 1024-star gather blocks
     assert b.variant("orbit") == 1 and b.variant("relax") == 1
     for g in (a, b):
@@ -66,9 +66,9 @@ def test_persistent_orbit_kernels_are_bit_identical(gpulib, variant):
             assert a.scalar(s, c) == b.scalar(s, c), (c, s)
 
 
-@pytest.mark.parametrize("sort_tile,gather_tile", [(1, 1), (0, 2), (1, 0)])
+@pytest.mark.parametrize("sort_tile,gather_tile", [(1, 1), (0, 2), (1, 0), (2, 0), (2, 1)])
 def test_sort_tile_variants_are_bit_identical(gpulib, sort_tile, gather_tile):
-    """The sort's tile sizes (digit pass 2048 or 1024 keys; gather blocks of
+    """The sort's tile sizes (digit pass 4096, 2048 or 1024 keys; gather blocks of
     256, 128 or 1024 stars) on a 200,000-star cluster: hundreds of tiles, so
     the look-back and the tile tables are exercised at every size."""
     a, b = _pair(200000, 87)
@@ -98,10 +98,10 @@ def test_tuning_steps_are_steps_of_the_run(gpulib):
     rep = b.autotune(1)
     assert "orbit:" in rep and "relax:" in rep and "sort_tile:" in rep and "gather_tile:" in rep, rep
     assert b.variant("orbit") in (0, 1, 2, 3) and b.variant("relax") in (0, 1)
-    assert b.variant("sort_tile") in (0, 1) and b.variant("gather_tile") in (0, 1, 2)
-    # orbit with four variants, relax and the sort tile with two, the gather
+    assert b.variant("sort_tile") in (0, 1, 2) and b.variant("gather_tile") in (0, 1, 2)
+    # orbit with four variants, relax with two, the sort tile and the gather
     # with three, each variant one untimed and one timed step
-    a.step(2 * (4 + 2 + 2 + 3))
+    a.step(2 * (4 + 2 + 3 + 3))
     a.check_device("plain")
     b.check_device("tuned")
     _same_state(a, b)

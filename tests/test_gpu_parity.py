@@ -373,6 +373,50 @@ def _run_steps(gpulib, ic, N, chunks, graph):
     return out
 
 
+@pytest.mark.parametrize("strip", [1, 0])
+def test_whole_steps_equal_the_phase_calls(gpulib, strip):
+    """Whole steps (cmcg_step) against the same steps made of the phase entry
+    points in the main loop's order (cmcg_begin_step ... cmcg_compute_energy),
+    with tidal stripping on (a King model that strips stars at once, so escapers
+    go through the sort) and off: three steps each way, bit-identical."""
+    N = 20000
+    ic = cmcgpu.generate(cmcgpu.KING, N, seed=91, w0=6.0, imf=1)
+    ctx = []
+    for _ in range(2):
+        p = cmcgpu.default_params(orbit_r=ic["rtid"] * 0.6, seed=91, TIDALLY_STRIP_STARS=strip)
+        g = cmcgpu.Context([N], p)
+        g.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
+        g.initialize()
+        ctx.append(g)
+    a, b = ctx
+    a.step(3)
+    a.check_device("steps")
+    for step in range(3):
+        if step:
+            b.end_step()
+        b.begin_step()
+        b.calc_timestep()
+        b.dynamics_apply()
+        b.new_orbits_calculate()
+        b.tidally_strip_stars()
+        b.qsorts_new()
+        b.calc_potential()
+        b.energy_conservation3()
+        b.compute_energy()
+    b.end_step()
+    b.check_device("phases")
+    assert a.nstars() == b.nstars()
+    if strip:
+        assert a.nstars() < N  # stars were stripped: escapers went through the sort
+    assert np.array_equal(a.ids(), b.ids())
+    for name in ("r", "m", "phi", "vr", "vt", "E", "J"):
+        assert np.array_equal(a.get(name), b.get(name)), name
+    for sname in ("Etot", "Mtotal", "TidalMassLoss", "max_r", "Dt"):
+        assert a.scalar(sname) == b.scalar(sname), sname
+    a.close()
+    b.close()
+
+
 def test_graph_replay_equals_direct_launches_and_is_deterministic(gpulib):
     """Steps replayed from the captured CUDA graphs (cooperative tidal launch
     included) give the same bits as direct launches, and a run repeats

@@ -95,6 +95,9 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
     if (hx) {  // the caller's copy; k_ec3_fix rewrites the stars it changes
         hx[4 * ct.x][i - 1] = vr;
         hx[4 * ct.x + 1][i - 1] = vt;
+        // J = r vt as compute_energy_new forms it (cmc_utils.c:604-617), sent
+        // here so that it crosses the host link while this kernel runs
+        hx[4 * ct.x + 3][i - 1] = ri * vt;
     }
 }
 
@@ -105,7 +108,7 @@ __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, 
 // left on reaching `end`, 0 once it is used up.  WRITE applies the changes.
 template <bool WRITE>
 static __device__ double ec3_walk(const Fields &f, long long off, long long i0, long long end, double E,
-                                  double *hvr = nullptr, double *hvt = nullptr)
+                                  double *hvr = nullptr, double *hvt = nullptr, double *hJ = nullptr)
 {
     const double E_dump_factor = 0.8;
     for (long long i = i0 + 1; i < end && E > 0; ++i) {
@@ -121,6 +124,7 @@ static __device__ double ec3_walk(const Fields &f, long long off, long long i0, 
             if (hvr) {
                 hvr[i - 1] = vr * exc_ratio;
                 hvt[i - 1] = vt * exc_ratio;
+                hJ[i - 1] = f.r[g] * (vt * exc_ratio);
             }
         }
         E -= E_dump;
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
     if (!counts_ok(C)) return;
     Scalars *sc = C.sc;
     const long long off = C.off, N = sc->N_MAX_NEW;
-    double *hvr = hx ? hx[4 * c] : nullptr, *hvt = hx ? hx[4 * c + 1] : nullptr;
+    double *hvr = hx ? hx[4 * c] : nullptr, *hvt = hx ? hx[4 * c + 1] : nullptr, *hJ = hx ? hx[4 * c + 3] : nullptr;
     const unsigned int n = eb.nlist[c];
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
         __syncthreads();
         for (int t = threadIdx.x; t < nn; t += blockDim.x) {
             const long long i0 = L[t], end = (t + 1 < nn) ? L[t + 1] : N + 1;
-            ec3_walk<true>(f, off, i0, end, carry[t] + eb.a[off + i0], hvr, hvt);  // 0 + a = a when nothing is carried
+            ec3_walk<true>(f, off, i0, end, carry[t] + eb.a[off + i0], hvr, hvt, hJ);  // 0 + a = a when nothing is carried
         }
         return;
     }
@@ -259,6 +263,7 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
                     if (hvr) {
                         hvr[i - 1] = vr;
                         hvt[i - 1] = vt;
+                        hJ[i - 1] = f.r[off + i] * vt;
                     }
                     Eexcess -= E_dump;
                 }
@@ -292,7 +297,8 @@ __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict
     // (two FP64 operations a star fewer for each; the sums are tree sums anyway)
     double K = 0.0, P = 0.0;
     int cnt = 0;
-    double *hE = hx ? hx[4 * ct.x + 2] : nullptr, *hJ = hx ? hx[4 * ct.x + 3] : nullptr;
+    // the caller's E (J went there from energy conservation, with the final vt)
+    double *hE = hx ? hx[4 * ct.x + 2] : nullptr;
 #pragma unroll 4
     for (int it = 0; it < EN_T / EN_THREADS; ++it) {
         const long long i = 1 + (long long)ct.y * EN_T + it * EN_THREADS + threadIdx.x;
@@ -303,10 +309,7 @@ __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict
         const double E = ph + 0.5 * v2, J = f.r[g] * vt;
         f.E[g] = E;
         f.J[g] = J;
-        if (hE) {  // the caller's copy
-            hE[i - 1] = E;
-            hJ[i - 1] = J;
-        }
+        if (hE) hE[i - 1] = E;  // the caller's copy
         K += v2 * m;
         P += ph * m;
         ++cnt;

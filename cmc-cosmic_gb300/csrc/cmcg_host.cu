@@ -1892,9 +1892,9 @@ static const void *device_view(const void *p)
 // memory, or device memory).  The uploads of r, m, vr, vt, which precede the
 // time step with nothing else to run, go by one k_xfer launch over every
 // cluster.  The results that are final only at the step's end are written
-// into the caller's arrays by the kernels that compute them: vr and vt by
-// energy conservation, E and J by the energies (part HX_XTAIL), so that they
-// cross the host link while those kernels run.  The transfers that
+// into the caller's arrays by the kernels that compute them: vr, vt and
+// J = r vt by energy conservation, E by the energies (part HX_XTAIL), so that
+// they cross the host link while those kernels run.  The transfers that
 // overlap other kernels stay on the copy engines, one cudaMemcpyAsync per
 // array (id up during the time step, E and J staged during the relaxation,
 // r, m, id down during the potential): a copy kernel beside a kernel that

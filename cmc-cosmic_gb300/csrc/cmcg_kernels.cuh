@@ -248,8 +248,8 @@ __global__ void k_begin_step(const Cluster *cls, int nclusters);
 __global__ void k_end_step(const Cluster *cls, int nclusters);
 // hx: nullptr, or (host exchange) every cluster's pinned host arrays, which
 // these kernels write as well as the fields: for cluster c, hx[4c] = vr,
-// hx[4c+1] = vt (k_ec3, k_ec3_fix), hx[4c+2] = E, hx[4c+3] = J (k_energy),
-// star i at element i - 1.
+// hx[4c+1] = vt, hx[4c+3] = J = r vt (k_ec3, k_ec3_fix), hx[4c+2] = E
+// (k_energy), star i at element i - 1.
 __global__ void k_ec3(const Cluster *cls, Tiles tm, Fields f, Ec3Bufs eb, double *const *hx);
 __global__ void k_ec3_fix(const Cluster *cls, Fields f, Ec3Bufs eb, int nclusters, double *const *hx);
 __global__ void k_energy(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,

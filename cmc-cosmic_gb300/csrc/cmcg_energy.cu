@@ -22,28 +22,16 @@ __global__ void k_begin_step(const Cluster *__restrict__ cls, int nclusters)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nclusters) return;
-    Scalars *sc = cls[c].sc;
-    sc->Eescaped_old = sc->Eescaped;
-    sc->Jescaped_old = sc->Jescaped;
-    sc->TidalMassLoss_old = sc->TidalMassLoss;
-    sc->Etidal_old = sc->Etidal;
-    sc->Eescaped = 0.0;
-    sc->Jescaped = 0.0;
-    sc->TidalMassLoss = 0.0;
-    sc->Etidal = 0.0;
-    sc->N_MAX_NEW = sc->N_MAX;
-    sc->tidal_done = cls[c].TIDALLY_STRIP_STARS ? 0 : 1;
-    sc->tidal_iters = 0;
+    begin_step(cls[c]);
 }
 
 __global__ void k_end_step(const Cluster *__restrict__ cls, int nclusters)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nclusters) return;
-    Scalars *sc = cls[c].sc;
-    sc->Prev_Dt = sc->Dt;
-    sc->tcount += 1;
+    end_step(cls[c].sc);
 }
+
 
 __global__ void __launch_bounds__(EC3_T) k_ec3(const Cluster *__restrict__ cls, Tiles tm, Fields f, Ec3Bufs eb,
                                                double *const *hx)
@@ -280,7 +268,8 @@ __global__ void __launch_bounds__(EC3_FIX_THREADS) k_ec3_fix(const Cluster *__re
 // Eight stars per thread: the per-star FP64 work is the reference's
 // expressions; the sums take one addition per star before the block tree.
 __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                       double *partials, unsigned int *tickets, double *const *hx)
+                                                       double *partials, unsigned int *tickets, double *const *hx,
+                                                       int end)
 {
     __shared__ double red[EN_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
@@ -348,6 +337,7 @@ __global__ void __launch_bounds__(EN_THREADS) k_energy(const Cluster *__restrict
             double tot = aK + aP + 0.0 + 0.0;
             tot += sc->cenma_E + sc->Eescaped + 0.0 + 0.0;
             sc->Etot = tot;
+            if (end) end_step(sc);  // a whole step's last kernel: k_end_step's work
         }
     }
 }

@@ -790,11 +790,12 @@ static int L_pot(cmcg_ctx *c)
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
-static int L_energy(cmcg_ctx *c, double *const *hx = nullptr)
+// end: the step's last kernel, which also does k_end_step's work
+static int L_energy(cmcg_ctx *c, double *const *hx = nullptr, bool end = false)
 {
     fam_begin(c, F_ENERGY);
     k_energy<<<c->t2048.ntiles, EN_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->f, c->partials,
-                                                             c->tickets, hx);
+                                                             c->tickets, hx, end ? 1 : 0);
     fam_end(c);
     c->launches += 1;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
@@ -818,10 +819,12 @@ static int L_end(cmcg_ctx *c)
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 
-static int L_timestep(cmcg_ctx *c)
+// begin: the step's first kernel, which also does k_begin_step's work
+static int L_timestep(cmcg_ctx *c, bool begin = false)
 {
     fam_begin(c, F_TIMESTEP);
-    k_timestep<<<c->t1024.ntiles, TS_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->f, c->partials, c->tickets);
+    k_timestep<<<c->t1024.ntiles, TS_THREADS, 0, c->stream>>>(c->d_cls, c->t1024.view(), c->f, c->partials, c->tickets,
+                                                             begin ? 1 : 0);
     fam_end(c);
     c->launches += 1;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
@@ -987,8 +990,7 @@ static int issue_part(cmcg_ctx *c, int part)
 {
     switch (part) {
     case 0:
-        RUN(L_begin(c));
-        RUN(L_timestep(c));
+        RUN(L_timestep(c, true));
         break;
     case 1:
         RUN(L_relax(c, -1.0));
@@ -1013,12 +1015,10 @@ static int issue_part(cmcg_ctx *c, int part)
     case HX_XTAIL:
         RUN(L_pot(c));
         RUN(L_ec3(c, c->d_hx));
-        RUN(L_energy(c, c->d_hx));
-        RUN(L_end(c));
+        RUN(L_energy(c, c->d_hx, true));
         break;
     default:
-        RUN(L_energy(c));
-        RUN(L_end(c));
+        RUN(L_energy(c, nullptr, true));
     }
     return CMCG_OK;
 }

@@ -110,7 +110,8 @@ struct Ec3Bufs {
     double *carry;       // per cluster: [EXCESS_CAP] excess entering each listed star's segment
 };
 
-__global__ void k_timestep(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets);
+__global__ void k_timestep(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
+                           int begin);
 // FP64 kinematics (parity with the reference) and FP32 kinematics with FP64 energies
 __global__ void k_relax64(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
                           double dt_override);
@@ -246,6 +247,31 @@ __global__ void k_ridx_build(const Cluster *cls, Fields f, PhiBufs ph, int nclus
 constexpr int RIDX_THREADS = 256;
 __global__ void k_begin_step(const Cluster *cls, int nclusters);
 __global__ void k_end_step(const Cluster *cls, int nclusters);
+// Their work for one cluster (cmc.c:246-257; cmc.c:294, 390); a whole step
+// does them in the last block of its first kernel (k_timestep, begin = 1)
+// and of its last (k_energy, end = 1).
+__device__ __forceinline__ void begin_step(const Cluster &C)
+{
+    Scalars *sc = C.sc;
+    sc->Eescaped_old = sc->Eescaped;
+    sc->Jescaped_old = sc->Jescaped;
+    sc->TidalMassLoss_old = sc->TidalMassLoss;
+    sc->Etidal_old = sc->Etidal;
+    sc->Eescaped = 0.0;
+    sc->Jescaped = 0.0;
+    sc->TidalMassLoss = 0.0;
+    sc->Etidal = 0.0;
+    sc->N_MAX_NEW = sc->N_MAX;
+    sc->tidal_done = C.TIDALLY_STRIP_STARS ? 0 : 1;
+    sc->tidal_iters = 0;
+}
+
+__device__ __forceinline__ void end_step(Scalars *sc)
+{
+    sc->Prev_Dt = sc->Dt;
+    sc->tcount += 1;
+}
+
 // hx: nullptr, or (host exchange) every cluster's pinned host arrays, which
 // these kernels write as well as the fields: for cluster c, hx[4c] = vr,
 // hx[4c+1] = vt, hx[4c+3] = J = r vt (k_ec3, k_ec3_fix), hx[4c+2] = E
@@ -253,7 +279,7 @@ __global__ void k_end_step(const Cluster *cls, int nclusters);
 __global__ void k_ec3(const Cluster *cls, Tiles tm, Fields f, Ec3Bufs eb, double *const *hx);
 __global__ void k_ec3_fix(const Cluster *cls, Fields f, Ec3Bufs eb, int nclusters, double *const *hx);
 __global__ void k_energy(const Cluster *cls, Tiles tm, Fields f, double *partials, unsigned int *tickets,
-                         double *const *hx);
+                         double *const *hx, int end);
 __global__ void k_potential_query(const Cluster *cls, Fields f, int c, double x, double *out);
 
 // ---- step diagnostics of dyn.dat and lagrad.dat (cmcg_diag.cu)

@@ -53,7 +53,7 @@ static __device__ __forceinline__ double n_local_at(const double *__restrict__ r
 // memory; then one thread per window adds its terms in the reference's
 // order, so every sum, and Dt, is bit-identical.
 __global__ void __launch_bounds__(TS_THREADS) k_timestep(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                         double *partials, unsigned int *tickets)
+                                                         double *partials, unsigned int *tickets, int begin)
 {
     constexpr int LMAX = TS_T + 2 * PMAX;  // stars of the windows centred in one tile
     __shared__ double s_mv[LMAX], s_mm[LMAX], s_m2[LMAX];
@@ -110,6 +110,9 @@ __global__ void __launch_bounds__(TS_THREADS) k_timestep(const Cluster *__restri
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {
         const double Dtmin = -reduce_partials_max<TS_THREADS>(partials, tm.first[ct.x], tm.count[ct.x], 1, 0, red);
         if (threadIdx.x == 0) {
+            // a whole step's first kernel: k_begin_step's work, before the
+            // tallies below read it (no block reads what it changes)
+            if (begin) begin_step(C);
             double Dt = C.RELAXATION ? Dtmin : INFINITY;
             // GetTimeStep, cmc_evolution_thr.c:420: all other time scales are infinite
             if (isinf(Dt)) Dt = 0.001;

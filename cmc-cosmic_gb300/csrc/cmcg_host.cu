@@ -395,11 +395,11 @@ void cmcg_default_params(cmcg_params *p)
 // is computed by the one-thread loop.
 static long long phi_rec_cap(long long cap) { return 4096 + cap / 16; }
 
-// Buckets of the radius index: about 16 stars each, 2^10 to 2^16.
+// Buckets of the radius index: about 16 stars each, 2^10 to 2^20.
 static int ridx_buckets(long long cap)
 {
     int B = 1024;
-    while (B < 65536 && (long long)B * 16 < cap) B <<= 1;
+    while (B < (1 << 20) && (long long)B * 16 < cap) B <<= 1;
     return B;
 }
 

@@ -68,6 +68,19 @@ static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
     return fq_sign_at(o, k, __ldg(o.rphif + k));
 }
 
+// Pull a table entry into L2 (no register holds it).  In clusters whose
+// tables exceed L2 (from PREFETCH_MIN_STARS stars: a 64 MB FP32 table beside
+// 192 MB of FP64 ones), the bisections ask for the two entries their next
+// round can probe while this round's probe is in flight, so that the next
+// probe finds its sector in L2 instead of waiting on DRAM.  At 10^7 stars the
+// orbit kernel took 11.16 against 11.38 ms a step with them; at 10^6 stars,
+// where the tables sit in L2, the extra L2 requests cost 4.6%.
+constexpr long long PREFETCH_MIN_STARS = 1ll << 22;
+static __device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // find_zero_Q, cmc_nr.c:316-383 (bounded; returns -1 if it does not terminate).
 // The reference compares the end-point values to choose the direction; when
 // their signs differ the signs decide it, and only same-signed ends are
@@ -78,10 +91,15 @@ static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long 
 {
     const int smin = fq_sign(o, kmin), smax = fq_sign(o, kmax);
     const bool up = (smin != smax) ? (smin < smax) : (fq(o, kmin) < fq(o, kmax));
+    const bool pf = o.N_MAX >= PREFETCH_MIN_STARS;
     int it = 0;
     if (up) {
         do {
             const long long ktry = (kmin + kmax + 1) / 2;
+            if (pf) {  // the next probe, either way (within [kmin, kmax])
+                prefetch_l2(o.rphif + (ktry + kmax + 1) / 2);
+                prefetch_l2(o.rphif + (kmin + ktry) / 2);
+            }
             if (fq_sign(o, ktry) < 0)
                 kmin = ktry;
             else
@@ -91,6 +109,10 @@ static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long 
     } else {
         do {
             const long long ktry = (kmin + kmax + 1) / 2;
+            if (pf) {
+                prefetch_l2(o.rphif + (ktry + kmax + 1) / 2);
+                prefetch_l2(o.rphif + (kmin + ktry) / 2);
+            }
             if (fq_sign(o, ktry) > 0)
                 kmin = ktry;
             else

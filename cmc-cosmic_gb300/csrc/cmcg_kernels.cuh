@@ -31,11 +31,11 @@ struct SortBufs {
     unsigned int *vals[2];
     unsigned long long *ghist;   // per cluster: [SORT_MAX_PASSES][RADIX] digit totals
     unsigned long long *status;  // per tile: [RADIX] look-back words (epoch | flag | count)
-    unsigned int *tile_next;     // [SORT_MAX_PASSES] tile counters, zeroed before each sort
+    unsigned int *tile_next;     // [SORT_MAX_PASSES] tile counters, zeroed by k_sort_prep
     unsigned int *epoch;         // sorts so far (advanced by k_sort_prep): tags the status words
     int *npass;                  // per cluster: passes needed
     int *shift;                  // per cluster: bits below the sorted prefix (0: the passes sort every bit)
-    unsigned int *nlong;         // per cluster: runs longer than FIX_SHORT, zeroed before each sort
+    unsigned int *nlong;         // per cluster: runs longer than FIX_SHORT, zeroed by k_sort_prep
     long long *lstart;           // their first positions: cluster c from off[c] / 32 + 64 c
     unsigned long long *kmin, *kmax;
 };

@@ -136,10 +136,7 @@ extern "C" int cmcg_sort_radii_noalloc(const double *d_r, long n, uint32_t *d_pe
     Tiles tm{(const int2 *)(base + NA_TILE), (const int *)(base + NA_FC), (const int *)(base + NA_FC) + 1, ntiles};
     double *partials = (double *)(base + NA_PART);
     unsigned int *tickets = (unsigned int *)(base + NA_TICK);
-    if (cudaMemsetAsync(sb.ghist, 0, sizeof(unsigned long long) * SORT_MAX_PASSES * RADIX, s) != cudaSuccess ||
-        cudaMemsetAsync(sb.tile_next, 0, sizeof(unsigned int) * SORT_MAX_PASSES, s) != cudaSuccess ||
-        cudaMemsetAsync(sb.nlong, 0, sizeof(unsigned int), s) != cudaSuccess)
-        return CMCG_ERR_CUDA;
+    // k_sort_prep zeroes the digit totals, tile counters and long-run count
     k_sort_prep<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb, partials, tickets);
     k_sort_ghist<<<ntiles, SORT_THREADS, 0, s>>>(cls, tm, f, sb);
     for (int p = 0; p < SORT_MAX_PASSES; ++p) launch_sort_onesweep(SORT_T, ntiles, s, cls, tm, f, sb, p);

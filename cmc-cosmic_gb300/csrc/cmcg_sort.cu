@@ -45,6 +45,14 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
     __shared__ unsigned long long s_min[SORT_THREADS / 32], s_max[SORT_THREADS / 32];
     __shared__ long long s_cnt[SORT_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
+    // the sort's counters start at zero: the digit passes' tile counters, and
+    // each cluster's digit totals and long-run count (k_sort_ghist, the gather)
+    if (blockIdx.x == 0 && threadIdx.x < SORT_MAX_PASSES) sb.tile_next[threadIdx.x] = 0u;
+    if (ct.y == 0) {
+        for (int i = threadIdx.x; i < SORT_MAX_PASSES * RADIX; i += SORT_THREADS)
+            sb.ghist[(size_t)ct.x * SORT_MAX_PASSES * RADIX + i] = 0ull;
+        if (threadIdx.x == 0) sb.nlong[ct.x] = 0u;
+    }
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
     Scalars *sc = C.sc;

@@ -202,7 +202,8 @@ def test_config5_size_one_step_properties(gpulib, orc):
         subset of the initial ones, the stars removed accounted for by the
         tidal mass loss;
       * the potential the step ends with equal, bit for bit, to the oracle's
-        potential_calculate on the GPU's own post-step radii and masses."""
+        potential_calculate on the GPU's own post-step radii and masses, and
+        potential(r) through the radius index equal to the oracle's search."""
     N = 10_000_000
     ic = cmcgpu.generate(cmcgpu.KING, N, seed=31, w0=7.0, imf=1, binary_fraction=0.1)
     seed = 4242
@@ -253,5 +254,13 @@ def test_config5_size_one_step_properties(gpulib, orc):
     assert o2.nstars() == n1
     assert o2.scalar("Mtotal") == m1
     assert np.array_equal(g.get("star_phi"), o2.get("star_phi"))
+    # potential(r) through the radius index (2^20 buckets at this size) against
+    # the oracle's full binary search on the same table
+    rng = np.random.default_rng(5)
+    pick = rng.choice(n1, 200, replace=False)
+    xs = list(r[pick]) + list(np.nextafter(r[pick], np.inf)) + list(np.nextafter(r[pick], 0.0))
+    xs += list(np.exp(rng.uniform(np.log(r[0]), np.log(r[-1]), 200))) + [r[0], r[-1], 2.0 * r[-1]]
+    for x in xs:
+        assert g.potential(float(x)) == o2.potential(float(x)), x
     o2.close()
     g.close()

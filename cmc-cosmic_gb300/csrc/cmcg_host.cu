@@ -778,7 +778,6 @@ static int L_pot(cmcg_ctx *c)
     const int nt = c->t1024.ntiles;
     k_pot_agg<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb);
     k_pot_carry<<<c->ncl, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->pb, c->ph, c->ncl);
-    k_pot_apply<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph);
     k_phi_cls12<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
     k_phi_rec12<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
     k_phi_cls3<<<nt, POT_THREADS, 0, c->stream>>>(c->d_cls, tv, c->f, c->pb, c->ph, c->tickets);
@@ -788,7 +787,7 @@ static int L_pot(cmcg_ctx *c)
     k_ridx_build<<<dim3((unsigned)((c->ridx_Bmax + RIDX_THREADS) / RIDX_THREADS), (unsigned)c->ncl), RIDX_THREADS, 0,
                    c->stream>>>(c->d_cls, c->f, c->ph, c->ncl);
     fam_end(c);
-    c->launches += 10;
+    c->launches += 9;
     return cudaGetLastError() == cudaSuccess ? CMCG_OK : CMCG_ERR_CUDA;
 }
 

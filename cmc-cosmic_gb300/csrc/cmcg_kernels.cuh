@@ -52,6 +52,36 @@ struct PotBufs {
 };
 constexpr int POT_AGG = 5, POT_CARRY = 3;
 
+// 1/r of the star just outside a potential tile whose largest index is kstart
+// (r[N+1] = SF_INFINITY).  A tile map sized for the capacity has tiles lying
+// wholly below star 1 once N has shrunk (kstart < 1); they hold no stars and
+// must not read r at all.
+__device__ __forceinline__ double pot_r_next_inv(const double *r, long long kstart, long long N)
+{
+    if (kstart < 1 || kstart > N) return 0.0;
+    return __drcp_rn(kstart == N ? CMCG_SF_INFINITY : r[kstart + 1]);
+}
+
+// Exclusive block prefix of one double per thread (thread order), as the
+// potential's scans take it: warp shuffles, then the warps' totals in order.
+template <int NT>
+__device__ __forceinline__ double pot_block_excl_prefix(double tsum, double *s_w)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) s_w[w] = x;
+    __syncthreads();
+    double b = 0.0;
+    for (int q = 0; q < w; ++q) b += s_w[q];
+    return b + x - tsum;  // exclusive prefix of this thread
+}
+
 // ---- exact replay of the sequential potential recurrences (cmcg_phi.cu)
 // A "sequential point" is a position whose rounding cannot be proven to stay
 // on one binade grid; the other positions add an integer number of grid units.
@@ -236,7 +266,6 @@ __global__ void k_sort_fix_long(const Cluster *cls, Tiles tm, SortBufs sb, Field
 void launch_sort_gather(int block, int ntiles, cudaStream_t s, const Cluster *cls, Tiles tm, Fields f, SortBufs sb);
 __global__ void k_pot_agg(const Cluster *cls, Tiles tm, Fields f, PotBufs pb);
 __global__ void k_pot_carry(const Cluster *cls, Tiles tm, PotBufs pb, PhiBufs ph, int nclusters);
-__global__ void k_pot_apply(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph);
 __global__ void k_phi_cls12(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);
 __global__ void k_phi_rec12(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);
 __global__ void k_phi_cls3(const Cluster *cls, Tiles tm, Fields f, PotBufs pb, PhiBufs ph, unsigned int *tickets);

@@ -12,8 +12,8 @@
 // the grid u = 2^(E-52), on which s_{j-1} already lies, so
 //     s_j = s_{j-1} + rho_j u,    rho_j = round(a_j / u), an integer,
 // unless a_j / u ends in exactly one half (a tie, decided by s_{j-1}).  So a
-// chain is an integer prefix sum except at a few positions.  k_pot_apply
-// gives every s_j to within a proven bound; a position whose before and
+// chain is an integer prefix sum except at a few positions.  The carries
+// of cmcg_potential.cu give every s_j to within a proven bound (tile_approx); a position whose before and
 // after values are both farther than that bound from the edges of the same
 // binade, and whose term is no tie, is "regular".  Every other position -- a
 // binade change, a value within the bound of an edge, a tie, the first and
@@ -197,9 +197,15 @@ __device__ __forceinline__ int block_int_excl(int v, int *s_w, int *total)
 
 // ---- the three chains seen from one tile
 struct View {
-    const double *m, *q, *t, *inv_r, *sapx, *mapx, *papx;  // cluster-relative, index k
+    const double *m, *q, *t, *inv_r, *papx;  // cluster-relative, index k
     long long N;
     double marg1, marg2, c0, c1;
+    // chains 1 and 2 (k_phi_cls12 only): the tile's approximate S_k and M_k by
+    // position p = kst - k (tile_approx), and those of the tile below's first
+    // position (p = POT_T)
+    const double *sS, *sM;
+    long long kst;
+    double Sb, Mb;
 };
 
 __device__ __forceinline__ View make_view(const Cluster &C, const Fields &f, const PotBufs &pb, const PhiCtl &ctl)
@@ -210,9 +216,10 @@ __device__ __forceinline__ View make_view(const Cluster &C, const Fields &f, con
     v.q = pb.q + off;
     v.t = pb.t + off;
     v.inv_r = f.inv_r + off;
-    v.sapx = pb.sapx + off;
-    v.mapx = pb.mapx + off;
     v.papx = pb.papx + off;
+    v.sS = v.sM = nullptr;
+    v.kst = 0;
+    v.Sb = v.Mb = 0.0;
     v.N = C.sc->N_MAX;
     v.marg1 = ctl.marg1;
     v.marg2 = ctl.marg2;
@@ -232,10 +239,14 @@ __device__ __forceinline__ long long kpos(long long kstart, int p)
 template <int CH>
 __device__ __forceinline__ AState after_state(const View &v, long long k)
 {
-    if (CH == 1) return astate(v.sapx[k], v.marg1);
+    if (CH == 1) {
+        const long long p = v.kst - k;
+        return astate(p < POT_T ? v.sS[p] : v.Sb, v.marg1);
+    }
     if (CH == 2) {
         if (k <= 1) return AState{0, false};  // M_0 is never used
-        return astate(v.mapx[k - 1], v.marg2);
+        const long long p = v.kst - (k - 1);
+        return astate(p < POT_T ? v.sM[p] : v.Mb, v.marg2);
     }
     return astate(v.papx[k], __dadd_ru(v.c0, __dmul_ru(v.c1, v.inv_r[k])));
 }
@@ -555,13 +566,85 @@ __device__ __forceinline__ int ctl_failed(const PhiCtl &ctl) { return *(volatile
 
 }  // namespace
 
+// The approximate running values of chains 1 and 2 over one tile, and Phi_k
+// (chain 3's) into pb.papx, from the carries entering the tile (k_pot_carry):
+//   S_k, the forward mass sum through star k, and M_k, the enclosed mass the
+//   backward loop multiplies at star k, into sS and sM by position p = kstart - k;
+//   Phi_k for k_phi_cls3 and the Phi bound of k_phi_rec12.
+// Thread t holds k = kstart - 4t - i; every value is the carry plus a block
+// scan of the tile's terms (pot_block_excl_prefix), so the first position of
+// a tile -- whose value the tile above also needs, as its boundary -- is the
+// carry alone: S = Sm - SmIn, M = Mtot - Qin (tile_first_values).
+__device__ __forceinline__ void tile_approx(const Cluster &C, const Fields &f, const PotBufs &pb, const PhiCtl &ctl,
+                                            long long N, long long kstart, const double *cr, double *sS, double *sM,
+                                            double *s_w, double *s_lastinv)
+{
+    const long long off = C.off;
+    const double *r = f.r + off, *inv_r = f.inv_r + off, *m = f.m + off;
+    const double Mtot = ctl.Mapx, Sm = ctl.Sm;
+    const double Qin = cr[0], Din = cr[1], SmIn = cr[2];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    double q[POT_ITEMS], inv[POT_ITEMS], mm[POT_ITEMS];
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        q[i] = (k >= 1) ? pb.q[off + k] : 0.0;
+        inv[i] = (k >= 1) ? inv_r[k] : 0.0;
+        mm[i] = (k >= 1) ? m[k] : 0.0;
+    }
+    double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
+    if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
+    __syncthreads();
+    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : pot_r_next_inv(r, kstart, N);
+    double tq = 0.0, tmm = 0.0;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        tq += q[i];
+        tmm += mm[i];
+    }
+    const double qex = pot_block_excl_prefix<POT_THREADS>(tq, s_w);
+    const double mex = pot_block_excl_prefix<POT_THREADS>(tmm, s_w);
+    double dk[POT_ITEMS], run = qex, runm = mex, td = 0.0;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        const double innext = (i == 0) ? up : inv[i - 1];
+        const double Mk = (Mtot - Qin) - run;  // mprev when the reference reaches k
+        dk[i] = (k >= 1) ? Mk * (inv[i] - innext) : 0.0;
+        sM[POT_ITEMS * t + i] = Mk;
+        sS[POT_ITEMS * t + i] = Sm - (SmIn + runm);
+        run += q[i];
+        runm += mm[i];
+        td += dk[i];
+    }
+    const double dex = pot_block_excl_prefix<POT_THREADS>(td, s_w);
+    double acc = Din + dex;
+#pragma unroll
+    for (int i = 0; i < POT_ITEMS; ++i) {
+        const long long k = kstart - POT_ITEMS * t - i;
+        acc += dk[i];
+        if (k >= 1) pb.papx[off + k] = -acc;
+    }
+    __syncthreads();  // sS, sM complete
+}
+
+// S and M at a tile's first position (k = its kstart): the carries alone, as
+// tile_approx forms them there (its exclusive prefixes are +0 at thread 0).
+__device__ __forceinline__ void tile_first_values(const PhiCtl &ctl, const double *cr, double *S, double *M)
+{
+    *M = (ctl.Mapx - cr[0]) - 0.0;
+    *S = ctl.Sm - (cr[2] + 0.0);
+}
+
 // ------------------------------------------------------------ kernels ----
 
-__global__ void __launch_bounds__(POT_THREADS) k_phi_cls12(const Cluster *__restrict__ cls, Tiles tm, Fields f,
+__global__ void __launch_bounds__(POT_THREADS, 4) k_phi_cls12(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                             PotBufs pb, PhiBufs ph, unsigned int *tickets)
 {
     __shared__ TileSmem sm;
     __shared__ int s_last;
+    __shared__ double s_S[POT_T], s_M[POT_T];
+    __shared__ double s_w[POT_THREADS / 32], s_lastinv[POT_THREADS / 32];
     const int2 ct = tm.tiles[blockIdx.x];
     const Cluster &C = cls[ct.x];
     if (!counts_ok(C)) return;
@@ -569,7 +652,13 @@ __global__ void __launch_bounds__(POT_THREADS) k_phi_cls12(const Cluster *__rest
     const long long N = C.sc->N_MAX;
     const long long kstart = N - (long long)ct.y * POT_T;
     if (!ctl_failed(ctl) && kstart >= 1) {
-        const View v = make_view(C, f, pb, ctl);
+        tile_approx(C, f, pb, ctl, N, kstart, pb.carry + (size_t)blockIdx.x * POT_CARRY, s_S, s_M, s_w, s_lastinv);
+        View v = make_view(C, f, pb, ctl);
+        v.sS = s_S;
+        v.sM = s_M;
+        v.kst = kstart;
+        if (kstart - POT_T >= 1)  // the tile below (the next one of the cluster) starts at kstart - POT_T
+            tile_first_values(ctl, pb.carry + (size_t)(blockIdx.x + 1) * POT_CARRY, &v.Sb, &v.Mb);
         Items it;
         load_positions<1>(v, kstart, it);
 #pragma unroll

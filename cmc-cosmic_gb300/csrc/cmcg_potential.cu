@@ -18,44 +18,12 @@
 //                order, non-finite or negative values)
 //   k_pot_carry  per cluster: approximate Mtotal, the bounds the replay
 //                classifies with, scan of the triples over tiles
-//   k_pot_apply  per tile: approximate forward mass sum, M_k and Phi_k
+//   (k_phi_cls12, cmcg_phi.cu, then forms each tile's approximate forward
+//   mass sums, M_k and Phi_k from these carries before classifying them)
 #include "cmcg_kernels.cuh"
 
 namespace cmcg {
 
-
-static __device__ __forceinline__ double r_at(const double *r, long long k, long long N)
-{
-    return k == N + 1 ? CMCG_SF_INFINITY : r[k];
-}
-
-// 1/r of the star just outside a tile whose largest index is kstart.  A tile
-// map sized for the capacity has tiles lying wholly below star 1 once N has
-// shrunk (kstart < 1); they hold no stars and must not read r at all.
-static __device__ __forceinline__ double r_next_inv(const double *r, long long kstart, long long N)
-{
-    if (kstart < 1 || kstart > N) return 0.0;
-    return __drcp_rn(r_at(r, kstart + 1, N));
-}
-
-// inclusive block scan (blocked arrangement: thread t holds items t*4..t*4+3)
-template <int NT>
-static __device__ __forceinline__ double block_excl_prefix(double tsum, double *s_w)
-{
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    double x = tsum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        double y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    __syncthreads();
-    if (lane == 31) s_w[w] = x;
-    __syncthreads();
-    double b = 0.0;
-    for (int q = 0; q < w; ++q) b += s_w[q];
-    return b + x - tsum;  // exclusive prefix of this thread
-}
 
 __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restrict__ cls, Tiles tm, Fields f,
                                                           PotBufs pb)
@@ -99,7 +67,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
     double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
     if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
     __syncthreads();
-    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : r_next_inv(r, kstart, N);
+    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : pot_r_next_inv(r, kstart, N);
     double d[POT_ITEMS];
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) {
@@ -115,7 +83,7 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_agg(const Cluster *__restri
     double tq = 0.0;
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) tq += q[i];
-    const double qex = block_excl_prefix<POT_THREADS>(tq, s_w);
+    const double qex = pot_block_excl_prefix<POT_THREADS>(tq, s_w);
     double run = qex, tc = 0.0, td = 0.0, tm_ = 0.0;
 #pragma unroll
     for (int i = 0; i < POT_ITEMS; ++i) {
@@ -267,71 +235,6 @@ __global__ void __launch_bounds__(POT_THREADS) k_pot_carry(const Cluster *__rest
         eq += a[0];
         eD += a[1];
         em += a[3];
-    }
-}
-
-// Approximate running values in the reference's indexing:
-//   sapx[k] = S_k (forward mass sum through star k), mapx[k] = M_k (the
-//   enclosed mass the backward loop multiplies at star k), papx[k] = Phi_k.
-__global__ void __launch_bounds__(POT_THREADS) k_pot_apply(const Cluster *__restrict__ cls, Tiles tm, Fields f,
-                                                            PotBufs pb, PhiBufs ph)
-{
-    __shared__ double s_w[POT_THREADS / 32];
-    __shared__ double s_lastinv[POT_THREADS / 32];
-    const int2 ct = tm.tiles[blockIdx.x];
-    const Cluster &C = cls[ct.x];
-    if (!counts_ok(C)) return;
-    Scalars *sc = C.sc;
-    const long long N = sc->N_MAX, off = C.off;
-    const long long kstart = N - (long long)ct.y * POT_T;
-    const double *r = f.r + off, *inv_r = f.inv_r + off, *m = f.m + off;
-    const PhiCtl &ctl = ph.ctl[ct.x];
-    const double Mtot = ctl.Mapx, Sm = ctl.Sm;
-    const double *cr = pb.carry + (size_t)blockIdx.x * POT_CARRY;
-    const double Qin = cr[0], Din = cr[1], SmIn = cr[2];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    double q[POT_ITEMS], inv[POT_ITEMS], mm[POT_ITEMS];
-#pragma unroll
-    for (int i = 0; i < POT_ITEMS; ++i) {
-        const long long k = kstart - POT_ITEMS * t - i;
-        q[i] = (k >= 1) ? pb.q[off + k] : 0.0;
-        inv[i] = (k >= 1) ? inv_r[k] : 0.0;
-        mm[i] = (k >= 1) ? m[k] : 0.0;
-    }
-    double up = __shfl_up_sync(0xffffffffu, inv[POT_ITEMS - 1], 1);
-    if (lane == 31) s_lastinv[w] = inv[POT_ITEMS - 1];
-    __syncthreads();
-    if (lane == 0) up = (w > 0) ? s_lastinv[w - 1] : r_next_inv(r, kstart, N);
-    double tq = 0.0, tmm = 0.0;
-#pragma unroll
-    for (int i = 0; i < POT_ITEMS; ++i) {
-        tq += q[i];
-        tmm += mm[i];
-    }
-    const double qex = block_excl_prefix<POT_THREADS>(tq, s_w);
-    const double mex = block_excl_prefix<POT_THREADS>(tmm, s_w);
-    double dk[POT_ITEMS], run = qex, runm = mex, td = 0.0;
-#pragma unroll
-    for (int i = 0; i < POT_ITEMS; ++i) {
-        const long long k = kstart - POT_ITEMS * t - i;
-        const double innext = (i == 0) ? up : inv[i - 1];
-        const double Mk = (Mtot - Qin) - run;  // mprev when the reference reaches k
-        dk[i] = (k >= 1) ? Mk * (inv[i] - innext) : 0.0;
-        if (k >= 1) {
-            pb.mapx[off + k] = Mk;
-            pb.sapx[off + k] = Sm - (SmIn + runm);
-        }
-        run += q[i];
-        runm += mm[i];
-        td += dk[i];
-    }
-    const double dex = block_excl_prefix<POT_THREADS>(td, s_w);
-    double acc = Din + dex;
-#pragma unroll
-    for (int i = 0; i < POT_ITEMS; ++i) {
-        const long long k = kstart - POT_ITEMS * t - i;
-        acc += dk[i];
-        if (k >= 1) pb.papx[off + k] = -acc;
     }
 }
 

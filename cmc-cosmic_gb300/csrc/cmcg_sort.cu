@@ -14,11 +14,14 @@
 // in full-key order as the payload moves (runs are a star or two at the
 // densities of these clusters; the escapers' run is equal keys, already in
 // order).
+//   k_sort_prep      the key range and kept count per cluster; clears the
+//                    sort's counters
 //   k_sort_ghist     every 8-bit digit's histogram in one read of the keys
-//   k_sort_onesweep  one kernel per digit pass: stable in-tile ranking (warp
-//                    match + per-warp counters), tile offsets by decoupled
-//                    look-back, staging through shared memory so runs of one
-//                    digit leave the block as contiguous stores
+//   k_sort_onesweep  one kernel per digit pass over tiles of 4096 (default),
+//                    2048 or 1024 keys: stable in-tile ranking (warp match +
+//                    per-warp counters), tile offsets by decoupled look-back,
+//                    staging through shared memory so runs of one digit leave
+//                    the block as contiguous stores
 // Tiles never straddle clusters, so one launch sorts every cluster of an
 // ensemble independently.
 // The radii (pass 0, the histograms, the key range) and the keys and values of
@@ -140,7 +143,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_prep(const Cluster *__res
             sc->n_bound = n;
             // sort keys: a bound star's bit pattern minus the smallest one; the
             // digit passes sort the top SORT_PREFIX_BITS bits of the range
-            // (bits below the shift are left to k_sort_fix).  Escapers all take
+            // (bits below the shift are left to the run placement).  Escapers all take
             // the first key of the prefix after the largest bound key's: they
             // sort after every bound star as a run of equal keys of their own,
             // which the stable passes leave in input order.

@@ -320,6 +320,23 @@ __device__ __forceinline__ float d2f_rn(double x)
     return hi;
 }
 
+// (double)x, which is exact, assembled from x's bits with integer
+// instructions for normal floats and zeros (the FP64 conversion takes the
+// FP64 pipe); subnormals, infinities and NaN go through the conversion.
+__device__ __forceinline__ double f2d_exact(float x)
+{
+    const unsigned int u = __float_as_uint(x);
+    const unsigned int e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+    if (e == 0u) {
+        if ((u & 0x7fffffu) == 0u) return __longlong_as_double((long long)sgn);  // +-0
+        return (double)x;
+    }
+    if (e == 0xffu) return (double)x;
+    return __longlong_as_double(
+        (long long)(sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 // FindZero_r, cmc_nr.c:62-82: largest k in [kmin,kmax] with r[k] < x (x > 0),
 // for kmin < kmax (the only way the reference calls it).  The bisection
 // halves a range of at most 2^63, so 64 rounds bound it.

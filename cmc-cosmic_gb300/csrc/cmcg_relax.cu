@@ -169,43 +169,56 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
     }
     const int L = (int)(hi_load - lo_load + 1);
     const int chunk = (L + RELAX_THREADS - 1) / RELAX_THREADS;
-    double accw = 0.0, accm = 0.0;
+    // FP64 window sums, or with FP32 kinematics float sums of float copies (made
+    // with integer instructions, d2f_rn: the FP64 pipe is this kernel's bound)
+    using acc_t = typename std::conditional<FP32, float, double>::type;
+    acc_t *s_wa = reinterpret_cast<acc_t *>(s_w), *s_ma = reinterpret_cast<acc_t *>(s_m);
+    const float madhoc_f = d2f_rn(madhoc);
+    acc_t accw = 0, accm = 0;
     for (int i = tid * chunk; i < L && i < (tid + 1) * chunk; ++i) {
         const long long k = lo_load + i;
-        const double vrk = vr[k], vtk = vt[k];
-        const double mm = m[k] * madhoc;
-        const double w = mm * (sqr(vrk) + sqr(vtk));
-        accw += w;
-        accm += mm;
-        s_w[i] = accw;
-        s_m[i] = accm;
+        if constexpr (FP32) {
+            const float vrk = d2f_rn(vr[k]), vtk = d2f_rn(vt[k]);
+            const float mm = d2f_rn(m[k]) * madhoc_f;
+            accw += mm * (vrk * vrk + vtk * vtk);
+            accm += mm;
+        } else {
+            const double vrk = vr[k], vtk = vt[k];
+            const double mm = m[k] * madhoc;
+            const double w = mm * (sqr(vrk) + sqr(vtk));
+            accw += w;
+            accm += mm;
+        }
+        s_wa[i] = accw;
+        s_ma[i] = accm;
     }
     // exclusive scan of the per-thread totals
     {
-        double xw = accw, xm = accm;
+        acc_t xw = accw, xm = accm;
         const int lane = tid & 31, wid = tid >> 5;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            double yw = __shfl_up_sync(0xffffffffu, xw, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
+            acc_t yw = __shfl_up_sync(0xffffffffu, xw, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
             if (lane >= o) {
                 xw += yw;
                 xm += ym;
             }
         }
+        acc_t(*s_tota)[RELAX_THREADS / 32] = reinterpret_cast<acc_t(*)[RELAX_THREADS / 32]>(s_tot);
         if (lane == 31) {
-            s_tot[0][wid] = xw;
-            s_tot[1][wid] = xm;
+            s_tota[0][wid] = xw;
+            s_tota[1][wid] = xm;
         }
         __syncthreads();
-        double bw = 0.0, bm = 0.0;
+        acc_t bw = 0, bm = 0;
         for (int q = 0; q < wid; ++q) {
-            bw += s_tot[0][q];
-            bm += s_tot[1][q];
+            bw += s_tota[0][q];
+            bm += s_tota[1][q];
         }
-        const double ew = bw + xw - accw, em = bm + xm - accm;  // exclusive offsets
+        const acc_t ew = bw + xw - accw, em = bm + xm - accm;  // exclusive offsets
         for (int i = tid * chunk; i < L && i < (tid + 1) * chunk; ++i) {
-            s_w[i] += ew;
-            s_m[i] += em;
+            s_wa[i] += ew;
+            s_ma[i] += em;
         }
     }
     __syncthreads();
@@ -228,12 +241,15 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                 lo = hi - (2 * p - 1);
             }
             const int a = (int)(lo - lo_load) - 1, b = (int)(hi - lo_load);
-            const double Mv2 = s_w[b] - (a >= 0 ? s_w[a] : 0.0);
-            const double Mm = s_m[b] - (a >= 0 ? s_m[a] : 0.0);
+            const acc_t Mv2 = s_wa[b] - (a >= 0 ? s_wa[a] : acc_t(0));
+            const acc_t Mm = s_ma[b] - (a >= 0 ? s_ma[a] : acc_t(0));
             sig_r[si] = r[si];
             // sqrt(Mv2 / Mm) (calc_sigma_r, cmc_dynamics_helper.c:2977) as Mv2 rsqrt(Mv2 Mm): one
             // reciprocal square root for a division and a square root, within 3 ulps
-            sig[si] = Mv2 * rsqrt(Mv2 * Mm);
+            if constexpr (FP32)
+                sig[si] = f2d_exact(Mv2 * rsqrtf(Mv2 * Mm));
+            else
+                sig[si] = Mv2 * rsqrt(Mv2 * Mm);
         }
     }
 
@@ -258,99 +274,143 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
             const double Y = u01(wy);
             f.Y[off + k] = Y;
             f.Y[off + kp] = Y;
-            double v1 = vtk, v2 = 0.0, v3 = vrk, vp1, vp2, vp3 = vrkp, w1, w2, w3, W;
             double vr_k, vt_k, vr_kp, vt_kp;
             bool ok = true;
-            if (!FP32) {
-                double sa, ca;
-                if (TRIG32) {
-                    sincos_2pi_draw(wy, &sa, &ca);  // sin and cos of Y 2 pi on the FP32 pipe (cmcg_fftrig.cuh)
-                } else {
-                    const double ang = Y * 2.0 * CMCG_PI;
-                    sincos(ang, &sa, &ca);
-                }
-                vp1 = vtkp * ca;
-                vp2 = vtkp * sa;
-                w1 = vp1 - v1;
-                w2 = vp2 - v2;
-                w3 = vp3 - v3;
-                W = sqrt(sqr(w1) + sqr(w2) + sqr(w3));
-            } else {
-                const float ang = (float)Y * 2.0f * (float)CMCG_PI;
-                float sa, ca;
-                sincosf(ang, &sa, &ca);
-                vp1 = (double)((float)vtkp * ca);
-                vp2 = (double)((float)vtkp * sa);
-                w1 = (double)((float)vp1 - (float)v1);
-                w2 = (double)((float)vp2);
-                w3 = (double)((float)vp3 - (float)v3);
-                W = (double)sqrtf((float)(w1 * w1 + w2 * w2 + w3 * w3));
-            }
-            if (eq0(W)) {
-                set_error(sc, CMCG_ERR_W_ZERO, k);
-                ok = false;
-            }
-            // the three quotients by m_k + m_kp share one correctly rounded reciprocal (div_rcp)
-            const double msum = mass_k + mass_kp, imsum = __drcp_rn(msum);
-            // S = 0: single-single with SS_COLLISION off, so P_enc = 0 and the
-            // encounter draw (cmc_dynamics.c:406) can never succeed.
-            double beta = 0.0;
-            if (ok && C.RELAXATION) {
-                // beta = (pi/2) sqrt(dt / Trel12) with Trel12 = (pi/32) W^3 / (N_STAR n_local
-                // ((m_k + m_k') madhoc)^2) and n_local = 6p / (4 pi (r_max^3 - r_min^3))
-                // (cmc_dynamics_helper.c:768-786, 831-871): the three quotients as one, within a
-                // few ulps of the reference's beta
-                const double num = dt * NSTAR * (192.0 * (double)p) * sqr(msum * madhoc);
-                const double den = (4.0 * CMCG_PI * CMCG_PI) * window_dr3(r, k, p, N) * cub(W);
-                beta = (CMCG_PI / 2.0) * sqrt(num / den);
-                const double relbeta[4] = {CMCG_PI / 2.0, CMCG_PI / 4.0, CMCG_PI / 8.0, CMCG_PI / 16.0};
-                part[0] += 1.0;
-                if (gt_pos(beta, relbeta[3])) {  // the smallest threshold: ratio and centre formed once per pair
-                    const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
-                    const double rcm = div_rcp(m[k] * r[k] + m[kp] * r[kp], msum, imsum);
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        if (gt_pos(beta, relbeta[i])) {
-                            part[1 + i] += 1.0;
-                            part[5 + i] += qratio;
-                            part[9 + i] += (mass_k + mass_kp) / 2.0;
-                            part[13 + i] += rcm;
-                        }
-                    }
-                }
-                if (gt_pos(beta, CMCG_PI / 2.0)) beta = CMCG_PI / 2.0;
-                const unsigned int wpsi = draw_block(C.seed, tcount, SITE_PSI, idk, 0u).x;
-                if (!FP32) {
-                    const double wp = sqrt(sqr(w1) + sqr(w2));
-                    if (eq0(wp)) {
-                        set_error(sc, CMCG_ERR_WP_ZERO, k);
-                        ok = false;
+            if constexpr (!FP32) {
+                double v1 = vtk, v2 = 0.0, v3 = vrk, vp1, vp2, vp3 = vrkp, w1, w2, w3, W;
+                {
+                    double sa, ca;
+                    if (TRIG32) {
+                        sincos_2pi_draw(wy, &sa, &ca);  // sin and cos of Y 2 pi on the FP32 pipe (cmcg_fftrig.cuh)
                     } else {
-                        const double iwp = __drcp_rn(wp);  // the four quotients by wp (div_rcp)
-                        const double a1 = div_rcp(-w2 * W, wp, iwp), a2 = div_rcp(w1 * W, wp, iwp), a3 = 0.0;
-                        const double b1 = div_rcp(-w1 * w3, wp, iwp), b2 = div_rcp(-w2 * w3, wp, iwp), b3 = wp;
-                        double sb, cb, sp, cp;
-                        if (TRIG32) {
-                            sincos_beta(beta, &sb, &cb);     // cmcg_fftrig.cuh
-                            sincos_2pi_draw(wpsi, &sp, &cp);  // psi = u01 * 2 pi
-                        } else {
-                            const double psi = u01(wpsi) * 2 * CMCG_PI;
-                            sincos(beta, &sb, &cb);
-                            sincos(psi, &sp, &cp);
-                        }
-                        const double wn1 = w1 * cb + a1 * sb * cp + b1 * sb * sp;
-                        const double wn2 = w2 * cb + a2 * sb * cp + b2 * sb * sp;
-                        const double wn3 = w3 * cb + a3 * sb * cp + b3 * sb * sp;
-                        const double fk = div_rcp(mass_kp, msum, imsum), fkp = div_rcp(mass_k, msum, imsum);
-                        const double vn1 = v1 - fk * (wn1 - w1), vn2 = v2 - fk * (wn2 - w2), vn3 = v3 - fk * (wn3 - w3);
-                        const double pn1 = vp1 + fkp * (wn1 - w1), pn2 = vp2 + fkp * (wn2 - w2), pn3 = vp3 + fkp * (wn3 - w3);
-                        vr_k = vn3;
-                        vt_k = sqrt(sqr(vn1) + sqr(vn2));
-                        vr_kp = pn3;
-                        vt_kp = sqrt(sqr(pn1) + sqr(pn2));
+                        const double ang = Y * 2.0 * CMCG_PI;
+                        sincos(ang, &sa, &ca);
                     }
-                } else {
-                    const float fw1 = (float)w1, fw2 = (float)w2, fw3 = (float)w3, fW = (float)W;
+                    vp1 = vtkp * ca;
+                    vp2 = vtkp * sa;
+                    w1 = vp1 - v1;
+                    w2 = vp2 - v2;
+                    w3 = vp3 - v3;
+                    W = sqrt(sqr(w1) + sqr(w2) + sqr(w3));
+                }
+                if (eq0(W)) {
+                    set_error(sc, CMCG_ERR_W_ZERO, k);
+                    ok = false;
+                }
+                // the three quotients by m_k + m_kp share one correctly rounded reciprocal (div_rcp)
+                const double msum = mass_k + mass_kp, imsum = __drcp_rn(msum);
+                // S = 0: single-single with SS_COLLISION off, so P_enc = 0 and the
+                // encounter draw (cmc_dynamics.c:406) can never succeed.
+                double beta = 0.0;
+                if (ok && C.RELAXATION) {
+                    // beta = (pi/2) sqrt(dt / Trel12) with Trel12 = (pi/32) W^3 / (N_STAR n_local
+                    // ((m_k + m_k') madhoc)^2) and n_local = 6p / (4 pi (r_max^3 - r_min^3))
+                    // (cmc_dynamics_helper.c:768-786, 831-871): the three quotients as one, within a
+                    // few ulps of the reference's beta
+                    const double num = dt * NSTAR * (192.0 * (double)p) * sqr(msum * madhoc);
+                    const double den = (4.0 * CMCG_PI * CMCG_PI) * window_dr3(r, k, p, N) * cub(W);
+                    beta = (CMCG_PI / 2.0) * sqrt(num / den);
+                    const double relbeta[4] = {CMCG_PI / 2.0, CMCG_PI / 4.0, CMCG_PI / 8.0, CMCG_PI / 16.0};
+                    part[0] += 1.0;
+                    if (gt_pos(beta, relbeta[3])) {  // the smallest threshold: ratio and centre formed once per pair
+                        const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
+                        const double rcm = div_rcp(m[k] * r[k] + m[kp] * r[kp], msum, imsum);
+    #pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            if (gt_pos(beta, relbeta[i])) {
+                                part[1 + i] += 1.0;
+                                part[5 + i] += qratio;
+                                part[9 + i] += (mass_k + mass_kp) / 2.0;
+                                part[13 + i] += rcm;
+                            }
+                        }
+                    }
+                    if (gt_pos(beta, CMCG_PI / 2.0)) beta = CMCG_PI / 2.0;
+                    const unsigned int wpsi = draw_block(C.seed, tcount, SITE_PSI, idk, 0u).x;
+                    {
+                        const double wp = sqrt(sqr(w1) + sqr(w2));
+                        if (eq0(wp)) {
+                            set_error(sc, CMCG_ERR_WP_ZERO, k);
+                            ok = false;
+                        } else {
+                            const double iwp = __drcp_rn(wp);  // the four quotients by wp (div_rcp)
+                            const double a1 = div_rcp(-w2 * W, wp, iwp), a2 = div_rcp(w1 * W, wp, iwp), a3 = 0.0;
+                            const double b1 = div_rcp(-w1 * w3, wp, iwp), b2 = div_rcp(-w2 * w3, wp, iwp), b3 = wp;
+                            double sb, cb, sp, cp;
+                            if (TRIG32) {
+                                sincos_beta(beta, &sb, &cb);     // cmcg_fftrig.cuh
+                                sincos_2pi_draw(wpsi, &sp, &cp);  // psi = u01 * 2 pi
+                            } else {
+                                const double psi = u01(wpsi) * 2 * CMCG_PI;
+                                sincos(beta, &sb, &cb);
+                                sincos(psi, &sp, &cp);
+                            }
+                            const double wn1 = w1 * cb + a1 * sb * cp + b1 * sb * sp;
+                            const double wn2 = w2 * cb + a2 * sb * cp + b2 * sb * sp;
+                            const double wn3 = w3 * cb + a3 * sb * cp + b3 * sb * sp;
+                            const double fk = div_rcp(mass_kp, msum, imsum), fkp = div_rcp(mass_k, msum, imsum);
+                            const double vn1 = v1 - fk * (wn1 - w1), vn2 = v2 - fk * (wn2 - w2), vn3 = v3 - fk * (wn3 - w3);
+                            const double pn1 = vp1 + fkp * (wn1 - w1), pn2 = vp2 + fkp * (wn2 - w2), pn3 = vp3 + fkp * (wn3 - w3);
+                            vr_k = vn3;
+                            vt_k = sqrt(sqr(vn1) + sqr(vn2));
+                            vr_kp = pn3;
+                            vt_kp = sqrt(sqr(pn1) + sqr(pn2));
+                        }
+                    }
+                    if (ok) {
+                        vr_o[k] = vr_k;
+                        vt_o[k] = vt_k;
+                        vr_o[kp] = vr_kp;
+                        vt_o[kp] = vt_kp;
+                        // set_star_EJ, cmc_dynamics_helper.c:878-882 (FP64 energies)
+                        f.E[off + k] = phi[k] + 0.5 * (sqr(vr_k) + sqr(vt_k));
+                        f.J[off + k] = r[k] * vt_k;
+                        f.E[off + kp] = phi[kp] + 0.5 * (sqr(vr_kp) + sqr(vt_kp));
+                        f.J[off + kp] = r[kp] * vt_kp;
+                    }
+                }
+            } else {
+                // FP32 kinematics with FP64 energies: the velocities as floats made with
+                // integer instructions (d2f_rn), W, beta and the deflection in float; the
+                // FP64 pipe keeps only the window's r^3 difference (which cancels), the
+                // rare statistics branch and the energies
+                const float fvtk = d2f_rn(vtk), fvrk = d2f_rn(vrk), fvtkp = d2f_rn(vtkp), fvrkp = d2f_rn(vrkp);
+                float sa, ca;
+                sincosf(__uint2float_rn(wy) * 0x1p-32f * 2.0f * (float)CMCG_PI, &sa, &ca);  // (float)Y 2 pi
+                const float fvp1 = fvtkp * ca, fvp2 = fvtkp * sa;
+                const float fw1 = fvp1 - fvtk, fw2 = fvp2, fw3 = fvrkp - fvrk;
+                const float fW = sqrtf(fw1 * fw1 + fw2 * fw2 + fw3 * fw3);
+                if (fW == 0.0f) {
+                    set_error(sc, CMCG_ERR_W_ZERO, k);
+                    ok = false;
+                }
+                if (ok && C.RELAXATION) {
+                    // beta as in the FP64 path (one quotient), in float
+                    const float fmk = d2f_rn(mass_k), fmkp = d2f_rn(mass_kp), msum_f = fmk + fmkp;
+                    const float mmf = msum_f * madhoc_f;
+                    const float num = d2f_rn(dt) * d2f_rn(NSTAR) * (192.0f * (float)p) * (mmf * mmf);
+                    const float den =
+                        (4.0f * (float)CMCG_PI * (float)CMCG_PI) * d2f_rn(window_dr3(r, k, p, N)) * (fW * fW * fW);
+                    float beta = ((float)CMCG_PI / 2.0f) * sqrtf(num / den);
+                    const float relbeta[4] = {(float)(CMCG_PI / 2.0), (float)(CMCG_PI / 4.0), (float)(CMCG_PI / 8.0),
+                                              (float)(CMCG_PI / 16.0)};
+                    part[0] += 1.0;
+                    if (beta > relbeta[3]) {  // the smallest threshold: ratio and centre formed once per pair
+                        const double msum = mass_k + mass_kp;
+                        const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
+                        const double rcm = (m[k] * r[k] + m[kp] * r[kp]) / msum;
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            if (beta > relbeta[i]) {
+                                part[1 + i] += 1.0;
+                                part[5 + i] += qratio;
+                                part[9 + i] += msum / 2.0;
+                                part[13 + i] += rcm;
+                            }
+                        }
+                    }
+                    if (beta > relbeta[0]) beta = relbeta[0];
+                    const unsigned int wpsi = draw_block(C.seed, tcount, SITE_PSI, idk, 0u).x;
                     const float wp = sqrtf(fw1 * fw1 + fw2 * fw2);
                     if (wp == 0.0f) {
                         set_error(sc, CMCG_ERR_WP_ZERO, k);
@@ -360,31 +420,30 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                         const float a1 = -fw2 * fW * iwp, a2 = fw1 * fW * iwp;
                         const float b1 = -fw1 * fw3 * iwp, b2 = -fw2 * fw3 * iwp, b3 = wp;
                         float sb, cb, sp, cp;
-                        const float psi = (float)(u01(wpsi) * 2 * CMCG_PI);
-                        sincosf((float)beta, &sb, &cb);
-                        sincosf(psi, &sp, &cp);
+                        sincosf(beta, &sb, &cb);
+                        sincosf(__uint2float_rn(wpsi) * 0x1p-32f * 2.0f * (float)CMCG_PI, &sp, &cp);  // psi
                         const float d1 = fw1 * (cb - 1.0f) + a1 * sb * cp + b1 * sb * sp;
                         const float d2 = fw2 * (cb - 1.0f) + a2 * sb * cp + b2 * sb * sp;
                         const float d3 = fw3 * (cb - 1.0f) + b3 * sb * sp;
-                        const float fk = (float)(mass_kp / (mass_k + mass_kp)), fkp = 1.0f - fk;
-                        const float vn1 = (float)v1 - fk * d1, vn2 = -fk * d2, vn3 = (float)v3 - fk * d3;
-                        const float pn1 = (float)vp1 + fkp * d1, pn2 = (float)vp2 + fkp * d2, pn3 = (float)vp3 + fkp * d3;
-                        vr_k = (double)vn3;
-                        vt_k = (double)sqrtf(vn1 * vn1 + vn2 * vn2);
-                        vr_kp = (double)pn3;
-                        vt_kp = (double)sqrtf(pn1 * pn1 + pn2 * pn2);
+                        const float fk = fmkp / msum_f, fkp = 1.0f - fk;
+                        const float vn1 = fvtk - fk * d1, vn2 = -fk * d2, vn3 = fvrk - fk * d3;
+                        const float pn1 = fvp1 + fkp * d1, pn2 = fvp2 + fkp * d2, pn3 = fvrkp + fkp * d3;
+                        vr_k = f2d_exact(vn3);
+                        vt_k = f2d_exact(sqrtf(vn1 * vn1 + vn2 * vn2));
+                        vr_kp = f2d_exact(pn3);
+                        vt_kp = f2d_exact(sqrtf(pn1 * pn1 + pn2 * pn2));
                     }
-                }
-                if (ok) {
-                    vr_o[k] = vr_k;
-                    vt_o[k] = vt_k;
-                    vr_o[kp] = vr_kp;
-                    vt_o[kp] = vt_kp;
-                    // set_star_EJ, cmc_dynamics_helper.c:878-882 (FP64 energies)
-                    f.E[off + k] = phi[k] + 0.5 * (sqr(vr_k) + sqr(vt_k));
-                    f.J[off + k] = r[k] * vt_k;
-                    f.E[off + kp] = phi[kp] + 0.5 * (sqr(vr_kp) + sqr(vt_kp));
-                    f.J[off + kp] = r[kp] * vt_kp;
+                    if (ok) {
+                        vr_o[k] = vr_k;
+                        vt_o[k] = vt_k;
+                        vr_o[kp] = vr_kp;
+                        vt_o[kp] = vt_kp;
+                        // set_star_EJ, cmc_dynamics_helper.c:878-882 (FP64 energies)
+                        f.E[off + k] = phi[k] + 0.5 * (sqr(vr_k) + sqr(vt_k));
+                        f.J[off + k] = r[k] * vt_k;
+                        f.E[off + kp] = phi[kp] + 0.5 * (sqr(vr_kp) + sqr(vt_kp));
+                        f.J[off + kp] = r[kp] * vt_kp;
+                    }
                 }
             }
             if (!ok || !C.RELAXATION) {

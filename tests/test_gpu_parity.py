@@ -110,7 +110,8 @@ def test_dynamics_with_sines_on_the_fp32_pipe(gpulib, orc, model, N, imf):
 @pytest.mark.parametrize("model,N,imf", CASES[:2])
 def test_dynamics_fp32_kinematics_error(gpulib, orc, model, N, imf):
     """FP32 relaxation kinematics with FP64 energies: the error of each output
-    against the FP64 oracle, relative to the star's speed (velocities) or value."""
+    against the FP64 oracle, relative to the star's speed (velocities) or value;
+    the velocity dispersion of the sliding windows (calc_sigma_r) too."""
     ic, o, g = _init(model, N, imf)
     g32 = gpulib.Context([N], gpulib.default_params(orbit_r=ic["rtid"], seed=12345, relax_fp32=1))
     g32.load(0, ic["r"], ic["m"], ic["vr"], ic["vt"], ic["id"])
@@ -127,9 +128,14 @@ def test_dynamics_fp32_kinematics_error(gpulib, orc, model, N, imf):
     err_v = max(np.max(np.abs(g32.get("vr_rel") - vro) / speed), np.max(np.abs(g32.get("vt_rel") - vto) / speed))
     err_E = max_rel(g32.get("E"), o.get("E"))
     err_J = np.max(np.abs(g32.get("J") - o.get("J")) / (o.get("star_r")[1:N + 1] * speed))
+    # the window's velocity dispersion, summed in float with FP32 kinematics
+    err_s = max_rel(g32.get("sigma")[1:N + 1], o.get("sigma")[1:N + 1])
+    print(f"\nFP32 kinematics against FP64: v {err_v:.2e} of the speed, E {err_E:.2e}, J {err_J:.2e}, "
+          f"sigma {err_s:.2e}")
     # measured on the GB300: velocities ~2e-6 of the speed, E ~3e-6 (FP32
     # deflection of nearly parallel velocities); the bound holds them to 1e-5
-    assert err_v <= 1e-5 and err_E <= 1e-5 and err_J <= 1e-5, (err_v, err_E, err_J)
+    assert err_v <= 1e-5 and err_E <= 1e-5 and err_J <= 1e-5 and err_s <= 1e-5, (err_v, err_E, err_J, err_s)
+    assert np.array_equal(g32.get("sigma_r")[1:N + 1], o.get("sigma_r")[1:N + 1])
     assert np.array_equal(g32.get("Y"), o.get("Y"))
     g32.close()
 

@@ -57,7 +57,9 @@ __device__ __forceinline__ void block_sums(double (&v)[K], double (*smem)[K] /* 
 #pragma unroll
     for (int i = 0; i < K; ++i) {
         double x = v[i];
-        if (__any_sync(0xffffffffu, x != 0.0)) {
+        // x != 0.0 (NaN included), decided on the bits: an FP64 comparison
+        // would take the FP64 pipe once per column and thread
+        if (__any_sync(0xffffffffu, ((unsigned long long)__double_as_longlong(x) << 1) != 0ull)) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) x = __dadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
         }

@@ -226,6 +226,7 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
     double part[RELAX_NPART];
 #pragma unroll
     for (int i = 0; i < RELAX_NPART; ++i) part[i] = 0.0;
+    int relaxed = 0;  // this thread's pair was relaxed (Nrel, part[0]: counted without the FP64 pipe)
 
     if (live) {
         double *sig_r = f.sigma_r + off, *sig = f.sigma + off;
@@ -311,7 +312,7 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                     const double den = (4.0 * CMCG_PI * CMCG_PI) * window_dr3(r, k, p, N) * cub(W);
                     beta = (CMCG_PI / 2.0) * sqrt(num / den);
                     const double relbeta[4] = {CMCG_PI / 2.0, CMCG_PI / 4.0, CMCG_PI / 8.0, CMCG_PI / 16.0};
-                    part[0] += 1.0;
+                    relaxed = 1;
                     if (gt_pos(beta, relbeta[3])) {  // the smallest threshold: ratio and centre formed once per pair
                         const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
                         const double rcm = div_rcp(m[k] * r[k] + m[kp] * r[kp], msum, imsum);
@@ -394,7 +395,7 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
                     float beta = ((float)CMCG_PI / 2.0f) * sqrtf(num / den);
                     const float relbeta[4] = {(float)(CMCG_PI / 2.0), (float)(CMCG_PI / 4.0), (float)(CMCG_PI / 8.0),
                                               (float)(CMCG_PI / 16.0)};
-                    part[0] += 1.0;
+                    relaxed = 1;
                     if (beta > relbeta[3]) {  // the smallest threshold: ratio and centre formed once per pair
                         const double msum = mass_k + mass_kp;
                         const double qratio = fmax(mass_k, mass_kp) / fmin(mass_k, mass_kp);
@@ -458,9 +459,11 @@ static __device__ __forceinline__ void relax_body(const Cluster *__restrict__ cl
     // ---- statistics (cmc_dynamics.c:430-440), deterministic block order
     __shared__ int s_last;
     __shared__ double s_part[RELAX_THREADS / 32][RELAX_NPART];
+    const int nrel = __syncthreads_count(relaxed);  // one pair per thread
     block_sums<RELAX_THREADS>(part, s_part);  // most columns are zero over most warps
     if (tid == 0) {
         double *slot = partials + (size_t)blockIdx.x * RELAX_NPART;
+        part[0] = (double)nrel;
         for (int i = 0; i < RELAX_NPART; ++i) slot[i] = part[i];
     }
     if (block_arrive_last(tickets + ct.x, tm.count[ct.x], &s_last)) {

@@ -112,7 +112,6 @@ struct cmcg_ctx {
     double *d_query = nullptr;
     DiagDev *d_diag = nullptr;
     TileTable t128, t256, t1024, t2048, t4096;  // t4096: the 4096-key digit passes
-    TileTable tcl;  // one tile per cluster
     void *arena = nullptr;
     size_t arena_bytes = 0;
     int relax_fp32 = 0, relax_trig32 = 0;
@@ -299,8 +298,8 @@ static int carve_all(cmcg_ctx *c, char *base, std::vector<int2> *tabs, size_t *b
     c->d_cls = cv.take<Cluster>(c->ncl);
     c->d_query = cv.take<double>(2);
     c->d_diag = cv.take<DiagDev>(1);
-    TileTable *tts[6] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t4096, &c->tcl};
-    for (int i = 0; i < 6; ++i) {
+    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t4096};
+    for (int i = 0; i < 5; ++i) {
         tts[i]->d_tiles = cv.take<int2>(tabs[i].size());
         tts[i]->d_first = cv.take<int>(c->ncl);
         tts[i]->d_count = cv.take<int>(c->ncl);
@@ -439,13 +438,12 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         c->ridx_total += ridx_buckets(capacity[k]) + 1;
         c->ridx_Bmax = std::max(c->ridx_Bmax, ridx_buckets(capacity[k]));
     }
-    std::vector<int2> tabs[6];
+    std::vector<int2> tabs[5];
     build_table(c->t128, c->cap, ORB_T, tabs[0]);
     build_table(c->t256, c->cap, RELAX_T, tabs[1]);
     build_table(c->t1024, c->cap, POT_T, tabs[2]);
     build_table(c->t2048, c->cap, SORT_T, tabs[3]);
     build_table(c->t4096, c->cap, 4096, tabs[4]);
-    build_table(c->tcl, c->cap, 1 << 30, tabs[5]);
     size_t bytes = 0;
     carve_all(c, nullptr, tabs, &bytes);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -492,8 +490,8 @@ int cmcg_create(cmcg_ctx **out, int nclusters, const long *capacity, const cmcg_
         ridx_off += C.ridx_B + 1;
     }
     CK(cudaMemcpyAsync(c->d_cls, c->h_cls.data(), nclusters * sizeof(Cluster), cudaMemcpyHostToDevice, c->stream));
-    TileTable *tts[6] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t4096, &c->tcl};
-    for (int i = 0; i < 6; ++i) {
+    TileTable *tts[5] = {&c->t128, &c->t256, &c->t1024, &c->t2048, &c->t4096};
+    for (int i = 0; i < 5; ++i) {
         CK(cudaMemcpyAsync(tts[i]->d_tiles, tabs[i].data(), tabs[i].size() * sizeof(int2), cudaMemcpyHostToDevice,
                            c->stream));
         CK(cudaMemcpyAsync(tts[i]->d_first, tts[i]->first.data(), nclusters * sizeof(int), cudaMemcpyHostToDevice,
@@ -959,9 +957,11 @@ static int L_sort(cmcg_ctx *c)
         const TileTable &gt = gv == 1 ? c->t128 : gv == 2 ? c->t1024 : c->t256;
         launch_sort_gather(gv == 1 ? 128 : gv == 2 ? 1024 : 256, gt.ntiles, c->stream, c->d_cls, gt.view(), c->f, c->sb);
     }
-    // one block per cluster: long runs are rare (its grid was mostly idle blocks)
-    k_sort_fix_long<<<c->tcl.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->tcl.view(), c->sb, c->f,
-                                                                    c->tickets);
+    // the long runs spread over the cluster's 2048-key tiles: at 10^8 stars, with
+    // ~6 stars to a 24-bit prefix, runs longer than FIX_SHORT number in the
+    // thousands (one block per cluster took 9 s a step there)
+    k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb, c->f,
+                                                                      c->tickets);
     fam_end(c);
     c->launches += 4 + SORT_MAX_PASSES;
     swap_sorted(c);

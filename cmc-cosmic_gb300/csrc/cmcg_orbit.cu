@@ -74,8 +74,10 @@ static __device__ __forceinline__ int fq_sign(const OrbitCtx &o, long long k)
 // round can probe while this round's probe is in flight, so that the next
 // probe finds its sector in L2 instead of waiting on DRAM.  At 10^7 stars the
 // orbit kernel took 11.16 against 11.38 ms a step with them; at 10^6 stars,
-// where the tables sit in L2, the extra L2 requests cost 4.6%.
-constexpr long long PREFETCH_MIN_STARS = 1ll << 22;
+// where the tables sit in L2, the extra L2 requests cost 4.6%, and at 10^8
+// stars, where the unused half of the prefetched sectors competes for DRAM
+// bandwidth, 202 against 138 ms: hence both bounds.
+constexpr long long PREFETCH_MIN_STARS = 1ll << 22, PREFETCH_MAX_STARS = 1ll << 24;
 static __device__ __forceinline__ void prefetch_l2(const void *p)
 {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
@@ -91,7 +93,7 @@ static __device__ long long find_zero_Q(const OrbitCtx &o, long long kmin, long 
 {
     const int smin = fq_sign(o, kmin), smax = fq_sign(o, kmax);
     const bool up = (smin != smax) ? (smin < smax) : (fq(o, kmin) < fq(o, kmax));
-    const bool pf = o.N_MAX >= PREFETCH_MIN_STARS;
+    const bool pf = o.N_MAX >= PREFETCH_MIN_STARS && o.N_MAX < PREFETCH_MAX_STARS;
     int it = 0;
     if (up) {
         do {

@@ -957,10 +957,10 @@ static int L_sort(cmcg_ctx *c)
         const TileTable &gt = gv == 1 ? c->t128 : gv == 2 ? c->t1024 : c->t256;
         launch_sort_gather(gv == 1 ? 128 : gv == 2 ? 1024 : 256, gt.ntiles, c->stream, c->d_cls, gt.view(), c->f, c->sb);
     }
-    // the long runs spread over the cluster's 2048-key tiles: at 10^8 stars, with
+    // the long runs spread over the cluster's 4096-key tiles: at 10^8 stars, with
     // ~6 stars to a 24-bit prefix, runs longer than FIX_SHORT number in the
     // thousands (one block per cluster took 9 s a step there)
-    k_sort_fix_long<<<c->t2048.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t2048.view(), c->sb, c->f,
+    k_sort_fix_long<<<c->t4096.ntiles, SORT_THREADS, 0, c->stream>>>(c->d_cls, c->t4096.view(), c->sb, c->f,
                                                                       c->tickets);
     fam_end(c);
     c->launches += 4 + SORT_MAX_PASSES;

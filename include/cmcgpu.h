@@ -321,10 +321,13 @@ int cmcg_step_host(cmcg_ctx *ctx, const cmcg_stars *in, cmcg_stars *out);
 
 /* ------------------------------------------------------- autotuner -----
  * Launch variants with bit-identical results, chosen by measurement on the
- * context's own clusters: "orbit" and "relax" (5 or 4 blocks per SM, i.e.
- * register budgets of 102 or 128), "orbit_learn" (the same for the learned
- * sampling pass) and "mlp_grid" (persistent CTAs per SM of the network's
- * inference: 4, 2, 3, 6).  cmcg_autotune times every variant of the
+ * context's own clusters: "orbit" (5 or 4 blocks per SM, i.e. register
+ * budgets of 102 or 128, each also as a persistent grid: variants 0-3),
+ * "relax" (5 or 4 blocks per SM), "orbit_learn" (the same for the learned
+ * sampling pass), "mlp_grid" (persistent CTAs per SM of the network's
+ * inference: 4, 2, 3, 6), "sort_tile" (keys per tile of the radius sort's
+ * digit passes: 4096, 2048, 1024) and "gather_tile" (stars per block of the
+ * sort's payload gather: 256, 128, 1024).  cmcg_autotune times every variant of the
  * launches the current configuration uses over `steps` steps each (plus one
  * untimed step), keeps the fastest, and writes a one-line report (may be
  * NULL).  The tuning steps are real steps of the run. */

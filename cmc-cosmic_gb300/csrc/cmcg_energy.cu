@@ -1,6 +1,7 @@
 // cmcg_energy.cu -- step bookkeeping on the device.
 //
-// k_begin_step   cmc.c:246-257 (tallies of the previous step move to *_old)
+// k_begin_step   cmc.c:246-257 (tallies of the previous step move to *_old);
+//                a whole step does this in k_timestep's last block
 // k_ec3 + k_ec3_fix   set_velocities3 (cmc_utils.c:254-349).  The per-star
 //     prediction v_new^2 = vold^2 + (Uoldrold - Uoldrnew) + (Unewrold - Unewrnew)
 //     and the velocity rescaling are independent per star (k_ec3).  Only the
@@ -9,7 +10,8 @@
 //     them in a list and k_ec3_fix replays exactly the reference's sequential
 //     loop from each of them until the excess is used up.
 // k_energy       compute_energy_new + ComputeEnergy (cmc_utils.c:2018-2028, 604-656)
-// k_end_step     tcount++, Prev_Dt (cmc.c:294, 390)
+// k_end_step     tcount++, Prev_Dt (cmc.c:294, 390); a whole step does this
+//                in k_energy's last block
 #include "cmcg_kernels.cuh"
 #include "cmcgpu.h"
 
